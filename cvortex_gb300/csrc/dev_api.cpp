@@ -1,0 +1,168 @@
+// dev_api.cpp -- device-pointer extension API (cvtx_gb300_dev_*).
+//
+// For callers whose particles already live in GPU memory (a time-stepping
+// solver, a serving loop, a framework tensor): no gather, no host copies, the
+// kernels run on the caller's stream. Split-source partial sums use the
+// active context's workspace; successive calls are ordered on the workspace
+// through an event so that calls on different streams do not overlap on it.
+#include <string>
+
+#include "cvortex/cvtx_gb300.h"
+#include "nbody.h"
+#include "runtime.h"
+
+namespace cvtx {
+namespace {
+
+struct DevCall {
+	std::lock_guard<std::recursive_mutex> lock;
+	DeviceContext* ctx;
+	cudaStream_t stream;
+	explicit DevCall(void* s)
+		: lock(Runtime::get().lock()), ctx(Runtime::get().active_context()),
+		  stream(static_cast<cudaStream_t>(s)) {}
+
+	// Serialise workspace users across streams.
+	int prepare(size_t ws_bytes, const char* what) {
+		if (!ctx) return -3;
+		cudaError_t e = ctx->ensure_ws(ws_bytes);
+		if (e == cudaSuccess && ws_event()) e = cudaStreamWaitEvent(stream, ws_event(), 0);
+		if (e != cudaSuccess) {
+			set_error(std::string(what) + ": " + cudaGetErrorString(e));
+			return -2;
+		}
+		return 0;
+	}
+	int done(cudaError_t e, const char* what) {
+		if (e == cudaSuccess && ws_event()) e = cudaEventRecord(ws_event(), stream);
+		if (e != cudaSuccess) {
+			set_error(std::string(what) + ": " + cudaGetErrorString(e));
+			return -2;
+		}
+		return 0;
+	}
+	LaunchEnv env() const {
+		LaunchEnv v = ctx->env();
+		v.stream = stream;
+		return v;
+	}
+	cudaEvent_t ws_event() {
+		static cudaEvent_t ev = nullptr;
+		if (!ev && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) ev = nullptr;
+		return ev;
+	}
+};
+
+bool bad_reg(int reg) { return reg < 0 || reg > 3; }
+
+}  // namespace
+}  // namespace cvtx
+
+using namespace cvtx;
+
+extern "C" {
+
+CVTX_EXPORT int cvtx_gb300_dev_P3D_M2M(const void* src, int n_src, const void* tgt,
+	int tgt_stride, int n_tgt, float* vel_out, float* dvort_out, int reg, float sigma,
+	void* stream)
+{
+	if (n_tgt <= 0) return 0;
+	if (n_src < 0 || !tgt || bad_reg(reg) || (!vel_out && !dvort_out) || tgt_stride < 1)
+		return -1;
+	if (dvort_out && tgt_stride < 2) return -1;
+	DevCall c(stream);
+	const unsigned ops = (vel_out ? kOpVel : 0u) | (dvort_out ? kOpDvort : 0u);
+	int st = c.prepare(p3d_induce_ws_bytes(reg, ops, n_src, n_tgt, c.ctx ? c.ctx->num_sms : 1),
+		"cvtx_gb300_dev_P3D_M2M");
+	if (st) return st;
+	P3DInduceProblem p;
+	p.src = static_cast<const float4*>(src); p.n_src = n_src;
+	p.tgt = static_cast<const float4*>(tgt); p.tstride = tgt_stride; p.n_tgt = n_tgt;
+	p.out_vel = vel_out; p.out_dvort = dvort_out; p.sigma = sigma;
+	return c.done(p3d_induce(reg, ops, p, c.env()), "cvtx_gb300_dev_P3D_M2M");
+}
+
+CVTX_EXPORT int cvtx_gb300_dev_P3D_M2M_visc(const void* src, int n_src, const void* tgt,
+	int tgt_stride, int n_tgt, float* out, int reg, float sigma, float nu, void* stream)
+{
+	if (n_tgt <= 0) return 0;
+	if (n_src < 0 || !tgt || !out || bad_reg(reg) || tgt_stride < 2) return -1;
+	DevCall c(stream);
+	if (reg == 0 || reg == 2) {
+		if (!c.ctx) return -3;
+		const cudaError_t e = cudaMemsetAsync(out, 0, sizeof(float) * 3 * size_t(n_tgt), c.stream);
+		return e == cudaSuccess ? 0 : -2;
+	}
+	int st = c.prepare(p3d_visc_ws_bytes(reg, n_src, n_tgt, c.ctx ? c.ctx->num_sms : 1),
+		"cvtx_gb300_dev_P3D_M2M_visc");
+	if (st) return st;
+	P3DViscProblem p;
+	p.src = static_cast<const float4*>(src); p.n_src = n_src;
+	p.tgt = static_cast<const float4*>(tgt); p.tstride = tgt_stride; p.n_tgt = n_tgt;
+	p.out = out; p.sigma = sigma; p.nu = nu;
+	return c.done(p3d_visc(reg, p, c.env()), "cvtx_gb300_dev_P3D_M2M_visc");
+}
+
+CVTX_EXPORT int cvtx_gb300_dev_P2D_M2M_vel(const void* src, int n_src, const void* tgt,
+	int n_tgt, float* out, int reg, float sigma, void* stream)
+{
+	if (n_tgt <= 0) return 0;
+	if (n_src < 0 || !tgt || !out || bad_reg(reg)) return -1;
+	DevCall c(stream);
+	int st = c.prepare(p2d_vel_ws_bytes(reg, n_src, n_tgt, c.ctx ? c.ctx->num_sms : 1),
+		"cvtx_gb300_dev_P2D_M2M_vel");
+	if (st) return st;
+	P2DVelProblem p;
+	p.src = static_cast<const float4*>(src); p.n_src = n_src;
+	p.tgt = static_cast<const float4*>(tgt); p.n_tgt = n_tgt;
+	p.out = out; p.sigma = sigma;
+	return c.done(p2d_vel(reg, p, c.env()), "cvtx_gb300_dev_P2D_M2M_vel");
+}
+
+CVTX_EXPORT int cvtx_gb300_dev_F3D_M2M_vel(const void* fil, int n_fil, const void* tgt,
+	int tgt_stride, int n_tgt, float* out, void* stream)
+{
+	if (n_tgt <= 0) return 0;
+	if (n_fil < 0 || !tgt || !out || tgt_stride < 1) return -1;
+	DevCall c(stream);
+	int st = c.prepare(f3d_vel_ws_bytes(n_fil, n_tgt, c.ctx ? c.ctx->num_sms : 1),
+		"cvtx_gb300_dev_F3D_M2M_vel");
+	if (st) return st;
+	F3DVelProblem p;
+	p.fil = static_cast<const float4*>(fil); p.n_fil = n_fil;
+	p.tgt = static_cast<const float4*>(tgt); p.tstride = tgt_stride; p.n_tgt = n_tgt;
+	p.out = out;
+	return c.done(f3d_vel(p, c.env()), "cvtx_gb300_dev_F3D_M2M_vel");
+}
+
+CVTX_EXPORT int cvtx_gb300_dev_pack_P3D(const cvtx_P3D* aos, int n, void* rec, void* stream) {
+	if (n < 0 || (n > 0 && (!aos || !rec))) return -1;
+	return pack_p3d(aos, n, static_cast<float4*>(rec), static_cast<cudaStream_t>(stream)) ==
+		cudaSuccess ? 0 : -2;
+}
+
+CVTX_EXPORT int cvtx_gb300_dev_pack_V3f(const bsv_V3f* pts, int n, void* rec, void* stream) {
+	if (n < 0 || (n > 0 && (!pts || !rec))) return -1;
+	return pack_v3(pts, n, static_cast<float4*>(rec), static_cast<cudaStream_t>(stream)) ==
+		cudaSuccess ? 0 : -2;
+}
+
+// Synchronise `stream`, read and reset the device error word of the active
+// context. Returns 0 if no device-side wait expired since the last check.
+CVTX_EXPORT int cvtx_gb300_dev_status(void* stream) {
+	std::lock_guard<std::recursive_mutex> g(Runtime::get().lock());
+	DeviceContext* c = Runtime::get().active_context();
+	if (!c) return -3;
+	cudaStream_t s = static_cast<cudaStream_t>(stream);
+	unsigned w = 0;
+	if (cudaStreamSynchronize(s) != cudaSuccess) return -2;
+	if (cudaMemcpy(&w, c->d_err, sizeof w, cudaMemcpyDeviceToHost) != cudaSuccess) return -2;
+	if (cudaMemset(c->d_err, 0, sizeof w) != cudaSuccess) return -2;
+	if (w) {
+		set_error("device-side wait expired (code " + std::to_string(w) + ")");
+		return -4;
+	}
+	return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,362 @@
+// f3d.cu -- straight singular vortex filament kernels for sm_103a.
+//
+// Replaces cvtx_nb_Filament_ind_{vel,vel_smes,dvort}_singular (reference
+// src/nbody.cl:611-728) and src/ocl_F3D.cpp. Per-pair arithmetic follows the
+// reference CPU path src/F3D.cpp:34-54 (velocity), :56-85 (vortex
+// stretching) and :204-227 (influence matrix), including its guards: a
+// velocity term is dropped when |t1| or |t2| exceeds FLT_MAX (or is NaN), a
+// stretching term when it contains NaN. For stretching the 1/(4 pi) factor is
+// applied once per target.
+#include <cmath>
+#include "nbody.h"
+#include "plan.cuh"
+#include "regfuncs.cuh"
+#include "tile_stream.cuh"
+
+namespace cvtx {
+namespace {
+
+constexpr int kTile = 256;
+constexpr int kStages = 2;
+using Stream2 = TileStream<2, kTile, kStages>;
+constexpr int kSmallTargets = 8192;
+constexpr double kInv4Pi = 1.0 / (4.0 * 3.14159265358979323846);
+constexpr float kBig = 3.40282346e38f;
+constexpr float kInv4PiF = float(kInv4Pi);
+
+// Velocity induced at m by filament (s -> e) of strength gamma (including the
+// 1/(4 pi) factor, which the reference folds into t1 before its guard).
+__device__ __forceinline__ void f3d_vel_pair(float mx, float my, float mz,
+	const float4 a, const float4 b, float& vx, float& vy, float& vz)
+{
+	const float r1x = mx - a.x, r1y = my - a.y, r1z = mz - a.z;
+	const float r2x = mx - b.x, r2y = my - b.y, r2z = mz - b.z;
+	const float r0x = r1x - r2x, r0y = r1y - r2y, r0z = r1z - r2z;
+	const float cx = fmaf(r1y, r2z, -r1z * r2y);
+	const float cy = fmaf(r1z, r2x, -r1x * r2z);
+	const float cz = fmaf(r1x, r2y, -r1y * r2x);
+	const float cc = fmaf(cz, cz, fmaf(cy, cy, cx * cx));
+	const float t1 = (a.w * kInv4PiF) / cc;
+	const float l1 = rsqrt_approx(fmaf(r1z, r1z, fmaf(r1y, r1y, r1x * r1x)));
+	const float l2 = rsqrt_approx(fmaf(r2z, r2z, fmaf(r2y, r2y, r2x * r2x)));
+	const float t21 = fmaf(r1z, r0z, fmaf(r1y, r0y, r1x * r0x)) * l1;
+	const float t22 = fmaf(r2z, r0z, fmaf(r2y, r0y, r2x * r0x)) * l2;
+	const float t2 = t21 - t22;
+	// |t1| <= FLT_MAX and |t2| <= FLT_MAX; NaN fails both tests.
+	const bool ok = fabsf(t1) <= kBig && fabsf(t2) <= kBig;
+	const float f = ok ? t1 * t2 : 0.f;
+	vx = ok ? cx * f : 0.f;
+	vy = ok ? cy * f : 0.f;
+	vz = ok ? cz * f : 0.f;
+}
+
+template <int TPT, int NT>
+__global__ void __launch_bounds__(NT)
+f3d_vel_kernel(const F3DVelProblem p, double* __restrict__ partial, int src_per_split,
+	unsigned* err)
+{
+	constexpr int NC = 3;
+	extern __shared__ __align__(16) unsigned char smem[];
+	float* hi = reinterpret_cast<float*>(smem + Stream2::kSmemBytes);
+	float* lo = hi + NC * TPT * NT;
+	const int tid = threadIdx.x;
+	const int tbase = blockIdx.x * (TPT * NT);
+	const int s_begin = blockIdx.y * src_per_split;
+	int n_s = p.n_fil - s_begin;
+	n_s = n_s < src_per_split ? n_s : src_per_split;
+	n_s = n_s > 0 ? n_s : 0;
+	float tx[TPT], ty[TPT], tz[TPT];
+#pragma unroll
+	for (int k = 0; k < TPT; ++k) {
+		int t = tbase + k * NT + tid;
+		t = t < p.n_tgt ? t : p.n_tgt - 1;
+		const float4 tp = p.tgt[size_t(t) * p.tstride];
+		tx[k] = tp.x; ty[k] = tp.y; tz[k] = tp.z;
+	}
+#pragma unroll
+	for (int i = 0; i < NC * TPT; ++i) { hi[i * NT + tid] = 0.f; lo[i * NT + tid] = 0.f; }
+	auto tile_fn = [&](const float4* __restrict__ st, int cnt) {
+		float acc[NC][TPT];
+#pragma unroll
+		for (int c = 0; c < NC; ++c)
+#pragma unroll
+			for (int k = 0; k < TPT; ++k) acc[c][k] = 0.f;
+		auto body = [&](int j) {
+			const float4 a = st[2 * j];
+			const float4 b = st[2 * j + 1];
+#pragma unroll
+			for (int k = 0; k < TPT; ++k) {
+				float vx, vy, vz;
+				f3d_vel_pair(tx[k], ty[k], tz[k], a, b, vx, vy, vz);
+				acc[0][k] += vx; acc[1][k] += vy; acc[2][k] += vz;
+			}
+		};
+		if (cnt == kTile) {
+#pragma unroll 2
+			for (int j = 0; j < kTile; ++j) body(j);
+		} else {
+#pragma unroll 1
+			for (int j = 0; j < cnt; ++j) body(j);
+		}
+#pragma unroll
+		for (int c = 0; c < NC; ++c)
+#pragma unroll
+			for (int k = 0; k < TPT; ++k) {
+				const int i = (c * TPT + k) * NT + tid;
+				float h = hi[i], l = lo[i];
+				fold_twosum(h, l, acc[c][k]);
+				hi[i] = h; lo[i] = l;
+			}
+	};
+	if (!Stream2::run(smem, p.fil, s_begin, n_s, err, tile_fn)) return;
+#pragma unroll
+	for (int k = 0; k < TPT; ++k) {
+		const int t = tbase + k * NT + tid;
+		if (t >= p.n_tgt) continue;
+#pragma unroll
+		for (int c = 0; c < NC; ++c) {
+			const int i = (c * TPT + k) * NT + tid;
+			const double s = double(hi[i]) + double(lo[i]);
+			if (gridDim.y == 1) p.out[3 * size_t(t) + c] = float(s);
+			else partial[(size_t(blockIdx.y) * NC + c) * p.n_tgt + t] = s;
+		}
+	}
+}
+
+// Vortex stretching of particle (x, alpha) by filament (s -> e), strength g,
+// without the 1/(4 pi) factor (reference src/F3D.cpp:56-85):
+//   r1 = x - s, r2 = x - e, r0 = r1 - r2, X = |r1 x r0|
+//   A = -r0 / X^2 * g * (r0.r1/|r1| - r0.r2/|r2|)
+//   B = 3/|r0| * g * (X/|r1| - X/|r2|)
+//   out = B alpha + A x alpha
+__device__ __forceinline__ void f3d_dvort_pair(float px, float py, float pz,
+	float wx, float wy, float wz, const float4 a, const float4 b,
+	float& ox, float& oy, float& oz)
+{
+	const float r1x = px - a.x, r1y = py - a.y, r1z = pz - a.z;
+	const float r2x = px - b.x, r2y = py - b.y, r2z = pz - b.z;
+	const float r0x = r1x - r2x, r0y = r1y - r2y, r0z = r1z - r2z;
+	const float xx = fmaf(r1y, r0z, -r1z * r0y);
+	const float xy = fmaf(r1z, r0x, -r1x * r0z);
+	const float xz = fmaf(r1x, r0y, -r1y * r0x);
+	const float X2 = fmaf(xz, xz, fmaf(xy, xy, xx * xx));
+	const float X = sqrtf(X2);
+	const float il1 = rsqrt_approx(fmaf(r1z, r1z, fmaf(r1y, r1y, r1x * r1x)));
+	const float il2 = rsqrt_approx(fmaf(r2z, r2z, fmaf(r2y, r2y, r2x * r2x)));
+	const float il0 = rsqrt_approx(fmaf(r0z, r0z, fmaf(r0y, r0y, r0x * r0x)));
+	const float t212 = fmaf(r0z, r1z, fmaf(r0y, r1y, r0x * r1x)) * il1
+		- fmaf(r0z, r2z, fmaf(r0y, r2y, r0x * r2x)) * il2;
+	const float t222 = X * il1 - X * il2;
+	const float kA = -a.w * t212 / X2;
+	const float Ax = r0x * kA, Ay = r0y * kA, Az = r0z * kA;
+	const float B = 3.f * il0 * a.w * t222;
+	const float vx = fmaf(wx, B, fmaf(Ay, wz, -Az * wy));
+	const float vy = fmaf(wy, B, fmaf(Az, wx, -Ax * wz));
+	const float vz = fmaf(wz, B, fmaf(Ax, wy, -Ay * wx));
+	const bool ok = (vx == vx) && (vy == vy) && (vz == vz) && (t222 == t222) && (t212 == t212);
+	ox = ok ? vx : 0.f;
+	oy = ok ? vy : 0.f;
+	oz = ok ? vz : 0.f;
+}
+
+template <int TPT, int NT>
+__global__ void __launch_bounds__(NT)
+f3d_dvort_kernel(const F3DDvortProblem p, double* __restrict__ partial, int src_per_split,
+	unsigned* err)
+{
+	constexpr int NC = 3;
+	extern __shared__ __align__(16) unsigned char smem[];
+	float* hi = reinterpret_cast<float*>(smem + Stream2::kSmemBytes);
+	float* lo = hi + NC * TPT * NT;
+	const int tid = threadIdx.x;
+	const int tbase = blockIdx.x * (TPT * NT);
+	const int s_begin = blockIdx.y * src_per_split;
+	int n_s = p.n_fil - s_begin;
+	n_s = n_s < src_per_split ? n_s : src_per_split;
+	n_s = n_s > 0 ? n_s : 0;
+	float tx[TPT], ty[TPT], tz[TPT], ax[TPT], ay[TPT], az[TPT];
+#pragma unroll
+	for (int k = 0; k < TPT; ++k) {
+		int t = tbase + k * NT + tid;
+		t = t < p.n_tgt ? t : p.n_tgt - 1;
+		const float4 tp = p.tgt[size_t(t) * p.tstride];
+		const float4 tv = p.tgt[size_t(t) * p.tstride + 1];
+		tx[k] = tp.x; ty[k] = tp.y; tz[k] = tp.z;
+		ax[k] = tv.x; ay[k] = tv.y; az[k] = tv.z;
+	}
+#pragma unroll
+	for (int i = 0; i < NC * TPT; ++i) { hi[i * NT + tid] = 0.f; lo[i * NT + tid] = 0.f; }
+	auto tile_fn = [&](const float4* __restrict__ st, int cnt) {
+		float acc[NC][TPT];
+#pragma unroll
+		for (int c = 0; c < NC; ++c)
+#pragma unroll
+			for (int k = 0; k < TPT; ++k) acc[c][k] = 0.f;
+		auto body = [&](int j) {
+			const float4 a = st[2 * j];
+			const float4 b = st[2 * j + 1];
+#pragma unroll
+			for (int k = 0; k < TPT; ++k) {
+				float vx, vy, vz;
+				f3d_dvort_pair(tx[k], ty[k], tz[k], ax[k], ay[k], az[k], a, b, vx, vy, vz);
+				acc[0][k] += vx; acc[1][k] += vy; acc[2][k] += vz;
+			}
+		};
+		if (cnt == kTile) {
+#pragma unroll 2
+			for (int j = 0; j < kTile; ++j) body(j);
+		} else {
+#pragma unroll 1
+			for (int j = 0; j < cnt; ++j) body(j);
+		}
+#pragma unroll
+		for (int c = 0; c < NC; ++c)
+#pragma unroll
+			for (int k = 0; k < TPT; ++k) {
+				const int i = (c * TPT + k) * NT + tid;
+				float h = hi[i], l = lo[i];
+				fold_twosum(h, l, acc[c][k]);
+				hi[i] = h; lo[i] = l;
+			}
+	};
+	if (!Stream2::run(smem, p.fil, s_begin, n_s, err, tile_fn)) return;
+#pragma unroll
+	for (int k = 0; k < TPT; ++k) {
+		const int t = tbase + k * NT + tid;
+		if (t >= p.n_tgt) continue;
+#pragma unroll
+		for (int c = 0; c < NC; ++c) {
+			const int i = (c * TPT + k) * NT + tid;
+			const double s = double(hi[i]) + double(lo[i]);
+			if (gridDim.y == 1) p.out[3 * size_t(t) + c] = float(kInv4Pi * s);
+			else partial[(size_t(blockIdx.y) * NC + c) * p.n_tgt + t] = s;
+		}
+	}
+}
+
+__global__ void f3d_finalize(float* __restrict__ out, int n_tgt,
+	const double* __restrict__ partial, int n_split, double scale)
+{
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= n_tgt) return;
+	double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+	for (int sp = 0; sp < n_split; ++sp) {
+		s0 += partial[(size_t(sp) * 3 + 0) * n_tgt + t];
+		s1 += partial[(size_t(sp) * 3 + 1) * n_tgt + t];
+		s2 += partial[(size_t(sp) * 3 + 2) * n_tgt + t];
+	}
+	out[3 * size_t(t) + 0] = float(scale * s0);
+	out[3 * size_t(t) + 1] = float(scale * s1);
+	out[3 * size_t(t) + 2] = float(scale * s2);
+}
+
+// Influence matrix: out[i * n_fil + j] = dot(vel_j(mes_i), dir_i).
+// Output-write bound: each thread writes a run of 4 consecutive filaments of
+// one row (one 16-byte store when aligned), reading filament records through
+// the read-only cache.
+__global__ void f3d_inf_kernel(const F3DInfProblem p)
+{
+	const int i = blockIdx.y;
+	const int j0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
+	if (i >= p.n_mes || j0 >= p.n_fil) return;
+	const float4 m = p.mes[i];
+	const float4 d = p.dir[i];
+	float r[4];
+#pragma unroll
+	for (int q = 0; q < 4; ++q) {
+		const int j = j0 + q;
+		r[q] = 0.f;
+		if (j < p.n_fil) {
+			const float4 a = __ldg(&p.fil[2 * size_t(j)]);
+			const float4 b = __ldg(&p.fil[2 * size_t(j) + 1]);
+			float vx, vy, vz;
+			f3d_vel_pair(m.x, m.y, m.z, a, b, vx, vy, vz);
+			r[q] = fmaf(vz, d.z, fmaf(vy, d.y, vx * d.x));
+		}
+	}
+	float* row = p.out + size_t(i) * p.n_fil;
+	if (j0 + 3 < p.n_fil && ((reinterpret_cast<uintptr_t>(row + j0) & 15u) == 0)) {
+		*reinterpret_cast<float4*>(row + j0) = make_float4(r[0], r[1], r[2], r[3]);
+	} else {
+#pragma unroll
+		for (int q = 0; q < 4; ++q) if (j0 + q < p.n_fil) row[j0 + q] = r[q];
+	}
+}
+
+template <int TPT, int NT>
+constexpr size_t smem_bytes() {
+	return Stream2::kSmemBytes + size_t(2) * 3 * TPT * NT * sizeof(float);
+}
+
+template <int TPT, int NT>
+Plan plan_vel(int n_fil, int n_tgt, int num_sms) {
+	constexpr size_t smem = smem_bytes<TPT, NT>();
+	static const int occ = resident_ctas(f3d_vel_kernel<TPT, NT>, NT, smem);
+	return make_plan(n_fil, n_tgt, TPT * NT, kTile, 3, num_sms * occ, smem);
+}
+template <int TPT, int NT>
+Plan plan_dvort(int n_fil, int n_tgt, int num_sms) {
+	constexpr size_t smem = smem_bytes<TPT, NT>();
+	static const int occ = resident_ctas(f3d_dvort_kernel<TPT, NT>, NT, smem);
+	return make_plan(n_fil, n_tgt, TPT * NT, kTile, 3, num_sms * occ, smem);
+}
+
+template <int TPT, int NT>
+cudaError_t launch_vel(const F3DVelProblem& p, const LaunchEnv& env) {
+	const Plan pl = plan_vel<TPT, NT>(p.n_fil, p.n_tgt, env.num_sms);
+	if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
+	double* partial = static_cast<double*>(env.ws);
+	f3d_vel_kernel<TPT, NT><<<dim3(pl.n_tblocks, pl.n_split), NT, pl.smem, env.stream>>>(
+		p, partial, pl.src_per_split, env.err);
+	count_launch();
+	if (pl.n_split > 1) {
+		f3d_finalize<<<(p.n_tgt + 255) / 256, 256, 0, env.stream>>>(p.out, p.n_tgt, partial, pl.n_split, 1.0);
+		count_launch();
+	}
+	return cudaGetLastError();
+}
+template <int TPT, int NT>
+cudaError_t launch_dvort(const F3DDvortProblem& p, const LaunchEnv& env) {
+	const Plan pl = plan_dvort<TPT, NT>(p.n_fil, p.n_tgt, env.num_sms);
+	if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
+	double* partial = static_cast<double*>(env.ws);
+	f3d_dvort_kernel<TPT, NT><<<dim3(pl.n_tblocks, pl.n_split), NT, pl.smem, env.stream>>>(
+		p, partial, pl.src_per_split, env.err);
+	count_launch();
+	if (pl.n_split > 1) {
+		f3d_finalize<<<(p.n_tgt + 255) / 256, 256, 0, env.stream>>>(p.out, p.n_tgt, partial, pl.n_split, kInv4Pi);
+		count_launch();
+	}
+	return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t f3d_vel_ws_bytes(int n_fil, int n_tgt, int num_sms) {
+	if (n_tgt <= 0) return 0;
+	return n_tgt < kSmallTargets ? plan_vel<1, 128>(n_fil, n_tgt, num_sms).ws_bytes
+	                             : plan_vel<4, 128>(n_fil, n_tgt, num_sms).ws_bytes;
+}
+cudaError_t f3d_vel(const F3DVelProblem& p, const LaunchEnv& env) {
+	if (p.n_tgt <= 0) return cudaSuccess;
+	return p.n_tgt < kSmallTargets ? launch_vel<1, 128>(p, env) : launch_vel<4, 128>(p, env);
+}
+size_t f3d_dvort_ws_bytes(int n_fil, int n_tgt, int num_sms) {
+	if (n_tgt <= 0) return 0;
+	return n_tgt < kSmallTargets ? plan_dvort<1, 128>(n_fil, n_tgt, num_sms).ws_bytes
+	                             : plan_dvort<2, 128>(n_fil, n_tgt, num_sms).ws_bytes;
+}
+cudaError_t f3d_dvort(const F3DDvortProblem& p, const LaunchEnv& env) {
+	if (p.n_tgt <= 0) return cudaSuccess;
+	return p.n_tgt < kSmallTargets ? launch_dvort<1, 128>(p, env) : launch_dvort<2, 128>(p, env);
+}
+cudaError_t f3d_inf_mtrx(const F3DInfProblem& p, const LaunchEnv& env) {
+	if (p.n_mes <= 0 || p.n_fil <= 0) return cudaSuccess;
+	const int per_row = (p.n_fil + 3) / 4;
+	dim3 grid((per_row + 127) / 128, p.n_mes);
+	f3d_inf_kernel<<<grid, 128, 0, env.stream>>>(p);
+	count_launch();
+	return cudaGetLastError();
+}
+
+}  // namespace cvtx

@@ -1,0 +1,135 @@
+// nbody.h -- host-side interface of the all-pairs kernels (sm_103a).
+//
+// Device data layout (packed once per call by the host runtime or by the
+// caller of the device-pointer API):
+//   P3D record: 2 float4 = (x, y, z, volume), (alpha_x, alpha_y, alpha_z, 0)
+//   P2D record: 1 float4 = (x, y, Gamma, area)
+//   F3D record: 2 float4 = (start_x, start_y, start_z, strength),
+//                          (end_x, end_y, end_z, 0)
+//   Measurement points:    float4 (x, y, z, 0) or (x, y, 0, 0)
+// Targets are addressed as tgt[k * tstride] (position record) and
+// tgt[k * tstride + 1] (vorticity record), so a source array with stride 2
+// can serve directly as the target array when the caller aliases them.
+// Outputs are written as packed float3 / float2 / float arrays, which is the
+// memory layout of bsv_V3f[] / bsv_V2f[] / float[] on the host.
+//
+// Every launcher takes a caller-provided workspace (for split-source partial
+// sums) whose required size is returned by the matching *_ws_bytes query for
+// the same arguments; the launchers never allocate.
+#pragma once
+#include <cstddef>
+#include <cuda_runtime.h>
+
+namespace cvtx {
+
+enum : unsigned { kOpVel = 1u, kOpDvort = 2u };
+
+struct P3DInduceProblem {
+	const float4* src; int n_src;
+	const float4* tgt; int tstride; int n_tgt;
+	float* out_vel;     // 3 * n_tgt floats, or nullptr
+	float* out_dvort;   // 3 * n_tgt floats, or nullptr (needs target vorticity)
+	float sigma;
+};
+
+struct P3DViscProblem {
+	const float4* src; int n_src;
+	const float4* tgt; int tstride; int n_tgt;
+	float* out;         // 3 * n_tgt floats
+	float sigma, nu;
+};
+
+struct P3DVortProblem {
+	const float4* src; int n_src;
+	const float4* tgt; int tstride; int n_tgt;
+	float* out;         // 3 * n_tgt floats
+	float sigma;
+};
+
+struct P2DVelProblem {
+	const float4* src; int n_src;
+	const float4* tgt; int n_tgt;   // tgt: (x, y, *, *)
+	float* out;         // 2 * n_tgt floats
+	float sigma;
+};
+
+struct P2DViscProblem {
+	const float4* src; int n_src;
+	const float4* tgt; int n_tgt;   // tgt: (x, y, Gamma, area)
+	float* out;         // n_tgt floats
+	float sigma, nu;
+};
+
+struct F3DVelProblem {
+	const float4* fil; int n_fil;
+	const float4* tgt; int tstride; int n_tgt;
+	float* out;         // 3 * n_tgt floats
+};
+
+struct F3DDvortProblem {
+	const float4* fil; int n_fil;
+	const float4* tgt; int tstride; int n_tgt;   // P3D records
+	float* out;         // 3 * n_tgt floats
+};
+
+struct F3DInfProblem {
+	const float4* fil; int n_fil;
+	const float4* mes; int n_mes;   // (x, y, z, 0)
+	const float4* dir;              // (x, y, z, 0)
+	float* out;                     // n_mes * n_fil floats, row-major by mes
+};
+
+struct LaunchEnv {
+	void* ws;            // workspace, 256-byte aligned
+	size_t ws_bytes;
+	unsigned* err;       // device error word (0 = ok)
+	cudaStream_t stream;
+	int num_sms;
+};
+
+// Kernel-launch counter shared by every launcher (for the launch statistics
+// exposed by the library).
+void count_launch(int n = 1);
+unsigned long long launch_count();
+
+// Regularisation id from the reference tag string; -1 if not GPU-capable.
+// Tags: "singular" 0, "winckelmans" 1, "planetary" 2, "gaussian" 3.
+int reg_from_tag(const char* tag);
+
+// Gaussian small-rho threshold (rho below which the series is used).
+float gaussian_rho_c();
+void set_gaussian_rho_c(float rho_c);
+
+size_t p3d_induce_ws_bytes(int reg, unsigned ops, int n_src, int n_tgt, int num_sms);
+cudaError_t p3d_induce(int reg, unsigned ops, const P3DInduceProblem& p, const LaunchEnv& env);
+
+size_t p3d_visc_ws_bytes(int reg, int n_src, int n_tgt, int num_sms);
+cudaError_t p3d_visc(int reg, const P3DViscProblem& p, const LaunchEnv& env);
+
+size_t p3d_vort_ws_bytes(int reg, int n_src, int n_tgt, int num_sms);
+cudaError_t p3d_vort(int reg, const P3DVortProblem& p, const LaunchEnv& env);
+
+size_t p2d_vel_ws_bytes(int reg, int n_src, int n_tgt, int num_sms);
+cudaError_t p2d_vel(int reg, const P2DVelProblem& p, const LaunchEnv& env);
+
+size_t p2d_visc_ws_bytes(int reg, int n_src, int n_tgt, int num_sms);
+cudaError_t p2d_visc(int reg, const P2DViscProblem& p, const LaunchEnv& env);
+
+size_t f3d_vel_ws_bytes(int n_fil, int n_tgt, int num_sms);
+cudaError_t f3d_vel(const F3DVelProblem& p, const LaunchEnv& env);
+
+size_t f3d_dvort_ws_bytes(int n_fil, int n_tgt, int num_sms);
+cudaError_t f3d_dvort(const F3DDvortProblem& p, const LaunchEnv& env);
+
+cudaError_t f3d_inf_mtrx(const F3DInfProblem& p, const LaunchEnv& env);
+
+// Repack kernels: caller AoS records (already on the device) -> records above.
+cudaError_t pack_p3d(const void* aos28, int n, float4* out, cudaStream_t s);
+cudaError_t pack_p2d(const void* aos16, int n, float4* out, cudaStream_t s);
+cudaError_t pack_f3d(const void* aos28, int n, float4* out, cudaStream_t s);
+cudaError_t pack_v3(const void* v12, int n, float4* out, cudaStream_t s);
+cudaError_t pack_v2(const void* v8, int n, float4* out, cudaStream_t s);
+// Gather through a device-visible array of record pointers.
+cudaError_t gather_p3d(const void* const* ptrs, int n, float4* out, cudaStream_t s);
+
+}  // namespace cvtx

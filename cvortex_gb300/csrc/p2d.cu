@@ -1,0 +1,311 @@
+// p2d.cu -- all-pairs 2D vortex particle kernels for sm_103a.
+//
+// Replaces cvtx_nb_P2D_{vel,smallmes_vel,visc_dvort}_* (reference
+// src/nbody.cl:220-338, 547-605) and src/ocl_P2D.cpp. Results follow the
+// reference CPU path src/P2D.cpp:49-69 (velocity) and :167-194 (viscous
+// exchange). Same CTA shape as p3d.cu; a P2D source record is one float4
+// (x, y, Gamma, area), so a 512-record tile is 8 KB.
+#include <cmath>
+#include "nbody.h"
+#include "plan.cuh"
+#include "regfuncs.cuh"
+#include "tile_stream.cuh"
+
+namespace cvtx {
+RegConsts make_reg_consts_host(float sigma);
+
+namespace {
+
+constexpr int kTile = 512;
+constexpr int kStages = 2;
+using Stream1 = TileStream<1, kTile, kStages>;
+constexpr int kSmallTargets = 8192;
+
+template <Reg R> struct HFinite { static constexpr bool value = true; };
+template <> struct HFinite<Reg::Singular> { static constexpr bool value = false; };
+
+// Velocity: out = S * sum_s Hs Gamma_s (dy, -dx), d = x_t - x_s.
+template <Reg R, int TPT, int NT>
+__global__ void __launch_bounds__(NT)
+p2d_vel_kernel(const P2DVelProblem p, const RegConsts rc, double scale,
+	double* __restrict__ partial, int src_per_split, unsigned* err)
+{
+	constexpr int NC = 2;
+	extern __shared__ __align__(16) unsigned char smem[];
+	float* hi = reinterpret_cast<float*>(smem + Stream1::kSmemBytes);
+	float* lo = hi + NC * TPT * NT;
+	const int tid = threadIdx.x;
+	const int tbase = blockIdx.x * (TPT * NT);
+	const int s_begin = blockIdx.y * src_per_split;
+	int n_s = p.n_src - s_begin;
+	n_s = n_s < src_per_split ? n_s : src_per_split;
+	n_s = n_s > 0 ? n_s : 0;
+	float tx[TPT], ty[TPT];
+#pragma unroll
+	for (int k = 0; k < TPT; ++k) {
+		int t = tbase + k * NT + tid;
+		t = t < p.n_tgt ? t : p.n_tgt - 1;
+		const float4 tp = p.tgt[t];
+		tx[k] = tp.x; ty[k] = tp.y;
+	}
+#pragma unroll
+	for (int i = 0; i < NC * TPT; ++i) { hi[i * NT + tid] = 0.f; lo[i * NT + tid] = 0.f; }
+	auto tile_fn = [&](const float4* __restrict__ st, int cnt) {
+		float acc[NC][TPT];
+#pragma unroll
+		for (int c = 0; c < NC; ++c)
+#pragma unroll
+			for (int k = 0; k < TPT; ++k) acc[c][k] = 0.f;
+		auto body = [&](int j) {
+			const float4 s = st[j];
+#pragma unroll
+			for (int k = 0; k < TPT; ++k) {
+				const float dx = tx[k] - s.x;
+				const float dy = ty[k] - s.y;
+				const float r2 = fmaf(dy, dy, dx * dx);
+				float h = RegP2D<R>::h(r2, rc);
+				if (!HFinite<R>::value) h = r2 > 0.f ? h : 0.f;
+				const float hg = h * s.z;
+				acc[0][k] = fmaf(hg, dy, acc[0][k]);
+				acc[1][k] = fmaf(-hg, dx, acc[1][k]);
+			}
+		};
+		if (cnt == kTile) {
+#pragma unroll 4
+			for (int j = 0; j < kTile; ++j) body(j);
+		} else {
+#pragma unroll 1
+			for (int j = 0; j < cnt; ++j) body(j);
+		}
+#pragma unroll
+		for (int c = 0; c < NC; ++c)
+#pragma unroll
+			for (int k = 0; k < TPT; ++k) {
+				const int i = (c * TPT + k) * NT + tid;
+				float h = hi[i], l = lo[i];
+				fold_twosum(h, l, acc[c][k]);
+				hi[i] = h; lo[i] = l;
+			}
+	};
+	if (!Stream1::run(smem, p.src, s_begin, n_s, err, tile_fn)) return;
+#pragma unroll
+	for (int k = 0; k < TPT; ++k) {
+		const int t = tbase + k * NT + tid;
+		if (t >= p.n_tgt) continue;
+#pragma unroll
+		for (int c = 0; c < NC; ++c) {
+			const int i = (c * TPT + k) * NT + tid;
+			const double s = double(hi[i]) + double(lo[i]);
+			if (gridDim.y == 1) p.out[2 * size_t(t) + c] = float(scale * s);
+			else partial[(size_t(blockIdx.y) * NC + c) * p.n_tgt + t] = s;
+		}
+	}
+}
+
+// Viscous exchange: out = S * sum_s Es (Gamma_s A_t - Gamma_t A_s).
+template <Reg R, int TPT, int NT>
+__global__ void __launch_bounds__(NT)
+p2d_visc_kernel(const P2DViscProblem p, const RegConsts rc, double scale,
+	double* __restrict__ partial, int src_per_split, unsigned* err)
+{
+	constexpr int NC = 1;
+	extern __shared__ __align__(16) unsigned char smem[];
+	float* hi = reinterpret_cast<float*>(smem + Stream1::kSmemBytes);
+	float* lo = hi + NC * TPT * NT;
+	const int tid = threadIdx.x;
+	const int tbase = blockIdx.x * (TPT * NT);
+	const int s_begin = blockIdx.y * src_per_split;
+	int n_s = p.n_src - s_begin;
+	n_s = n_s < src_per_split ? n_s : src_per_split;
+	n_s = n_s > 0 ? n_s : 0;
+	float tx[TPT], ty[TPT], tg[TPT], ta[TPT];
+#pragma unroll
+	for (int k = 0; k < TPT; ++k) {
+		int t = tbase + k * NT + tid;
+		t = t < p.n_tgt ? t : p.n_tgt - 1;
+		const float4 tp = p.tgt[t];
+		tx[k] = tp.x; ty[k] = tp.y; tg[k] = tp.z; ta[k] = tp.w;
+	}
+#pragma unroll
+	for (int i = 0; i < NC * TPT; ++i) { hi[i * NT + tid] = 0.f; lo[i * NT + tid] = 0.f; }
+	auto tile_fn = [&](const float4* __restrict__ st, int cnt) {
+		float acc[TPT];
+#pragma unroll
+		for (int k = 0; k < TPT; ++k) acc[k] = 0.f;
+		auto body = [&](int j) {
+			const float4 s = st[j];
+#pragma unroll
+			for (int k = 0; k < TPT; ++k) {
+				const float dx = s.x - tx[k];
+				const float dy = s.y - ty[k];
+				const float r2 = fmaf(dy, dy, dx * dx);
+				float e = RegP2D<R>::eta(r2, rc);
+				e = r2 > 0.f ? e : 0.f;
+				const float w = fmaf(s.z, ta[k], -tg[k] * s.w);
+				acc[k] = fmaf(e, w, acc[k]);
+			}
+		};
+		if (cnt == kTile) {
+#pragma unroll 4
+			for (int j = 0; j < kTile; ++j) body(j);
+		} else {
+#pragma unroll 1
+			for (int j = 0; j < cnt; ++j) body(j);
+		}
+#pragma unroll
+		for (int k = 0; k < TPT; ++k) {
+			const int i = k * NT + tid;
+			float h = hi[i], l = lo[i];
+			fold_twosum(h, l, acc[k]);
+			hi[i] = h; lo[i] = l;
+		}
+	};
+	if (!Stream1::run(smem, p.src, s_begin, n_s, err, tile_fn)) return;
+#pragma unroll
+	for (int k = 0; k < TPT; ++k) {
+		const int t = tbase + k * NT + tid;
+		if (t >= p.n_tgt) continue;
+		const int i = k * NT + tid;
+		const double s = double(hi[i]) + double(lo[i]);
+		if (gridDim.y == 1) p.out[t] = float(scale * s);
+		else partial[size_t(blockIdx.y) * p.n_tgt + t] = s;
+	}
+}
+
+template <int NC>
+__global__ void finalize_scaled(float* __restrict__ out, int n_tgt,
+	const double* __restrict__ partial, int n_split, double scale)
+{
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= n_tgt) return;
+	double s[NC];
+#pragma unroll
+	for (int c = 0; c < NC; ++c) s[c] = 0.0;
+	for (int sp = 0; sp < n_split; ++sp)
+#pragma unroll
+		for (int c = 0; c < NC; ++c) s[c] += partial[(size_t(sp) * NC + c) * n_tgt + t];
+#pragma unroll
+	for (int c = 0; c < NC; ++c) out[NC * size_t(t) + c] = float(scale * s[c]);
+}
+
+template <int TPT, int NT, int NC>
+constexpr size_t smem_bytes() {
+	return Stream1::kSmemBytes + size_t(2) * NC * TPT * NT * sizeof(float);
+}
+
+template <Reg R, int TPT, int NT>
+Plan plan_vel(int n_src, int n_tgt, int num_sms) {
+	constexpr size_t smem = smem_bytes<TPT, NT, 2>();
+	static const int occ = resident_ctas(p2d_vel_kernel<R, TPT, NT>, NT, smem);
+	return make_plan(n_src, n_tgt, TPT * NT, kTile, 2, num_sms * occ, smem);
+}
+
+// Reference scale 1/(2 pi) (src/P2D.cpp:118); Winckelmans and Gaussian H are
+// rho-normalised and carry an extra 1/sigma^2.
+double vel_scale(int reg, float sigma) {
+	const double inv2pi = 1.0 / (2.0 * 3.14159265358979323846);
+	if (reg == int(Reg::Winckelmans) || reg == int(Reg::Gaussian))
+		return inv2pi / (double(sigma) * double(sigma));
+	return inv2pi;
+}
+
+template <Reg R, int TPT, int NT>
+cudaError_t launch_vel(const P2DVelProblem& p, const LaunchEnv& env) {
+	const Plan pl = plan_vel<R, TPT, NT>(p.n_src, p.n_tgt, env.num_sms);
+	if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
+	const RegConsts rc = make_reg_consts_host(p.sigma);
+	const double scale = vel_scale(int(R), p.sigma);
+	double* partial = static_cast<double*>(env.ws);
+	p2d_vel_kernel<R, TPT, NT><<<dim3(pl.n_tblocks, pl.n_split), NT, pl.smem, env.stream>>>(
+		p, rc, scale, partial, pl.src_per_split, env.err);
+	count_launch();
+	if (pl.n_split > 1) {
+		finalize_scaled<2><<<(p.n_tgt + 255) / 256, 256, 0, env.stream>>>(
+			p.out, p.n_tgt, partial, pl.n_split, scale);
+		count_launch();
+	}
+	return cudaGetLastError();
+}
+
+template <Reg R, int TPT, int NT>
+Plan plan_visc(int n_src, int n_tgt, int num_sms) {
+	constexpr size_t smem = smem_bytes<TPT, NT, 1>();
+	static const int occ = resident_ctas(p2d_visc_kernel<R, TPT, NT>, NT, smem);
+	return make_plan(n_src, n_tgt, TPT * NT, kTile, 1, num_sms * occ, smem);
+}
+
+template <Reg R, int TPT, int NT>
+cudaError_t launch_visc(const P2DViscProblem& p, const LaunchEnv& env) {
+	const Plan pl = plan_visc<R, TPT, NT>(p.n_src, p.n_tgt, env.num_sms);
+	if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
+	const RegConsts rc = make_reg_consts_host(p.sigma);
+	const double scale = 2.0 * double(p.nu) / (double(p.sigma) * double(p.sigma));
+	double* partial = static_cast<double*>(env.ws);
+	p2d_visc_kernel<R, TPT, NT><<<dim3(pl.n_tblocks, pl.n_split), NT, pl.smem, env.stream>>>(
+		p, rc, scale, partial, pl.src_per_split, env.err);
+	count_launch();
+	if (pl.n_split > 1) {
+		finalize_scaled<1><<<(p.n_tgt + 255) / 256, 256, 0, env.stream>>>(
+			p.out, p.n_tgt, partial, pl.n_split, scale);
+		count_launch();
+	}
+	return cudaGetLastError();
+}
+
+template <Reg R>
+size_t ws_vel_r(int n_src, int n_tgt, int num_sms) {
+	return n_tgt < kSmallTargets ? plan_vel<R, 1, 128>(n_src, n_tgt, num_sms).ws_bytes
+	                             : plan_vel<R, 4, 128>(n_src, n_tgt, num_sms).ws_bytes;
+}
+template <Reg R>
+cudaError_t vel_r(const P2DVelProblem& p, const LaunchEnv& env) {
+	return p.n_tgt < kSmallTargets ? launch_vel<R, 1, 128>(p, env) : launch_vel<R, 4, 128>(p, env);
+}
+template <Reg R>
+size_t ws_visc_r(int n_src, int n_tgt, int num_sms) {
+	return n_tgt < kSmallTargets ? plan_visc<R, 1, 128>(n_src, n_tgt, num_sms).ws_bytes
+	                             : plan_visc<R, 4, 128>(n_src, n_tgt, num_sms).ws_bytes;
+}
+template <Reg R>
+cudaError_t visc_r(const P2DViscProblem& p, const LaunchEnv& env) {
+	return p.n_tgt < kSmallTargets ? launch_visc<R, 1, 128>(p, env) : launch_visc<R, 4, 128>(p, env);
+}
+
+}  // namespace
+
+size_t p2d_vel_ws_bytes(int reg, int n_src, int n_tgt, int num_sms) {
+	if (n_tgt <= 0) return 0;
+	switch (reg) {
+	case 0: return ws_vel_r<Reg::Singular>(n_src, n_tgt, num_sms);
+	case 1: return ws_vel_r<Reg::Winckelmans>(n_src, n_tgt, num_sms);
+	case 2: return ws_vel_r<Reg::Planetary>(n_src, n_tgt, num_sms);
+	default: return ws_vel_r<Reg::Gaussian>(n_src, n_tgt, num_sms);
+	}
+}
+
+cudaError_t p2d_vel(int reg, const P2DVelProblem& p, const LaunchEnv& env) {
+	if (p.n_tgt <= 0) return cudaSuccess;
+	switch (reg) {
+	case 0: return vel_r<Reg::Singular>(p, env);
+	case 1: return vel_r<Reg::Winckelmans>(p, env);
+	case 2: return vel_r<Reg::Planetary>(p, env);
+	case 3: return vel_r<Reg::Gaussian>(p, env);
+	default: return cudaErrorInvalidValue;
+	}
+}
+
+size_t p2d_visc_ws_bytes(int reg, int n_src, int n_tgt, int num_sms) {
+	if (n_tgt <= 0) return 0;
+	if (reg == int(Reg::Winckelmans)) return ws_visc_r<Reg::Winckelmans>(n_src, n_tgt, num_sms);
+	if (reg == int(Reg::Gaussian)) return ws_visc_r<Reg::Gaussian>(n_src, n_tgt, num_sms);
+	return 0;
+}
+
+cudaError_t p2d_visc(int reg, const P2DViscProblem& p, const LaunchEnv& env) {
+	if (p.n_tgt <= 0) return cudaSuccess;
+	if (reg == int(Reg::Winckelmans)) return visc_r<Reg::Winckelmans>(p, env);
+	if (reg == int(Reg::Gaussian)) return visc_r<Reg::Gaussian>(p, env);
+	return cudaErrorInvalidValue;
+}
+
+}  // namespace cvtx

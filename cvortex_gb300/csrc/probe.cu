@@ -1,0 +1,71 @@
+// probe.cu -- measured FP32 FMA throughput of the active GPU, used as the
+// denominator of the all-pairs kernels' roofline (they are FP32-pipe bound;
+// the device's HBM and tensor peaks do not bound them).
+//
+// Every thread runs 8 independent FMA chains; the grid fills every SM with
+// 8 CTAs of 256 threads. Flops counted: 2 per FMA.
+#include <algorithm>
+#include <string>
+
+#include "cvortex/cvtx_gb300.h"
+#include "nbody.h"
+#include "runtime.h"
+
+namespace cvtx {
+namespace {
+
+constexpr int kChains = 8;
+constexpr int kIters = 4096;
+
+__global__ void __launch_bounds__(256) fma_probe_kernel(float* out, float a, float b) {
+	float x[kChains];
+#pragma unroll
+	for (int c = 0; c < kChains; ++c) x[c] = float(threadIdx.x + c);
+#pragma unroll 4
+	for (int i = 0; i < kIters; ++i) {
+#pragma unroll
+		for (int c = 0; c < kChains; ++c) x[c] = fmaf(x[c], a, b);
+	}
+	float s = 0.f;
+#pragma unroll
+	for (int c = 0; c < kChains; ++c) s += x[c];
+	if (s == 1.2345f) out[threadIdx.x] = s;   // keeps the chains live
+}
+
+}  // namespace
+}  // namespace cvtx
+
+extern "C" CVTX_EXPORT int cvtx_gb300_probe_fp32_tflops(int repeats, double* tflops) {
+	using namespace cvtx;
+	if (!tflops || repeats < 1) return -1;
+	std::lock_guard<std::recursive_mutex> g(Runtime::get().lock());
+	DeviceContext* c = Runtime::get().active_context();
+	if (!c) return -3;
+	float* out = nullptr;
+	cudaEvent_t e0 = nullptr, e1 = nullptr;
+	cudaError_t e = cudaMalloc(&out, 256 * sizeof(float));
+	if (e == cudaSuccess) e = cudaEventCreate(&e0);
+	if (e == cudaSuccess) e = cudaEventCreate(&e1);
+	const int blocks = c->num_sms * 8;
+	double best = 0.0;
+	for (int r = 0; r <= repeats && e == cudaSuccess; ++r) {
+		cudaEventRecord(e0, c->stream);
+		fma_probe_kernel<<<blocks, 256, 0, c->stream>>>(out, 0.999f, 1e-3f);
+		count_launch();
+		cudaEventRecord(e1, c->stream);
+		e = cudaEventSynchronize(e1);
+		float ms = 0.f;
+		if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+		const double flops = 2.0 * kChains * double(kIters) * 256.0 * blocks;
+		if (r > 0 && ms > 0.f) best = std::max(best, flops / (double(ms) * 1e-3) / 1e12);
+	}
+	if (e0) cudaEventDestroy(e0);
+	if (e1) cudaEventDestroy(e1);
+	if (out) cudaFree(out);
+	if (e != cudaSuccess) {
+		set_error(std::string("cvtx_gb300_probe_fp32_tflops: ") + cudaGetErrorString(e));
+		return -2;
+	}
+	*tflops = best;
+	return 0;
+}

@@ -1,0 +1,234 @@
+// regfuncs.cuh -- per-pair regularisation kernels, one struct per
+// regularisation, chosen at compile time by the kernel templates.
+//
+// Notation: d = x_target - x_source, r2 = |d|^2, rho = r/|sigma|, x2 = rho^2.
+// The reference regularisation functions (src/VortFunc.cpp:64-199) are g(rho),
+// zeta(rho), eta(rho); the kernels need them in these combinations:
+//
+//   P3D induced velocity (src/P3D.cpp:51-72):
+//     u_t = S_vel * sum_s Gs * (d x alpha_s)
+//   P3D vortex stretching (src/P3D.cpp:86-114), with c = d x alpha_s:
+//     dalpha_t = S_dv * [ alpha_t x sum_s Gs alpha_s
+//                         + K_scale * sum_s Ks (alpha_t . c) d ]
+//     because d.(alpha_t x alpha_s) = -alpha_t.c.
+//   P3D viscous exchange (src/P3D.cpp:116-144):
+//     S_visc * sum_s Es * (alpha_s V_t - alpha_t V_s)
+//   P2D velocity (src/P2D.cpp:49-69): S_vel2 * sum_s Hs * Gamma_s (dy, -dx)
+//   P2D viscous exchange (src/P2D.cpp:167-194):
+//     S_visc2 * sum_s Es2 * (Gamma_s A_t - Gamma_t A_s)
+//
+// Gs, Ks, Es, Hs are computed per pair below; S_*, K_scale are per-call
+// constants computed on the host (p3d.cu / p2d.cu). Coincident pairs
+// (r2 == 0) are masked to zero by the callers, as the reference does.
+//
+// Winckelmans, rewritten with q = x2 + 1 and s = q^-1/2 (no cancellation):
+//   g/rho^3 = (q + 1.5) s^5,  (3 g/rho^3 - zeta)/rho^2 = (3 q + 7.5) s^7,
+//   eta3 = 52.5 s^9,  g2/rho^2 = (q + 1) s^4.
+// Gaussian 3D: the reference's Abramowitz & Stegun 7.1.26 erf (with g = 1 for
+// rho > 6) is used for rho >= rho_c; below rho_c, where erf minus its
+// leading term cancels catastrophically in FP32, the exact Taylor series of
+//   G = g/rho^3 = sqrt(2/pi) sum_n (-1)^n x2^n / (2^n n! (2n+3))
+//   K = (3G - zeta)/x2 = sqrt(2/pi) sum_{n>=1} (-1)^(n+1) 2n x2^(n-1)
+//                                            / (2^n n! (2n+3))
+// is evaluated instead (alternating, no cancellation for x2 < 1, so FP32
+// Horner is accurate to a few ulp).
+#pragma once
+#include "common.cuh"
+
+namespace cvtx {
+
+// Per-call constants derived from the regularisation distance.
+struct RegConsts {
+	float inv_s;      // 1/|sigma|
+	float inv_s2;     // 1/sigma^2
+	float s2;         // sigma^2
+	float inv_s3;     // 1/|sigma|^3
+	float rho_c2;     // Gaussian: series below rho^2 < rho_c2
+	float exp2_half;  // -0.5 * log2(e) / sigma^2   (exp(-x2/2) = 2^(r2*this))
+};
+
+enum class Reg : int { Singular = 0, Winckelmans = 1, Planetary = 2, Gaussian = 3 };
+
+constexpr float kSqrt2OverPi = 0.7978845608028654f;
+constexpr float kRecipSqrt2 = 0.7071067811865475f;
+
+template <Reg R> struct RegP3D;
+
+// ---- singular: g = 1, zeta = 0 ------------------------------------------
+template <> struct RegP3D<Reg::Singular> {
+	// Gs = 1/r^3, Ks = 1/r^5 (K_scale = 3)
+	__device__ __forceinline__ static void gk(float r2, const RegConsts&, float& G, float& K) {
+		const float ir = rsqrt_approx(r2);
+		const float ir2 = ir * ir;
+		G = ir * ir2;
+		K = G * ir2;
+	}
+	__device__ __forceinline__ static float g(float r2, const RegConsts&) {
+		const float ir = rsqrt_approx(r2);
+		return ir * ir * ir;
+	}
+};
+
+// ---- Winckelmans (high-order algebraic) ---------------------------------
+template <> struct RegP3D<Reg::Winckelmans> {
+	// Gs = (q+1.5) s^5, Ks = (3q+7.5) s^7 (K_scale = 1/sigma^2)
+	__device__ __forceinline__ static void gk(float r2, const RegConsts& c, float& G, float& K) {
+		const float q = fmaf(r2, c.inv_s2, 1.f);
+		const float s = rsqrt_approx(q);
+		const float s2 = s * s;
+		const float s5 = s2 * s2 * s;
+		G = (q + 1.5f) * s5;
+		K = fmaf(q, 3.f, 7.5f) * (s5 * s2);
+	}
+	__device__ __forceinline__ static float g(float r2, const RegConsts& c) {
+		const float q = fmaf(r2, c.inv_s2, 1.f);
+		const float s = rsqrt_approx(q);
+		const float s2 = s * s;
+		return (q + 1.5f) * (s2 * s2 * s);
+	}
+	// eta3 / 52.5 = s^9
+	__device__ __forceinline__ static float eta(float r2, const RegConsts& c) {
+		const float q = fmaf(r2, c.inv_s2, 1.f);
+		const float s = rsqrt_approx(q);
+		const float s2 = s * s;
+		const float s4 = s2 * s2;
+		return s4 * s4 * s;
+	}
+};
+
+// ---- planetary: g = rho^3 inside the core, 1 outside --------------------
+template <> struct RegP3D<Reg::Planetary> {
+	// inside: Gs = 1/|sigma|^3, Ks = 0; outside: Gs = 1/r^3, Ks = 1/r^5
+	// (K_scale = 3)
+	__device__ __forceinline__ static void gk(float r2, const RegConsts& c, float& G, float& K) {
+		const float ir = rsqrt_approx(r2);
+		const float ir2 = ir * ir;
+		const float ir3 = ir * ir2;
+		const bool inside = r2 < c.s2;
+		G = inside ? c.inv_s3 : ir3;
+		K = inside ? 0.f : ir3 * ir2;
+	}
+	__device__ __forceinline__ static float g(float r2, const RegConsts& c) {
+		const float ir = rsqrt_approx(r2);
+		return r2 < c.s2 ? c.inv_s3 : ir * ir * ir;
+	}
+};
+
+// ---- Gaussian -------------------------------------------------------------
+struct GaussSeries {
+	// sqrt(2/pi) * sum_n (-1)^n x^n / (2^n n! (2n+3)), n = 0..6
+	__device__ __forceinline__ static float G(float x) {
+		float p = 1.f / 691200.f;
+		p = fmaf(p, x, -1.f / 49920.f);
+		p = fmaf(p, x, 1.f / 4224.f);
+		p = fmaf(p, x, -1.f / 432.f);
+		p = fmaf(p, x, 1.f / 56.f);
+		p = fmaf(p, x, -1.f / 10.f);
+		p = fmaf(p, x, 1.f / 3.f);
+		return kSqrt2OverPi * p;
+	}
+	// sqrt(2/pi) * sum_{n>=1} (-1)^(n+1) 2n x^(n-1) / (2^n n! (2n+3)), n = 1..7
+	__device__ __forceinline__ static float K(float x) {
+		float p = 1.f / 783360.f;     // n = 7: 14 / (2^7 7! 17)
+		p = fmaf(p, x, -1.f / 57600.f);
+		p = fmaf(p, x, 1.f / 4992.f);
+		p = fmaf(p, x, -1.f / 528.f);
+		p = fmaf(p, x, 1.f / 72.f);
+		p = fmaf(p, x, -1.f / 14.f);
+		p = fmaf(p, x, 1.f / 5.f);
+		return kSqrt2OverPi * p;
+	}
+};
+
+template <> struct RegP3D<Reg::Gaussian> {
+	// Reference A&S form of g (src/VortFunc.cpp:155-176) for rho >= rho_c.
+	__device__ __forceinline__ static float g_as(float rho) {
+		if (rho > 6.f) return 1.f;
+		const float a1 = 0.254829592f, a2 = -0.284496736f, a3 = 1.421413741f;
+		const float a4 = -1.453152027f, a5 = 1.061405429f, p = 0.3275911f;
+		const float x = rho * kRecipSqrt2;
+		const float t = 1.f / fmaf(p, x, 1.f);
+		const float poly = t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, a5, a4), a3), a2), a1);
+		const float e = expf(-x * x);
+		return (1.f - poly * e) - rho * kSqrt2OverPi * e;
+	}
+	// Gs = g/rho^3, Ks = (3 Gs - zeta)/rho^2 (K_scale = 1/sigma^2)
+	__device__ __forceinline__ static void gk(float r2, const RegConsts& c, float& G, float& K) {
+		const float x2 = r2 * c.inv_s2;
+		if (x2 < c.rho_c2) {
+			G = GaussSeries::G(x2);
+			K = GaussSeries::K(x2);
+		} else {
+			const float rho = sqrtf(x2);
+			const float inv_rho3 = 1.f / (x2 * rho);
+			G = g_as(rho) * inv_rho3;
+			const float zeta = kSqrt2OverPi * expf(-0.5f * x2);
+			K = (3.f * G - zeta) / x2;
+		}
+	}
+	__device__ __forceinline__ static float g(float r2, const RegConsts& c) {
+		const float x2 = r2 * c.inv_s2;
+		if (x2 < c.rho_c2) return GaussSeries::G(x2);
+		const float rho = sqrtf(x2);
+		return g_as(rho) / (x2 * rho);
+	}
+	// eta3 / sqrt(2/pi) = exp(-x2/2)
+	__device__ __forceinline__ static float eta(float r2, const RegConsts& c) {
+		return exp2f(r2 * c.exp2_half);
+	}
+};
+
+// ---- 2D ------------------------------------------------------------------
+template <Reg R> struct RegP2D;
+
+template <> struct RegP2D<Reg::Singular> {
+	// Hs = 1/r^2
+	__device__ __forceinline__ static float h(float r2, const RegConsts&) {
+		return 1.f / r2;
+	}
+};
+template <> struct RegP2D<Reg::Winckelmans> {
+	// Hs = (q + 1)/q^2 with q = x2 + 1  (times 1/sigma^2 on the host)
+	__device__ __forceinline__ static float h(float r2, const RegConsts& c) {
+		const float q = fmaf(r2, c.inv_s2, 1.f);
+		const float rq = 1.f / q;
+		return (q + 1.f) * (rq * rq);
+	}
+	// eta2 = 24 exp(4/a^3) / a^4 with a = x2 + 1 (src/VortFunc.cpp:124-131)
+	__device__ __forceinline__ static float eta(float r2, const RegConsts& c) {
+		const float a = fmaf(r2, c.inv_s2, 1.f);
+		const float ra = 1.f / a;
+		const float ra2 = ra * ra;
+		const float ra4 = ra2 * ra2;
+		return 24.f * expf(4.f * (ra2 * ra)) * ra4;
+	}
+};
+template <> struct RegP2D<Reg::Planetary> {
+	// inside: 1/sigma^2, outside: 1/r^2
+	__device__ __forceinline__ static float h(float r2, const RegConsts& c) {
+		return r2 < c.s2 ? c.inv_s2 : 1.f / r2;
+	}
+};
+template <> struct RegP2D<Reg::Gaussian> {
+	// Hs = (1 - exp(-x2/2)) / x2 (times 1/sigma^2 on the host); series
+	// 1/2 (1 - y/2 + y^2/6 - y^3/24 + y^4/120 - y^5/720), y = x2/2, for y < 0.1
+	__device__ __forceinline__ static float h(float r2, const RegConsts& c) {
+		const float x2 = r2 * c.inv_s2;
+		const float y = 0.5f * x2;
+		if (y < 0.1f) {
+			float p = -1.f / 720.f;
+			p = fmaf(p, y, 1.f / 120.f);
+			p = fmaf(p, y, -1.f / 24.f);
+			p = fmaf(p, y, 1.f / 6.f);
+			p = fmaf(p, y, -0.5f);
+			p = fmaf(p, y, 1.f);
+			return 0.5f * p;
+		}
+		return (1.f - expf(-y)) / x2;
+	}
+	__device__ __forceinline__ static float eta(float r2, const RegConsts& c) {
+		return exp2f(r2 * c.exp2_half);
+	}
+};
+
+}  // namespace cvtx

@@ -1,0 +1,88 @@
+// runtime.h -- single-process CUDA device state behind the cvtx_ ABI.
+//
+// Replaces the reference's OpenCL runtime (src/opencl_acc.cpp,
+// src/OclPlatformState.cpp, src/OclDeviceState.cpp): enumerates CUDA devices,
+// keeps the list of enabled accelerators (accelerator ids = CUDA ordinals),
+// and owns, per device, one non-blocking stream plus grow-only device and
+// pinned host buffers reused across calls. All GPU work runs on the first
+// enabled accelerator, as in the reference (src/ocl_P3D.cpp:46).
+#pragma once
+#include <cstddef>
+#include <mutex>
+#include <string>
+#include <vector>
+#include <cuda_runtime.h>
+
+#include "nbody.h"
+
+namespace cvtx {
+
+// Grow-only device allocation (256-byte aligned by cudaMalloc).
+struct DevBuf {
+	void* ptr = nullptr;
+	size_t bytes = 0;
+	cudaError_t ensure(size_t need);
+	void release();
+};
+
+// Grow-only pinned host allocation.
+struct HostBuf {
+	void* ptr = nullptr;
+	size_t bytes = 0;
+	cudaError_t ensure(size_t need);
+	void release();
+};
+
+struct DeviceContext {
+	int device = -1;
+	int num_sms = 0;
+	cudaStream_t stream = nullptr;
+	unsigned* d_err = nullptr;      // device error word
+	unsigned* h_err = nullptr;      // pinned copy
+	DevBuf src, tgt, out0, out1, ws;
+	HostBuf h_src, h_tgt, h_out0, h_out1;
+	cudaError_t open(int dev);
+	void close();
+	LaunchEnv env() const;
+	// Make sure the workspace holds `bytes`.
+	cudaError_t ensure_ws(size_t bytes) { return ws.ensure(bytes); }
+};
+
+class Runtime {
+ public:
+	static Runtime& get();
+
+	void initialise();
+	void finalise();
+	bool is_initialised();
+	int num_devices();
+	const char* device_name(int id);
+	int num_enabled();
+	bool enabled(int id);
+	void enable(int id);
+	void disable(int id);
+	const char* information();
+
+	// Context of the first enabled accelerator (opened on first use) or
+	// nullptr when none is enabled. The caller must hold lock().
+	DeviceContext* active_context();
+	std::recursive_mutex& lock() { return mu_; }
+
+ private:
+	Runtime() = default;
+	void enumerate_locked();
+	std::recursive_mutex mu_;
+	bool initialised_ = false;
+	bool enumerated_ = false;
+	std::vector<std::string> names_;
+	std::vector<int> active_;
+	std::vector<DeviceContext*> ctx_;
+	std::string info_;
+};
+
+// Error reporting for the GPU path (the reference ABI functions return void).
+void set_error(const std::string& msg);
+void clear_error();
+const char* last_error();
+
+}  // namespace cvtx

@@ -1,0 +1,5 @@
+#ifndef BSV_V3F_H
+#define BSV_V3F_H
+/* Per-type header name used by some bsv callers; everything lives in bsv.h. */
+#include "bsv.h"
+#endif

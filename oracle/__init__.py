@@ -1,0 +1,176 @@
+"""The oracle -- TEST INFRASTRUCTURE ONLY.
+
+Three checkers for the GB300 library, none of which the product imports:
+
+* ``lib()``: ``cvtx_oracle.c``, a plain-C restatement of the reference
+  cvortex CPU (OpenMP) path for the M2M interactions, built here by ``build()``
+  into ``oracle/lib/libcvtx_oracle.so``. It runs anywhere gcc runs (including
+  the Arm GPU host), so tests, the smoke check and the CPU-baseline leg of the
+  benchmark can use it where the reference sources are absent.
+* ``ref_lib()``: the reference library itself, compiled from the reference
+  sources by ``oracle/build_ref.sh`` into ``oracle/_ref/libcvtx_ref.so`` when
+  those sources are present. It pins the restatement (tests compare the two)
+  and generates the golden fixtures under ``tests/golden``.
+* ``oracle.exact``: the same formulas in float64 with the exact error
+  function, i.e. the "error vs FP64" reference (independent of the reference
+  implementation and of FP32 rounding).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parent
+LIB = HERE / "lib" / "libcvtx_oracle.so"
+REF_LIB = HERE / "_ref" / "libcvtx_ref.so"
+REFERENCE_ROOT = Path(os.environ.get("CVTX_REFERENCE_ROOT", "/root/reference"))
+
+
+def build(force: bool = False) -> Path:
+    """Compile the C restatement with OpenMP (gcc, -O2, no fast-math)."""
+    src = HERE / "cvtx_oracle.c"
+    LIB.parent.mkdir(parents=True, exist_ok=True)
+    if force or not LIB.exists() or LIB.stat().st_mtime < src.stat().st_mtime:
+        cmd = [os.environ.get("CC", "gcc"), "-O2", "-fPIC", "-shared", "-fopenmp", "-std=c11",
+               "-I", str(REPO / "include"), str(src), "-o", str(LIB), "-lm"]
+        subprocess.run(cmd, check=True)
+    return LIB
+
+
+def build_ref() -> Path | None:
+    """Compile the reference CPU library if its sources are present."""
+    if not (REFERENCE_ROOT / "src").is_dir():
+        return None
+    subprocess.run(["bash", str(HERE / "build_ref.sh"), str(REFERENCE_ROOT)], check=True,
+                   capture_output=True)
+    return REF_LIB if REF_LIB.exists() else None
+
+
+_vp, _i, _f = C.c_void_p, C.c_int, C.c_float
+_SIGS = {
+    "oracle_regfunc": (_f, [_i, _i, _f]),
+    "oracle_P3D_M2M_vel": (None, [_vp, _i, _vp, _i, _vp, _i, _f]),
+    "oracle_P3D_M2M_dvort": (None, [_vp, _i, _vp, _i, _vp, _i, _f]),
+    "oracle_P3D_M2M_visc_dvort": (None, [_vp, _i, _vp, _i, _vp, _i, _f, _f]),
+    "oracle_P3D_M2M_vort": (None, [_vp, _i, _vp, _i, _vp, _i, _f]),
+    "oracle_P2D_M2M_vel": (None, [_vp, _i, _vp, _i, _vp, _i, _f]),
+    "oracle_P2D_M2M_visc_dvort": (None, [_vp, _i, _vp, _i, _vp, _i, _f, _f]),
+    "oracle_F3D_M2M_vel": (None, [_vp, _i, _vp, _i, _vp]),
+    "oracle_F3D_M2M_dvort": (None, [_vp, _i, _vp, _i, _vp]),
+    "oracle_F3D_inf_mtrx": (None, [_vp, _i, _vp, _vp, _i, _vp]),
+    "oracle_num_threads": (_i, []),
+}
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        path = build()
+        _lib = C.CDLL(str(path))
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(_lib, name)
+            fn.restype, fn.argtypes = res, args
+    return _lib
+
+
+def ref_lib():
+    """numpy front end (cvortex_gb300.abi.Cvtx) over the reference library
+    (oracle/_ref), or None when it has not been built."""
+    if not REF_LIB.exists():
+        return None
+    from cvortex_gb300.abi import Cvtx
+    return Cvtx(REF_LIB, extensions=False)
+
+
+REG = {"singular": 0, "winckelmans": 1, "planetary": 2, "gaussian": 3}
+
+
+def _ptrs(arr):
+    from cvortex_gb300.abi import ptr_array
+    return ptr_array(arr)
+
+
+def _a(x):
+    return x.ctypes.data
+
+
+# ---- numpy wrappers of the C restatement -----------------------------------
+def p3d_vel(src, mes, reg, sigma):
+    p = _ptrs(src)
+    mes = np.ascontiguousarray(mes, np.float32)
+    out = np.zeros((mes.shape[0], 3), np.float32)
+    lib().oracle_P3D_M2M_vel(_a(p), len(src), _a(mes), mes.shape[0], _a(out), REG[reg], sigma)
+    return out
+
+
+def p3d_dvort(src, ind, reg, sigma):
+    p, q = _ptrs(src), _ptrs(ind)
+    out = np.zeros((len(ind), 3), np.float32)
+    lib().oracle_P3D_M2M_dvort(_a(p), len(src), _a(q), len(ind), _a(out), REG[reg], sigma)
+    return out
+
+
+def p3d_visc(src, ind, reg, sigma, nu):
+    p, q = _ptrs(src), _ptrs(ind)
+    out = np.zeros((len(ind), 3), np.float32)
+    lib().oracle_P3D_M2M_visc_dvort(_a(p), len(src), _a(q), len(ind), _a(out), REG[reg], sigma, nu)
+    return out
+
+
+def p3d_vort(src, mes, reg, sigma):
+    p = _ptrs(src)
+    mes = np.ascontiguousarray(mes, np.float32)
+    out = np.zeros((mes.shape[0], 3), np.float32)
+    lib().oracle_P3D_M2M_vort(_a(p), len(src), _a(mes), mes.shape[0], _a(out), REG[reg], sigma)
+    return out
+
+
+def p2d_vel(src, mes, reg, sigma):
+    p = _ptrs(src)
+    mes = np.ascontiguousarray(mes, np.float32)
+    out = np.zeros((mes.shape[0], 2), np.float32)
+    lib().oracle_P2D_M2M_vel(_a(p), len(src), _a(mes), mes.shape[0], _a(out), REG[reg], sigma)
+    return out
+
+
+def p2d_visc(src, ind, reg, sigma, nu):
+    p, q = _ptrs(src), _ptrs(ind)
+    out = np.zeros(len(ind), np.float32)
+    lib().oracle_P2D_M2M_visc_dvort(_a(p), len(src), _a(q), len(ind), _a(out), REG[reg], sigma, nu)
+    return out
+
+
+def f3d_vel(fil, mes):
+    p = _ptrs(fil)
+    mes = np.ascontiguousarray(mes, np.float32)
+    out = np.zeros((mes.shape[0], 3), np.float32)
+    lib().oracle_F3D_M2M_vel(_a(p), len(fil), _a(mes), mes.shape[0], _a(out))
+    return out
+
+
+def f3d_dvort(fil, ind):
+    p, q = _ptrs(fil), _ptrs(ind)
+    out = np.zeros((len(ind), 3), np.float32)
+    lib().oracle_F3D_M2M_dvort(_a(p), len(fil), _a(q), len(ind), _a(out))
+    return out
+
+
+def f3d_inf_mtrx(fil, mes, dirs):
+    p = _ptrs(fil)
+    mes = np.ascontiguousarray(mes, np.float32)
+    dirs = np.ascontiguousarray(dirs, np.float32)
+    out = np.zeros((mes.shape[0], len(fil)), np.float32)
+    lib().oracle_F3D_inf_mtrx(_a(p), len(fil), _a(mes), _a(dirs), mes.shape[0], _a(out))
+    return out
+
+
+def regfunc(reg: str, which: str, rho: float) -> float:
+    w = {"g3": 0, "g2": 1, "zeta3": 2, "eta3": 3, "eta2": 4}[which]
+    return float(lib().oracle_regfunc(REG[reg], w, rho))

@@ -1,0 +1,146 @@
+"""Generate the golden fixtures in this directory from the reference library.
+
+The reference CPU library is compiled from the reference sources by
+oracle/build_ref.sh (into oracle/_ref/, not committed). This script feeds it
+seeded inputs through the unchanged cvtx_ ABI (no accelerator: the
+reference's OpenMP path) and stores inputs and outputs as compressed .npz:
+
+* p3d_<set>.npz   -- vel / dvort / visc_dvort / vort for the four
+                     regularisations on a uniform cube (700 particles,
+                     sigma 0.2, plus 300 separate measurement points) and a
+                     vortex ring (600 particles, sigma 0.05)
+* p2d_patch.npz    -- P2D vel and visc_dvort for the four regularisations
+* f3d_sheet.npz    -- F3D vel, dvort and influence matrix on a wake sheet
+* reftest_many.npz -- the inputs of the reference's own CPU/GPU comparison
+                     test (reference test/testsamecpugpuresultmany.h:67-89,
+                     LCG of test/testmain.c:87-92) with its outputs
+* kat.npz          -- g, zeta, eta (3D and 2D) of every regularisation on a
+                     grid of rho, from the reference's function pointers
+
+Run from the repository root: python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import ctypes as C
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+import oracle  # noqa: E402
+from cvortex_gb300 import abi, workloads  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+REGS = ("singular", "winckelmans", "planetary", "gaussian")
+NU = 1e-3
+
+
+def reference():
+    oracle.build_ref()
+    ref = oracle.ref_lib()
+    if ref is None:
+        raise SystemExit("reference library not available (oracle/build_ref.sh)")
+    ref.initialise()
+    assert ref.num_accelerators() == 0
+    return ref
+
+
+def p3d_case(ref, name, p, mes, sigma):
+    d = {"particles": p, "mes": mes, "sigma": np.float32(sigma), "nu": np.float32(NU)}
+    for reg in REGS:
+        d[f"vel_{reg}"] = ref.p3d_vel(p, p["coord"], reg, sigma)
+        d[f"velmes_{reg}"] = ref.p3d_vel(p, mes, reg, sigma)
+        d[f"dvort_{reg}"] = ref.p3d_dvort(p, p, reg, sigma, same=True)
+        d[f"visc_{reg}"] = ref.p3d_visc(p, p, reg, sigma, NU, same=True)
+        d[f"vort_{reg}"] = ref.p3d_vort(p, mes, reg, sigma)
+    np.savez_compressed(OUT / f"p3d_{name}.npz", **d)
+
+
+def p2d_case(ref):
+    q = workloads.gaussian_patch_2d(800)
+    mes = q["coord"].copy()
+    d = {"particles": q, "sigma": np.float32(0.05), "nu": np.float32(NU)}
+    for reg in REGS:
+        d[f"vel_{reg}"] = ref.p2d_vel(q, mes, reg, 0.05)
+        d[f"visc_{reg}"] = ref.p2d_visc(q, q, reg, 0.05, NU, same=True)
+    np.savez_compressed(OUT / "p2d_patch.npz", **d)
+
+
+def f3d_case(ref):
+    f = workloads.wake_sheet(500)
+    t = workloads.sheet_targets(400)
+    pts = workloads.uniform_cube(400, seed=77)
+    pts["coord"] = t
+    dirs = np.random.Generator(np.random.PCG64(78)).normal(size=(40, 3)).astype(np.float32)
+    d = {"filaments": f, "mes": t, "particles": pts, "dirs": dirs,
+         "vel": ref.f3d_vel(f, t), "dvort": ref.f3d_dvort(f, pts),
+         "inf": ref.f3d_inf_mtrx(f[:200], t[:40], dirs)}
+    np.savez_compressed(OUT / "f3d_sheet.npz", **d)
+
+
+def reftest_inputs(n=1000):
+    """Inputs of the reference's first comparison repeat: LCG x*214013+2531011
+    seeded 0xF0F0F0F0 (test/testmain.c:87-92), values (float)mrand() /
+    (float)(RAND_MAX / 10) with glibc RAND_MAX = 2^31-1 (integer division)."""
+    state = [0xF0F0F0F0]
+
+    def mrand():
+        state[0] = (state[0] * 214013 + 2531011) & 0xFFFFFFFF
+        s = state[0] - (1 << 32) if state[0] & 0x80000000 else state[0]
+        return ((s >> 16) & 0x7FFF) % 2147483647
+
+    div10 = np.float32(2147483647 // 10)
+    div001 = np.float32(int(2147483647 / 0.01))
+    p = np.zeros(n, abi.P3D_DTYPE)
+    for i in range(n):
+        p["coord"][i] = [np.float32(mrand()) / div10 for _ in range(3)]
+        p["vorticity"][i] = [np.float32(mrand()) / div10 for _ in range(3)]
+        p["volume"][i] = np.float32(mrand()) / div001
+    return p
+
+
+def reftest_case(ref):
+    p = reftest_inputs()
+    d = {"particles": p, "sigma": np.float32(0.3)}
+    for reg in ("singular", "winckelmans", "planetary"):
+        d[f"vel_{reg}"] = ref.p3d_vel(p, p["coord"], reg, 0.3)
+        d[f"dvort_{reg}"] = ref.p3d_dvort(p, p, reg, 0.3, same=True)
+    np.savez_compressed(OUT / "reftest_many.npz", **d)
+
+
+def kat_case(ref):
+    rho = np.concatenate([[0.0, 1e-4, 1e-3, 1e-2], np.linspace(0.05, 8.0, 160, dtype=np.float32)])
+    rho = rho.astype(np.float32)
+    d = {"rho": rho}
+    for reg in REGS:
+        vf = getattr(ref.lib, f"cvtx_VortFunc_{reg}")()
+        d[f"g3_{reg}"] = np.array([vf.g_3D(float(r)) for r in rho], np.float32)
+        d[f"g2_{reg}"] = np.array([vf.g_2D(float(r)) for r in rho], np.float32)
+        d[f"zeta3_{reg}"] = np.array([vf.zeta_3D(float(r)) for r in rho], np.float32)
+        if reg in ("winckelmans", "gaussian"):
+            d[f"eta3_{reg}"] = np.array([vf.eta_3D(float(r)) for r in rho], np.float32)
+            d[f"eta2_{reg}"] = np.array([vf.eta_2D(float(r)) for r in rho], np.float32)
+        d[f"tag_{reg}"] = np.frombuffer(bytes(vf.cl_kernel_name_ext), np.uint8)
+    np.savez_compressed(OUT / "kat.npz", **d)
+
+
+def main():
+    ref = reference()
+    cube = workloads.uniform_cube(700, seed=11)
+    mes = workloads.uniform_cube(300, seed=12)["coord"].copy()
+    p3d_case(ref, "cube", cube, mes, 0.2)
+    ring = workloads.vortex_ring(600, seed=13)
+    p3d_case(ref, "ring", ring, workloads.vortex_ring(200, seed=14)["coord"].copy(), 0.05)
+    p2d_case(ref)
+    f3d_case(ref)
+    reftest_case(ref)
+    kat_case(ref)
+    for f in sorted(OUT.glob("*.npz")):
+        print(f.name, f.stat().st_size)
+
+
+if __name__ == "__main__":
+    main()

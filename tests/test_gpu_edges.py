@@ -1,0 +1,131 @@
+"""Edge cases of the CUDA path (through the C ABI) against the oracle:
+empty and tiny sets, sizes around the tile boundaries, coincident points,
+aliasing of sources and targets, few targets with many sources (source
+splits) and the reverse, negative regularisation distance, filaments with
+targets on their axis."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import REGS
+from cvortex_gb300 import abi, workloads
+from oracle import exact
+
+pytestmark = pytest.mark.gpu
+
+
+def close(a, b, tol=1e-5):
+    assert np.all(np.isfinite(a))
+    e = exact.rel_l2(a, b)
+    assert e <= tol, e
+
+
+def test_no_sources_gives_zeros(gpu):
+    p = workloads.uniform_cube(1)
+    mes = workloads.uniform_cube(300, seed=3)["coord"]
+    out = np.full((300, 3), 5.0, np.float32)
+    ptrs = abi.ptr_array(p)
+    gpu.lib.cvtx_P3D_M2M_vel(ptrs.ctypes.data, 0, mes.ctypes.data, 300, out.ctypes.data,
+                             C.byref(gpu.vortfunc("winckelmans")), 0.05)
+    assert not np.any(out)
+
+
+@pytest.mark.parametrize("n", [1, 2, 31, 255, 256, 257, 511, 512, 513, 1023, 8191, 8192, 8193])
+def test_sizes_around_tiles(gpu, n):
+    p = workloads.uniform_cube(n, seed=n)
+    vel, dv = gpu.p3d_vel_dvort(p, "winckelmans", 0.3)
+    close(vel, oracle.p3d_vel(p, p["coord"], "winckelmans", 0.3))
+    close(dv, oracle.p3d_dvort(p, p, "winckelmans", 0.3))
+
+
+@pytest.mark.parametrize("reg", REGS)
+def test_coincident_distinct_particles(gpu, reg):
+    p = workloads.uniform_cube(600, seed=41)
+    p["coord"][300:] = p["coord"][:300]          # 300 exact twins, different vorticity
+    vel = gpu.p3d_vel(p, p["coord"], reg, 0.2)
+    dv = gpu.p3d_dvort(p, p, reg, 0.2, same=True)
+    close(vel, oracle.p3d_vel(p, p["coord"], reg, 0.2))
+    close(dv, oracle.p3d_dvort(p, p, reg, 0.2))
+
+
+def test_aliased_and_copied_targets_agree(gpu):
+    p = workloads.vortex_ring(5000, seed=42)
+    a = gpu.p3d_dvort(p, p, "gaussian", 0.05, same=True)
+    b = gpu.p3d_dvort(p, p.copy(), "gaussian", 0.05)
+    np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("reg", REGS)
+def test_few_targets_many_sources(gpu, reg):
+    p = workloads.vortex_ring(60_000, seed=43)
+    q = workloads.vortex_ring(3, seed=44)
+    close(gpu.p3d_vel(p, q["coord"], reg, 0.05), oracle.p3d_vel(p, q["coord"], reg, 0.05))
+    close(gpu.p3d_dvort(p, q, reg, 0.05), oracle.p3d_dvort(p, q, reg, 0.05))
+
+
+def test_many_targets_few_sources(gpu):
+    p = workloads.uniform_cube(3, seed=45)
+    mes = workloads.uniform_cube(40_000, seed=46)["coord"]
+    close(gpu.p3d_vel(p, mes, "winckelmans", 0.05), oracle.p3d_vel(p, mes, "winckelmans", 0.05))
+
+
+@pytest.mark.parametrize("reg", REGS)
+def test_negative_sigma(gpu, reg):
+    p = workloads.uniform_cube(700, seed=47)
+    close(gpu.p3d_vel(p, p["coord"], reg, -0.2), oracle.p3d_vel(p, p["coord"], reg, -0.2))
+    close(gpu.p3d_dvort(p, p, reg, -0.2, same=True), oracle.p3d_dvort(p, p, reg, -0.2))
+
+
+def test_visc_without_eta_returns_zeros(gpu):
+    p = workloads.uniform_cube(500, seed=48)
+    for reg in ("singular", "planetary"):
+        before = gpu.launches()
+        out = gpu.p3d_visc(p, p, reg, 0.2, 1e-3, same=True)
+        assert not np.any(out)
+        assert gpu.launches() == before
+    q = workloads.gaussian_patch_2d(500)
+    for reg in ("singular", "planetary"):
+        assert not np.any(gpu.p2d_visc(q, q, reg, 0.05, 1e-3, same=True))
+
+
+def test_p2d_sizes_and_visc(gpu):
+    for n in (1, 511, 512, 513, 9000):
+        q = workloads.gaussian_patch_2d(n)
+        close(gpu.p2d_vel(q, q["coord"], "winckelmans", 0.05),
+              oracle.p2d_vel(q, q["coord"], "winckelmans", 0.05))
+        for reg in ("winckelmans", "gaussian"):
+            close(gpu.p2d_visc(q, q, reg, 0.05, 1e-3, same=True),
+                  oracle.p2d_visc(q, q, reg, 0.05, 1e-3))
+
+
+def test_f3d_targets_on_filament_axis(gpu):
+    f = workloads.wake_sheet(300)
+    t = workloads.sheet_targets(500)
+    t[:50] = f["start"][:50]                       # exactly at segment ends
+    t[50:100] = 0.5 * (f["start"][50:100] + f["end"][50:100])  # on the segment
+    close(gpu.f3d_vel(f, t), oracle.f3d_vel(f, t))
+    pts = workloads.uniform_cube(500, seed=49)
+    pts["coord"] = t
+    close(gpu.f3d_dvort(f, pts), oracle.f3d_dvort(f, pts))
+
+
+def test_f3d_split_sources(gpu):
+    f = workloads.wake_sheet(40_000)
+    t = workloads.sheet_targets(50)
+    close(gpu.f3d_vel(f, t), oracle.f3d_vel(f, t))
+
+
+@pytest.mark.parametrize("reg", REGS)
+def test_vort_and_relaxation(gpu, reg):
+    p = workloads.vortex_ring(4000, seed=50)
+    mes = p["coord"].copy()
+    close(gpu.p3d_vort(p, mes, reg, 0.05), oracle.p3d_vort(p, mes, reg, 0.05))
+    a = p.copy()
+    b = p.copy()
+    gpu.relax(a, 0.3, reg, 0.05)
+    gpu.set_accelerated(False)
+    gpu.relax(b, 0.3, reg, 0.05)
+    gpu.set_accelerated(True)
+    close(a["vorticity"], b["vorticity"], 1e-5)
