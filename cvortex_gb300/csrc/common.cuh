@@ -94,6 +94,14 @@ __device__ __forceinline__ float rsqrt_approx(float x) {
 	return y;
 }
 
+// rsqrt with one Newton step, y (1.5 - 0.5 x y^2): about half an ulp, for
+// kernels whose per-pair weights are high powers of 1/r (errors triple in 1/r^3).
+__device__ __forceinline__ float rsqrt_refined(float x) {
+	const float y = rsqrt_approx(x);
+	const float h = x * y;
+	return y * fmaf(-0.5f * h, y, 1.5f);
+}
+
 // Knuth TwoSum fold of an FP32 tile partial `p` into the pair (hi, lo).
 __device__ __forceinline__ void fold_twosum(float& hi, float& lo, float p) {
 	const float s = __fadd_rn(hi, p);

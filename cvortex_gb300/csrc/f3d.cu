@@ -251,35 +251,39 @@ __global__ void f3d_finalize(float* __restrict__ out, int n_tgt,
 }
 
 // Influence matrix: out[i * n_fil + j] = dot(vel_j(mes_i), dir_i).
-// Output-write bound: each thread writes a run of 4 consecutive filaments of
-// one row (one 16-byte store when aligned), reading filament records through
-// the read-only cache.
+// Output-write bound: each work item is a run of 4 consecutive filaments of
+// one row (one 16-byte store when aligned); a grid-stride loop over the
+// n_mes * ceil(n_fil / 4) items uses 64-bit indices.
 __global__ void f3d_inf_kernel(const F3DInfProblem p)
 {
-	const int i = blockIdx.y;
-	const int j0 = (blockIdx.x * blockDim.x + threadIdx.x) * 4;
-	if (i >= p.n_mes || j0 >= p.n_fil) return;
-	const float4 m = p.mes[i];
-	const float4 d = p.dir[i];
-	float r[4];
+	const long long per_row = (p.n_fil + 3) / 4;
+	const long long items = per_row * p.n_mes;
+	for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < items;
+		w += (long long)gridDim.x * blockDim.x) {
+		const int i = int(w / per_row);
+		const int j0 = int(w - (long long)i * per_row) * 4;
+		const float4 m = p.mes[i];
+		const float4 d = p.dir[i];
+		float r[4];
 #pragma unroll
-	for (int q = 0; q < 4; ++q) {
-		const int j = j0 + q;
-		r[q] = 0.f;
-		if (j < p.n_fil) {
-			const float4 a = __ldg(&p.fil[2 * size_t(j)]);
-			const float4 b = __ldg(&p.fil[2 * size_t(j) + 1]);
-			float vx, vy, vz;
-			f3d_vel_pair(m.x, m.y, m.z, a, b, vx, vy, vz);
-			r[q] = fmaf(vz, d.z, fmaf(vy, d.y, vx * d.x));
+		for (int q = 0; q < 4; ++q) {
+			const int j = j0 + q;
+			r[q] = 0.f;
+			if (j < p.n_fil) {
+				const float4 a = __ldg(&p.fil[2 * size_t(j)]);
+				const float4 b = __ldg(&p.fil[2 * size_t(j) + 1]);
+				float vx, vy, vz;
+				f3d_vel_pair(m.x, m.y, m.z, a, b, vx, vy, vz);
+				r[q] = fmaf(vz, d.z, fmaf(vy, d.y, vx * d.x));
+			}
 		}
-	}
-	float* row = p.out + size_t(i) * p.n_fil;
-	if (j0 + 3 < p.n_fil && ((reinterpret_cast<uintptr_t>(row + j0) & 15u) == 0)) {
-		*reinterpret_cast<float4*>(row + j0) = make_float4(r[0], r[1], r[2], r[3]);
-	} else {
+		float* row = p.out + size_t(i) * p.n_fil;
+		if (j0 + 3 < p.n_fil && ((reinterpret_cast<uintptr_t>(row + j0) & 15u) == 0)) {
+			*reinterpret_cast<float4*>(row + j0) = make_float4(r[0], r[1], r[2], r[3]);
+		} else {
 #pragma unroll
-		for (int q = 0; q < 4; ++q) if (j0 + q < p.n_fil) row[j0 + q] = r[q];
+			for (int q = 0; q < 4; ++q) if (j0 + q < p.n_fil) row[j0 + q] = r[q];
+		}
 	}
 }
 
@@ -352,9 +356,10 @@ cudaError_t f3d_dvort(const F3DDvortProblem& p, const LaunchEnv& env) {
 }
 cudaError_t f3d_inf_mtrx(const F3DInfProblem& p, const LaunchEnv& env) {
 	if (p.n_mes <= 0 || p.n_fil <= 0) return cudaSuccess;
-	const int per_row = (p.n_fil + 3) / 4;
-	dim3 grid((per_row + 127) / 128, p.n_mes);
-	f3d_inf_kernel<<<grid, 128, 0, env.stream>>>(p);
+	const long long items = (long long)((p.n_fil + 3) / 4) * p.n_mes;
+	const long long want = (items + 255) / 256;
+	const int blocks = int(want < (long long)env.num_sms * 32 ? want : (long long)env.num_sms * 32);
+	f3d_inf_kernel<<<blocks, 256, 0, env.stream>>>(p);
 	count_launch();
 	return cudaGetLastError();
 }

@@ -103,12 +103,26 @@ __device__ __forceinline__ void write_induce(const P3DInduceProblem& p,
 	}
 }
 
+// Accumulators per target (registers, FP32, reset every tile):
+//   VEL only : u  = sum G c,            c  = d x alpha_s
+//   DV       : A' = sum G da,           da = alpha_s - alpha_t
+//              B  = sum K (alpha_t.c') d, c' = d x da
+//   VEL + DV : also u' = sum G c' and W = sum G d; since d x alpha_s =
+//              c' + d x alpha_t, the velocity partial of a tile is
+//              u' + W x alpha_t, formed once per tile.
+// Working with da rather than alpha_s keeps the stretching terms free of the
+// cancellation of nearly parallel vorticity: alpha_t x alpha_s = alpha_t x da
+// and alpha_t.(d x alpha_s) = alpha_t.c' hold exactly, and da, c' are small
+// when the cross products are.
+// Shared state per target (compensated across tiles): u (3, VEL), A' and B
+// (6, DV).
 template <Reg R, bool VEL, bool DV, int TPT, int NT>
 __global__ void __launch_bounds__(NT)
 p3d_induce_kernel(const P3DInduceProblem p, const InduceConsts kc,
 	double* __restrict__ partial, int src_per_split, unsigned* err)
 {
-	constexpr int NC = (VEL ? 3 : 0) + (DV ? 6 : 0);
+	constexpr int NC = (VEL ? 3 : 0) + (DV ? 6 : 0);     // compensated sums
+	constexpr int NR = (VEL ? (DV ? 6 : 3) : 0) + (DV ? 6 : 0);  // register partials
 	constexpr bool kFinite = FiniteAtZero<R>::value;
 	extern __shared__ __align__(16) unsigned char smem[];
 	float* hi = reinterpret_cast<float*>(smem + Stream2::kSmemBytes);
@@ -139,9 +153,9 @@ p3d_induce_kernel(const P3DInduceProblem p, const InduceConsts kc,
 	for (int i = 0; i < NC * TPT; ++i) { hi[i * NT + tid] = 0.f; lo[i * NT + tid] = 0.f; }
 
 	auto tile_fn = [&](const float4* __restrict__ st, int cnt) {
-		float acc[NC][TPT];
+		float acc[NR][TPT];
 #pragma unroll
-		for (int c = 0; c < NC; ++c)
+		for (int c = 0; c < NR; ++c)
 #pragma unroll
 			for (int k = 0; k < TPT; ++k) acc[c][k] = 0.f;
 
@@ -154,31 +168,41 @@ p3d_induce_kernel(const P3DInduceProblem p, const InduceConsts kc,
 				const float dy = ty[k] - sp.y;
 				const float dz = tz[k] - sp.z;
 				const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-				// c = d x alpha_s
-				const float cx = fmaf(dy, sv.z, -dz * sv.y);
-				const float cy = fmaf(dz, sv.x, -dx * sv.z);
-				const float cz = fmaf(dx, sv.y, -dy * sv.x);
 				if (DV) {
+					const float ex = sv.x - ax[k];
+					const float ey = sv.y - ay[k];
+					const float ez = sv.z - az[k];
+					// c' = d x da
+					const float cx = fmaf(dy, ez, -dz * ey);
+					const float cy = fmaf(dz, ex, -dx * ez);
+					const float cz = fmaf(dx, ey, -dy * ex);
 					float G, K;
 					RegP3D<R>::gk(r2, kc.rc, G, K);
 					const bool nz = r2 > 0.f;
 					G = nz ? G : 0.f;
 					if (!kFinite) K = nz ? K : 0.f;
+					constexpr int o = VEL ? 6 : 0;
 					if (VEL) {
 						acc[0][k] = fmaf(G, cx, acc[0][k]);
 						acc[1][k] = fmaf(G, cy, acc[1][k]);
 						acc[2][k] = fmaf(G, cz, acc[2][k]);
+						acc[3][k] = fmaf(G, dx, acc[3][k]);
+						acc[4][k] = fmaf(G, dy, acc[4][k]);
+						acc[5][k] = fmaf(G, dz, acc[5][k]);
 					}
-					constexpr int o = VEL ? 3 : 0;
-					acc[o + 0][k] = fmaf(G, sv.x, acc[o + 0][k]);
-					acc[o + 1][k] = fmaf(G, sv.y, acc[o + 1][k]);
-					acc[o + 2][k] = fmaf(G, sv.z, acc[o + 2][k]);
+					acc[o + 0][k] = fmaf(G, ex, acc[o + 0][k]);
+					acc[o + 1][k] = fmaf(G, ey, acc[o + 1][k]);
+					acc[o + 2][k] = fmaf(G, ez, acc[o + 2][k]);
 					const float pd = fmaf(az[k], cz, fmaf(ay[k], cy, ax[k] * cx));
 					const float kk = K * pd;
 					acc[o + 3][k] = fmaf(kk, dx, acc[o + 3][k]);
 					acc[o + 4][k] = fmaf(kk, dy, acc[o + 4][k]);
 					acc[o + 5][k] = fmaf(kk, dz, acc[o + 5][k]);
 				} else {
+					// c = d x alpha_s
+					const float cx = fmaf(dy, sv.z, -dz * sv.y);
+					const float cy = fmaf(dz, sv.x, -dx * sv.z);
+					const float cz = fmaf(dx, sv.y, -dy * sv.x);
 					float G = RegP3D<R>::g(r2, kc.rc);
 					if (!kFinite) G = r2 > 0.f ? G : 0.f;
 					acc[0][k] = fmaf(G, cx, acc[0][k]);
@@ -194,15 +218,27 @@ p3d_induce_kernel(const P3DInduceProblem p, const InduceConsts kc,
 #pragma unroll 1
 			for (int j = 0; j < cnt; ++j) body(j);
 		}
+		if (VEL && DV) {
+			// tile velocity u' + W x alpha_t into slots 0..2
 #pragma unroll
-		for (int c = 0; c < NC; ++c)
+			for (int k = 0; k < TPT; ++k) {
+				const float wx = acc[3][k], wy = acc[4][k], wz = acc[5][k];
+				acc[0][k] += fmaf(wy, az[k], -wz * ay[k]);
+				acc[1][k] += fmaf(wz, ax[k], -wx * az[k]);
+				acc[2][k] += fmaf(wx, ay[k], -wy * ax[k]);
+			}
+		}
+#pragma unroll
+		for (int c = 0; c < NC; ++c) {
+			const int src_c = (VEL && DV && c >= 3) ? c + 3 : c;
 #pragma unroll
 			for (int k = 0; k < TPT; ++k) {
 				const int i = (c * TPT + k) * NT + tid;
 				float h = hi[i], l = lo[i];
-				fold_twosum(h, l, acc[c][k]);
+				fold_twosum(h, l, acc[src_c][k]);
 				hi[i] = h; lo[i] = l;
 			}
+		}
 	};
 
 	if (!Stream2::run(smem, p.src, s_begin, n_s, err, tile_fn)) return;

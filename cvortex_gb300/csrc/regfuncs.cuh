@@ -8,9 +8,9 @@
 //   P3D induced velocity (src/P3D.cpp:51-72):
 //     u_t = S_vel * sum_s Gs * (d x alpha_s)
 //   P3D vortex stretching (src/P3D.cpp:86-114), with c = d x alpha_s:
-//     dalpha_t = S_dv * [ alpha_t x sum_s Gs alpha_s
+//     dalpha_t = S_dv * [ alpha_t x sum_s Gs (alpha_s - alpha_t)
 //                         + K_scale * sum_s Ks (alpha_t . c) d ]
-//     because d.(alpha_t x alpha_s) = -alpha_t.c.
+//     because d.(alpha_t x alpha_s) = -alpha_t.c and alpha_t x alpha_t = 0.
 //   P3D viscous exchange (src/P3D.cpp:116-144):
 //     S_visc * sum_s Es * (alpha_s V_t - alpha_t V_s)
 //   P2D velocity (src/P2D.cpp:49-69): S_vel2 * sum_s Hs * Gamma_s (dy, -dx)
@@ -22,7 +22,8 @@
 // (r2 == 0) are masked to zero by the callers, as the reference does.
 //
 // Winckelmans, rewritten with q = x2 + 1 and s = q^-1/2 (no cancellation):
-//   g/rho^3 = (q + 1.5) s^5,  (3 g/rho^3 - zeta)/rho^2 = (3 q + 7.5) s^7,
+//   g/rho^3 = (q + 1.5) s^5 = s^3 (1 + 1.5 s^2),
+//   (3 g/rho^3 - zeta)/rho^2 = (3 q + 7.5) s^7 = s^5 (3 + 7.5 s^2),
 //   eta3 = 52.5 s^9,  g2/rho^2 = (q + 1) s^4.
 // Gaussian 3D: the reference's Abramowitz & Stegun 7.1.26 erf (with g = 1 for
 // rho > 6) is used for rho >= rho_c; below rho_c, where erf minus its
@@ -58,7 +59,7 @@ template <Reg R> struct RegP3D;
 template <> struct RegP3D<Reg::Singular> {
 	// Gs = 1/r^3, Ks = 1/r^5 (K_scale = 3)
 	__device__ __forceinline__ static void gk(float r2, const RegConsts&, float& G, float& K) {
-		const float ir = rsqrt_approx(r2);
+		const float ir = rsqrt_refined(r2);
 		const float ir2 = ir * ir;
 		G = ir * ir2;
 		K = G * ir2;
@@ -71,20 +72,21 @@ template <> struct RegP3D<Reg::Singular> {
 
 // ---- Winckelmans (high-order algebraic) ---------------------------------
 template <> struct RegP3D<Reg::Winckelmans> {
-	// Gs = (q+1.5) s^5, Ks = (3q+7.5) s^7 (K_scale = 1/sigma^2)
+	// Gs = (q+1.5) s^5 = s^3 (1 + 1.5 s^2), Ks = (3q+7.5) s^7 = s^5 (3 + 7.5 s^2)
+	// (q s^2 = 1; K_scale = 1/sigma^2)
 	__device__ __forceinline__ static void gk(float r2, const RegConsts& c, float& G, float& K) {
 		const float q = fmaf(r2, c.inv_s2, 1.f);
 		const float s = rsqrt_approx(q);
 		const float s2 = s * s;
-		const float s5 = s2 * s2 * s;
-		G = (q + 1.5f) * s5;
-		K = fmaf(q, 3.f, 7.5f) * (s5 * s2);
+		const float s3 = s2 * s;
+		G = s3 * fmaf(1.5f, s2, 1.f);
+		K = (s3 * s2) * fmaf(7.5f, s2, 3.f);
 	}
 	__device__ __forceinline__ static float g(float r2, const RegConsts& c) {
 		const float q = fmaf(r2, c.inv_s2, 1.f);
 		const float s = rsqrt_approx(q);
 		const float s2 = s * s;
-		return (q + 1.5f) * (s2 * s2 * s);
+		return (s2 * s) * fmaf(1.5f, s2, 1.f);
 	}
 	// eta3 / 52.5 = s^9
 	__device__ __forceinline__ static float eta(float r2, const RegConsts& c) {
@@ -101,7 +103,7 @@ template <> struct RegP3D<Reg::Planetary> {
 	// inside: Gs = 1/|sigma|^3, Ks = 0; outside: Gs = 1/r^3, Ks = 1/r^5
 	// (K_scale = 3)
 	__device__ __forceinline__ static void gk(float r2, const RegConsts& c, float& G, float& K) {
-		const float ir = rsqrt_approx(r2);
+		const float ir = rsqrt_refined(r2);
 		const float ir2 = ir * ir;
 		const float ir3 = ir * ir2;
 		const bool inside = r2 < c.s2;
@@ -141,16 +143,19 @@ struct GaussSeries {
 };
 
 template <> struct RegP3D<Reg::Gaussian> {
-	// Reference A&S form of g (src/VortFunc.cpp:155-176) for rho >= rho_c.
-	__device__ __forceinline__ static float g_as(float rho) {
-		if (rho > 6.f) return 1.f;
+	// Reference A&S form of g (src/VortFunc.cpp:155-176) for rho >= rho_c,
+	// given rho and e = exp(-rho^2/2). In this range g = 1 - e (poly + rho
+	// sqrt(2/pi)) still cancels (by ~30x at rho = 0.5), so the rounding inside
+	// it matters: t and e are evaluated correctly rounded, as the reference
+	// does. Perturbations of rho itself are not amplified, so rho and its
+	// inverse powers come from one approximate rsqrt.
+	__device__ __forceinline__ static float g_as(float rho, float e) {
 		const float a1 = 0.254829592f, a2 = -0.284496736f, a3 = 1.421413741f;
 		const float a4 = -1.453152027f, a5 = 1.061405429f, p = 0.3275911f;
-		const float x = rho * kRecipSqrt2;
-		const float t = 1.f / fmaf(p, x, 1.f);
+		const float t = __frcp_rn(fmaf(p, rho * kRecipSqrt2, 1.f));
 		const float poly = t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, a5, a4), a3), a2), a1);
-		const float e = expf(-x * x);
-		return (1.f - poly * e) - rho * kSqrt2OverPi * e;
+		const float g = (1.f - poly * e) - rho * kSqrt2OverPi * e;
+		return rho > 6.f ? 1.f : g;
 	}
 	// Gs = g/rho^3, Ks = (3 Gs - zeta)/rho^2 (K_scale = 1/sigma^2)
 	__device__ __forceinline__ static void gk(float r2, const RegConsts& c, float& G, float& K) {
@@ -159,18 +164,18 @@ template <> struct RegP3D<Reg::Gaussian> {
 			G = GaussSeries::G(x2);
 			K = GaussSeries::K(x2);
 		} else {
-			const float rho = sqrtf(x2);
-			const float inv_rho3 = 1.f / (x2 * rho);
-			G = g_as(rho) * inv_rho3;
-			const float zeta = kSqrt2OverPi * expf(-0.5f * x2);
-			K = (3.f * G - zeta) / x2;
+			const float s = rsqrt_approx(x2);   // 1/rho
+			const float s2 = s * s;
+			const float e = expf(-0.5f * x2);
+			G = g_as(x2 * s, e) * (s2 * s);
+			K = fmaf(3.f, G, -kSqrt2OverPi * e) * s2;
 		}
 	}
 	__device__ __forceinline__ static float g(float r2, const RegConsts& c) {
 		const float x2 = r2 * c.inv_s2;
 		if (x2 < c.rho_c2) return GaussSeries::G(x2);
-		const float rho = sqrtf(x2);
-		return g_as(rho) / (x2 * rho);
+		const float s = rsqrt_approx(x2);
+		return g_as(x2 * s, expf(-0.5f * x2)) * (s * s * s);
 	}
 	// eta3 / sqrt(2/pi) = exp(-x2/2)
 	__device__ __forceinline__ static float eta(float r2, const RegConsts& c) {

@@ -1,0 +1,44 @@
+"""Parity assertions shared by the GPU tests.
+
+Bar: relative L2 error <= 1e-5 per output array against the reference path.
+
+Gaussian regularisation: below rho_c the kernels evaluate g/rho^3 and
+(3 g/rho^3 - zeta)/rho^2 from their exact series, where the reference's erf
+approximation cancels (reference src/VortFunc.cpp:164-174). For that
+regularisation parity is asserted on targets with no source closer than
+rho_c * |sigma|, and, when an FP64 result is given, the GPU's error against
+FP64 on all targets must not exceed the reference's own.
+"""
+import numpy as np
+
+from oracle import exact
+
+TOL = 1e-5
+
+
+def min_rho(src_xyz, tgt_xyz, sigma):
+    """Smallest nonzero separation / |sigma| from each target to the sources."""
+    s = np.asarray(src_xyz, np.float64)
+    out = np.empty(len(tgt_xyz))
+    for i, t in enumerate(np.asarray(tgt_xyz, np.float64)):
+        r2 = ((s - t) ** 2).sum(axis=1)
+        r2 = r2[r2 > 0]
+        out[i] = np.sqrt(r2.min()) / abs(sigma) if len(r2) else np.inf
+    return out
+
+
+def check(got, want, reg=None, tgt_xyz=None, src_xyz=None, sigma=None, fp64=None, tol=TOL,
+          rho_c=0.5):
+    got = np.asarray(got)
+    assert np.all(np.isfinite(got)), "non-finite output"
+    if reg != "gaussian" or tgt_xyz is None:
+        e = exact.rel_l2(got, want)
+        assert e <= tol, f"rel L2 vs reference {e:.3e}"
+        return
+    keep = min_rho(src_xyz, tgt_xyz, sigma) >= rho_c
+    if keep.any():
+        e = exact.rel_l2(got[keep], np.asarray(want)[keep])
+        assert e <= tol, f"rel L2 vs reference on {keep.sum()} unaffected targets {e:.3e}"
+    if fp64 is not None:
+        e_gpu, e_ref = exact.rel_l2(got, fp64), exact.rel_l2(want, fp64)
+        assert e_gpu <= max(e_ref, 1e-6) * 1.05, f"vs FP64: gpu {e_gpu:.3e}, reference {e_ref:.3e}"

@@ -12,14 +12,13 @@ import oracle
 from conftest import REGS
 from cvortex_gb300 import abi, workloads
 from oracle import exact
+from parity import check
 
 pytestmark = pytest.mark.gpu
 
 
 def close(a, b, tol=1e-5):
-    assert np.all(np.isfinite(a))
-    e = exact.rel_l2(a, b)
-    assert e <= tol, e
+    check(a, b, tol=tol)
 
 
 def test_no_sources_gives_zeros(gpu):
@@ -46,8 +45,10 @@ def test_coincident_distinct_particles(gpu, reg):
     p["coord"][300:] = p["coord"][:300]          # 300 exact twins, different vorticity
     vel = gpu.p3d_vel(p, p["coord"], reg, 0.2)
     dv = gpu.p3d_dvort(p, p, reg, 0.2, same=True)
-    close(vel, oracle.p3d_vel(p, p["coord"], reg, 0.2))
-    close(dv, oracle.p3d_dvort(p, p, reg, 0.2))
+    x = p["coord"]
+    ev, ed = exact.p3d_vel_dvort(p, x, p["vorticity"], reg, 0.2)
+    check(vel, oracle.p3d_vel(p, x, reg, 0.2), reg, x, x, 0.2, ev)
+    check(dv, oracle.p3d_dvort(p, p, reg, 0.2), reg, x, x, 0.2, ed)
 
 
 def test_aliased_and_copied_targets_agree(gpu):
@@ -61,8 +62,10 @@ def test_aliased_and_copied_targets_agree(gpu):
 def test_few_targets_many_sources(gpu, reg):
     p = workloads.vortex_ring(60_000, seed=43)
     q = workloads.vortex_ring(3, seed=44)
-    close(gpu.p3d_vel(p, q["coord"], reg, 0.05), oracle.p3d_vel(p, q["coord"], reg, 0.05))
-    close(gpu.p3d_dvort(p, q, reg, 0.05), oracle.p3d_dvort(p, q, reg, 0.05))
+    x, y = p["coord"], q["coord"]
+    ev, ed = exact.p3d_vel_dvort(p, y, q["vorticity"], reg, 0.05)
+    check(gpu.p3d_vel(p, y, reg, 0.05), oracle.p3d_vel(p, y, reg, 0.05), reg, y, x, 0.05, ev)
+    check(gpu.p3d_dvort(p, q, reg, 0.05), oracle.p3d_dvort(p, q, reg, 0.05), reg, y, x, 0.05, ed)
 
 
 def test_many_targets_few_sources(gpu):
@@ -74,8 +77,11 @@ def test_many_targets_few_sources(gpu):
 @pytest.mark.parametrize("reg", REGS)
 def test_negative_sigma(gpu, reg):
     p = workloads.uniform_cube(700, seed=47)
-    close(gpu.p3d_vel(p, p["coord"], reg, -0.2), oracle.p3d_vel(p, p["coord"], reg, -0.2))
-    close(gpu.p3d_dvort(p, p, reg, -0.2, same=True), oracle.p3d_dvort(p, p, reg, -0.2))
+    x = p["coord"]
+    ev, ed = exact.p3d_vel_dvort(p, x, p["vorticity"], reg, -0.2)
+    check(gpu.p3d_vel(p, x, reg, -0.2), oracle.p3d_vel(p, x, reg, -0.2), reg, x, x, -0.2, ev)
+    check(gpu.p3d_dvort(p, p, reg, -0.2, same=True), oracle.p3d_dvort(p, p, reg, -0.2), reg, x, x,
+          -0.2, ed)
 
 
 def test_visc_without_eta_returns_zeros(gpu):

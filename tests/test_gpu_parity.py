@@ -16,43 +16,16 @@ import oracle
 from conftest import REGS, golden
 from cvortex_gb300 import workloads
 from oracle import exact
+from parity import TOL, check as _check
 
 pytestmark = pytest.mark.gpu
-TOL = 1e-5
 
 
-def min_rho(src_xyz, tgt_xyz, sigma):
-    """Smallest nonzero separation / |sigma| from each target to the sources."""
-    s = np.asarray(src_xyz, np.float64)
-    out = np.empty(len(tgt_xyz))
-    for i, t in enumerate(np.asarray(tgt_xyz, np.float64)):
-        r = np.sqrt(((s - t) ** 2).sum(axis=1))
-        r = r[r > 0]
-        out[i] = r.min() / abs(sigma) if len(r) else np.inf
-    return out
-
-
-def check(got, want, reg, tgt_xyz=None, src_xyz=None, sigma=None, fp64=None, tol=TOL):
-    assert np.all(np.isfinite(got))
-    if reg != "gaussian" or tgt_xyz is None:
-        e = exact.rel_l2(got, want)
-        assert e <= tol, f"rel L2 vs reference {e:.3e}"
-        return
-    rc = oracle_rho_c()
-    keep = min_rho(src_xyz, tgt_xyz, sigma) >= rc
-    if keep.any():
-        e = exact.rel_l2(got[keep], want[keep])
-        assert e <= tol, f"rel L2 vs reference on unaffected targets {e:.3e}"
-    if fp64 is not None:
-        e_gpu, e_ref = exact.rel_l2(got, fp64), exact.rel_l2(want, fp64)
-        assert e_gpu <= max(e_ref, 1e-6) * 1.05, f"gpu {e_gpu:.3e} vs ref {e_ref:.3e} (fp64)"
+def check(got, want, reg=None, tgt_xyz=None, src_xyz=None, sigma=None, fp64=None, tol=TOL):
+    _check(got, want, reg, tgt_xyz, src_xyz, sigma, fp64, tol, rho_c=_RHO_C.get("v", 0.5))
 
 
 _RHO_C = {}
-
-
-def oracle_rho_c():
-    return _RHO_C.get("v", 0.5)
 
 
 @pytest.fixture(autouse=True)
