@@ -134,6 +134,7 @@ _EXT_SIGS = {
     "cvtx_gb300_dev_P3D_M2M_visc": (_i, [_vp, _i, _vp, _i, _i, _vp, _i, _f, _f, _vp]),
     "cvtx_gb300_dev_P2D_M2M_vel": (_i, [_vp, _i, _vp, _i, _vp, _i, _f, _vp]),
     "cvtx_gb300_dev_F3D_M2M_vel": (_i, [_vp, _i, _vp, _i, _i, _vp, _vp]),
+    "cvtx_gb300_dev_P3D_M2M_noalloc": (_i, [_vp, _i, _vp, _i, _i, _vp, _vp, _i, _f, _vp]),
     "cvtx_gb300_dev_status": (_i, [_vp]),
     "cvtx_gb300_probe_fp32_tflops": (_i, [_i, C.POINTER(C.c_double)]),
     "cvtx_gb300_dev_pack_P3D": (_i, [_vp, _i, _vp, _vp]),

@@ -103,6 +103,11 @@ void set_gaussian_rho_c(float rho_c);
 size_t p3d_induce_ws_bytes(int reg, unsigned ops, int n_src, int n_tgt, int num_sms);
 cudaError_t p3d_induce(int reg, unsigned ops, const P3DInduceProblem& p, const LaunchEnv& env);
 
+// As p3d_induce, with the source-split count capped so that the partial sums
+// fit env.ws_bytes (a fixed scratch area); never needs more than that.
+cudaError_t p3d_induce_bounded(int reg, unsigned ops, const P3DInduceProblem& p,
+	const LaunchEnv& env);
+
 size_t p3d_visc_ws_bytes(int reg, int n_src, int n_tgt, int num_sms);
 cudaError_t p3d_visc(int reg, const P3DViscProblem& p, const LaunchEnv& env);
 

@@ -566,6 +566,48 @@ cudaError_t induce_ops(unsigned ops, const P3DInduceProblem& p, const LaunchEnv&
 	}
 }
 
+// The same launch with the number of source splits capped so that the FP64
+// split partials fit the workspace the caller supplies (env.ws_bytes), for
+// callers that provide a fixed scratch area instead of a sized one.
+template <Reg R, bool VEL, bool DV, int TPT, int NT>
+cudaError_t launch_induce_bounded(const P3DInduceProblem& p, const LaunchEnv& env) {
+	constexpr int NC = (VEL ? 3 : 0) + (DV ? 6 : 0);
+	constexpr size_t smem = smem_bytes<TPT, NT, NC>();
+	static const int occ = resident_ctas(p3d_induce_kernel<R, VEL, DV, TPT, NT>, NT, smem);
+	const size_t per_split = size_t(NC) * size_t(p.n_tgt) * sizeof(double);
+	size_t cap = env.ws_bytes / per_split;
+	cap = cap < 1 ? 1 : (cap > 64 ? 64 : cap);
+	const Plan pl = make_plan(p.n_src, p.n_tgt, TPT * NT, kTile, NC, env.num_sms * occ, smem,
+		int(cap));
+	if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
+	const InduceConsts kc = make_induce_consts(int(R), p.sigma);
+	double* partial = static_cast<double*>(env.ws);
+	p3d_induce_kernel<R, VEL, DV, TPT, NT><<<dim3(pl.n_tblocks, pl.n_split), NT, pl.smem,
+		env.stream>>>(p, kc, partial, pl.src_per_split, env.err);
+	count_launch();
+	if (pl.n_split > 1) {
+		p3d_induce_finalize<VEL, DV><<<(p.n_tgt + 255) / 256, 256, 0, env.stream>>>(
+			p, kc, partial, pl.n_split);
+		count_launch();
+	}
+	return cudaGetLastError();
+}
+
+template <Reg R, bool VEL, bool DV>
+cudaError_t induce_bounded_r(const P3DInduceProblem& p, const LaunchEnv& env) {
+	if (p.n_tgt < kSmallTargets) return launch_induce_bounded<R, VEL, DV, 1, 128>(p, env);
+	return launch_induce_bounded<R, VEL, DV, 4, 128>(p, env);
+}
+
+template <Reg R>
+cudaError_t induce_bounded_ops(unsigned ops, const P3DInduceProblem& p, const LaunchEnv& env) {
+	switch (ops) {
+	case kOpVel: return induce_bounded_r<R, true, false>(p, env);
+	case kOpDvort: return induce_bounded_r<R, false, true>(p, env);
+	default: return induce_bounded_r<R, true, true>(p, env);
+	}
+}
+
 template <Reg R, int TPT, int NT>
 Plan plan_visc(int n_src, int n_tgt, int num_sms) {
 	constexpr size_t smem = smem_bytes<TPT, NT, 3>();
@@ -641,6 +683,18 @@ cudaError_t p3d_induce(int reg, unsigned ops, const P3DInduceProblem& p, const L
 	case 1: return induce_ops<Reg::Winckelmans>(ops, p, env);
 	case 2: return induce_ops<Reg::Planetary>(ops, p, env);
 	case 3: return induce_ops<Reg::Gaussian>(ops, p, env);
+	default: return cudaErrorInvalidValue;
+	}
+}
+
+cudaError_t p3d_induce_bounded(int reg, unsigned ops, const P3DInduceProblem& p,
+	const LaunchEnv& env) {
+	if (p.n_tgt <= 0) return cudaSuccess;
+	switch (reg) {
+	case 0: return induce_bounded_ops<Reg::Singular>(ops, p, env);
+	case 1: return induce_bounded_ops<Reg::Winckelmans>(ops, p, env);
+	case 2: return induce_bounded_ops<Reg::Planetary>(ops, p, env);
+	case 3: return induce_bounded_ops<Reg::Gaussian>(ops, p, env);
 	default: return cudaErrorInvalidValue;
 	}
 }

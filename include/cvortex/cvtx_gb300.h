@@ -71,6 +71,19 @@ CVTX_EXPORT int cvtx_gb300_dev_P2D_M2M_vel(const void* src, int n_src,
 	float regularisation_radius, void* stream);
 CVTX_EXPORT int cvtx_gb300_dev_F3D_M2M_vel(const void* fil, int n_fil,
 	const void* tgt, int tgt_stride, int n_tgt, float* out, void* stream);
+/* cvtx_gb300_dev_P3D_M2M without any device allocation. It has no
+ * counterpart in the reference. For callers that cannot let a library call
+ * cudaMalloc: device memory owned by one pool reserved up front, or loops
+ * that cannot take the latency and synchronisation of cudaMalloc/cudaFree.
+ * Split partial sums live in a fixed 32 MiB scratch area inside the library
+ * image (held in every GPU's memory while the library is loaded); at most
+ * 233,016 targets per call (more: returns -1 with a message), any number of
+ * sources. Calls that overlap on the GPU share that scratch and race. The
+ * first call on a device resolves the scratch address and should precede any
+ * stream capture. A device-side wait expiry turns the outputs into NaN. */
+CVTX_EXPORT int cvtx_gb300_dev_P3D_M2M_noalloc(const void* src, int n_src,
+	const void* tgt, int tgt_stride, int n_tgt, float* vel_out,
+	float* dvort_out, int reg, float regularisation_radius, void* stream);
 /* Synchronise `stream`, then read and reset the device error word. Returns 0
  * if no device-side wait expired since the previous check. */
 CVTX_EXPORT int cvtx_gb300_dev_status(void* stream);
