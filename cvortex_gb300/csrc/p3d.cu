@@ -15,6 +15,7 @@
 // it writes FP64 partials that a finalize kernel combines in split order.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <mutex>
 #include "nbody.h"
 #include "plan.cuh"
@@ -259,6 +260,167 @@ p3d_induce_kernel(const P3DInduceProblem p, const InduceConsts kc,
 #pragma unroll
 			for (int c = 0; c < NC; ++c)
 				partial[(size_t(blockIdx.y) * NC + c) * p.n_tgt + t] = s[c];
+		}
+	}
+}
+
+// Packed variant of p3d_induce_kernel for VEL+DV and DV with an even number
+// of targets per thread: targets (2h, 2h+1) of a thread share one float2 lane
+// pair, so every per-pair FP32 operation (except rsqrt and the coincidence
+// select) is one f32x2 instruction for two interactions. Same sums, same
+// order of operations per target as the scalar kernel.
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+
+template <Reg R, bool VEL, bool DV, int TPT, int NT>
+__global__ void __launch_bounds__(NT)
+p3d_induce2_kernel(const P3DInduceProblem p, const InduceConsts kc,
+	double* __restrict__ partial, int src_per_split, unsigned* err)
+{
+	static_assert(DV && TPT % 2 == 0, "packed kernel: stretching, even TPT");
+	constexpr int H = TPT / 2;
+	constexpr int NC = (VEL ? 3 : 0) + 6;
+	constexpr int NR = (VEL ? 6 : 0) + 6;
+	constexpr bool kFinite = FiniteAtZero<R>::value;
+	extern __shared__ __align__(16) unsigned char smem[];
+	float* hi = reinterpret_cast<float*>(smem + Stream2::kSmemBytes);
+	float* lo = hi + NC * TPT * NT;
+
+	const int tid = threadIdx.x;
+	const int tbase = blockIdx.x * (TPT * NT);
+	const int s_begin = blockIdx.y * src_per_split;
+	int n_s = p.n_src - s_begin;
+	n_s = n_s < src_per_split ? n_s : src_per_split;
+	n_s = n_s > 0 ? n_s : 0;
+
+	float2 tx[H], ty[H], tz[H], ax[H], ay[H], az[H];
+#pragma unroll
+	for (int h = 0; h < H; ++h) {
+		float4 q[2], v[2];
+#pragma unroll
+		for (int e = 0; e < 2; ++e) {
+			int t = tbase + (2 * h + e) * NT + tid;
+			t = t < p.n_tgt ? t : p.n_tgt - 1;
+			q[e] = p.tgt[size_t(t) * p.tstride];
+			v[e] = p.tgt[size_t(t) * p.tstride + 1];
+		}
+		tx[h] = make_float2(q[0].x, q[1].x); ty[h] = make_float2(q[0].y, q[1].y);
+		tz[h] = make_float2(q[0].z, q[1].z);
+		ax[h] = make_float2(v[0].x, v[1].x); ay[h] = make_float2(v[0].y, v[1].y);
+		az[h] = make_float2(v[0].z, v[1].z);
+	}
+#pragma unroll
+	for (int i = 0; i < NC * TPT; ++i) { hi[i * NT + tid] = 0.f; lo[i * NT + tid] = 0.f; }
+
+	auto tile_fn = [&](const float4* __restrict__ st, int cnt) {
+		float2 acc[NR][H];
+#pragma unroll
+		for (int c = 0; c < NR; ++c)
+#pragma unroll
+			for (int h = 0; h < H; ++h) acc[c][h] = make_float2(0.f, 0.f);
+
+		auto body = [&](int j) {
+			const float4 sp = st[2 * j];
+			const float4 sv = st[2 * j + 1];
+			const float2 nsx = bc2(-sp.x), nsy = bc2(-sp.y), nsz = bc2(-sp.z);
+			const float2 wx = bc2(sv.x), wy = bc2(sv.y), wz = bc2(sv.z);
+#pragma unroll
+			for (int h = 0; h < H; ++h) {
+				const float2 dx = __fadd2_rn(tx[h], nsx);
+				const float2 dy = __fadd2_rn(ty[h], nsy);
+				const float2 dz = __fadd2_rn(tz[h], nsz);
+				const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+				// da = alpha_s - alpha_t, c' = d x da
+				const float2 ex = __ffma2_rn(ax[h], bc2(-1.f), wx);
+				const float2 ey = __ffma2_rn(ay[h], bc2(-1.f), wy);
+				const float2 ez = __ffma2_rn(az[h], bc2(-1.f), wz);
+				const float2 cx = __ffma2_rn(dy, ez, neg2(__fmul2_rn(dz, ey)));
+				const float2 cy = __ffma2_rn(dz, ex, neg2(__fmul2_rn(dx, ez)));
+				const float2 cz = __ffma2_rn(dx, ey, neg2(__fmul2_rn(dy, ex)));
+				float2 G, K;
+				RegP3D2<R>::gk2(r2, kc.rc, G, K);
+				G.x = r2.x > 0.f ? G.x : 0.f;
+				G.y = r2.y > 0.f ? G.y : 0.f;
+				if (!kFinite) {
+					K.x = r2.x > 0.f ? K.x : 0.f;
+					K.y = r2.y > 0.f ? K.y : 0.f;
+				}
+				constexpr int o = VEL ? 6 : 0;
+				if (VEL) {
+					acc[0][h] = __ffma2_rn(G, cx, acc[0][h]);
+					acc[1][h] = __ffma2_rn(G, cy, acc[1][h]);
+					acc[2][h] = __ffma2_rn(G, cz, acc[2][h]);
+					acc[3][h] = __ffma2_rn(G, dx, acc[3][h]);
+					acc[4][h] = __ffma2_rn(G, dy, acc[4][h]);
+					acc[5][h] = __ffma2_rn(G, dz, acc[5][h]);
+				}
+				acc[o + 0][h] = __ffma2_rn(G, ex, acc[o + 0][h]);
+				acc[o + 1][h] = __ffma2_rn(G, ey, acc[o + 1][h]);
+				acc[o + 2][h] = __ffma2_rn(G, ez, acc[o + 2][h]);
+				const float2 pd = __ffma2_rn(az[h], cz, __ffma2_rn(ay[h], cy, __fmul2_rn(ax[h], cx)));
+				const float2 kk = __fmul2_rn(K, pd);
+				acc[o + 3][h] = __ffma2_rn(kk, dx, acc[o + 3][h]);
+				acc[o + 4][h] = __ffma2_rn(kk, dy, acc[o + 4][h]);
+				acc[o + 5][h] = __ffma2_rn(kk, dz, acc[o + 5][h]);
+			}
+		};
+		if (cnt == kTile) {
+#pragma unroll 2
+			for (int j = 0; j < kTile; ++j) body(j);
+		} else {
+#pragma unroll 1
+			for (int j = 0; j < cnt; ++j) body(j);
+		}
+		if (VEL) {
+#pragma unroll
+			for (int h = 0; h < H; ++h) {
+				const float2 wx_ = acc[3][h], wy_ = acc[4][h], wz_ = acc[5][h];
+				acc[0][h] = __fadd2_rn(acc[0][h], __ffma2_rn(wy_, az[h], neg2(__fmul2_rn(wz_, ay[h]))));
+				acc[1][h] = __fadd2_rn(acc[1][h], __ffma2_rn(wz_, ax[h], neg2(__fmul2_rn(wx_, az[h]))));
+				acc[2][h] = __fadd2_rn(acc[2][h], __ffma2_rn(wx_, ay[h], neg2(__fmul2_rn(wy_, ax[h]))));
+			}
+		}
+#pragma unroll
+		for (int c = 0; c < NC; ++c) {
+			const int src_c = (VEL && c >= 3) ? c + 3 : c;
+#pragma unroll
+			for (int h = 0; h < H; ++h) {
+#pragma unroll
+				for (int e = 0; e < 2; ++e) {
+					const int k = 2 * h + e;
+					const int i = (c * TPT + k) * NT + tid;
+					float hh = hi[i], ll = lo[i];
+					fold_twosum(hh, ll, e == 0 ? acc[src_c][h].x : acc[src_c][h].y);
+					hi[i] = hh; lo[i] = ll;
+				}
+			}
+		}
+	};
+
+	if (!Stream2::run(smem, p.src, s_begin, n_s, err, tile_fn)) return;
+
+#pragma unroll
+	for (int h = 0; h < H; ++h) {
+#pragma unroll
+		for (int e = 0; e < 2; ++e) {
+			const int k = 2 * h + e;
+			const int t = tbase + k * NT + tid;
+			if (t >= p.n_tgt) continue;
+			double sacc[NC];
+#pragma unroll
+			for (int c = 0; c < NC; ++c) {
+				const int i = (c * TPT + k) * NT + tid;
+				sacc[c] = double(hi[i]) + double(lo[i]);
+			}
+			const float tax = e == 0 ? ax[h].x : ax[h].y;
+			const float tay = e == 0 ? ay[h].x : ay[h].y;
+			const float taz = e == 0 ? az[h].x : az[h].y;
+			if (gridDim.y == 1) {
+				write_induce<VEL, DV>(p, kc, t, sacc, tax, tay, taz);
+			} else {
+#pragma unroll
+				for (int c = 0; c < NC; ++c)
+					partial[(size_t(blockIdx.y) * NC + c) * p.n_tgt + t] = sacc[c];
+			}
 		}
 	}
 }
@@ -508,11 +670,34 @@ constexpr size_t smem_bytes() {
 // counts use 1 so that the source dimension can be split across more CTAs.
 constexpr int kSmallTargets = 8192;
 
+// Packed (f32x2) kernel for stretching with an even number of targets per
+// thread; CVTX_GB300_SCALAR=1 in the environment selects the scalar kernel
+// (kept for comparison).
+bool use_packed() {
+	static const bool v = [] {
+		const char* e = std::getenv("CVTX_GB300_SCALAR");
+		return !(e && e[0] == '1');
+	}();
+	return v;
+}
+
+template <Reg R, bool VEL, bool DV, int TPT, int NT>
+struct InduceKernel {
+	using Fn = void (*)(const P3DInduceProblem, const InduceConsts, double*, int, unsigned*);
+	static constexpr bool kPackable = DV && (TPT % 2 == 0);
+	static Fn get() {
+		if constexpr (kPackable) {
+			if (use_packed()) return p3d_induce2_kernel<R, VEL, DV, TPT, NT>;
+		}
+		return p3d_induce_kernel<R, VEL, DV, TPT, NT>;
+	}
+};
+
 template <Reg R, bool VEL, bool DV, int TPT, int NT>
 Plan plan_induce(int n_src, int n_tgt, int num_sms) {
 	constexpr int NC = (VEL ? 3 : 0) + (DV ? 6 : 0);
 	constexpr size_t smem = smem_bytes<TPT, NT, NC>();
-	static const int occ = resident_ctas(p3d_induce_kernel<R, VEL, DV, TPT, NT>, NT, smem);
+	static const int occ = resident_ctas(InduceKernel<R, VEL, DV, TPT, NT>::get(), NT, smem);
 	return make_plan(n_src, n_tgt, TPT * NT, kTile, NC, num_sms * occ, smem);
 }
 
@@ -524,7 +709,7 @@ cudaError_t launch_induce(const P3DInduceProblem& p, const LaunchEnv& env) {
 	const InduceConsts kc = make_induce_consts(int(R), p.sigma);
 	double* partial = static_cast<double*>(env.ws);
 	dim3 grid(pl.n_tblocks, pl.n_split);
-	p3d_induce_kernel<R, VEL, DV, TPT, NT><<<grid, NT, pl.smem, env.stream>>>(
+	InduceKernel<R, VEL, DV, TPT, NT>::get()<<<grid, NT, pl.smem, env.stream>>>(
 		p, kc, partial, pl.src_per_split, env.err);
 	count_launch();
 	if (pl.n_split > 1) {
@@ -573,7 +758,7 @@ template <Reg R, bool VEL, bool DV, int TPT, int NT>
 cudaError_t launch_induce_bounded(const P3DInduceProblem& p, const LaunchEnv& env) {
 	constexpr int NC = (VEL ? 3 : 0) + (DV ? 6 : 0);
 	constexpr size_t smem = smem_bytes<TPT, NT, NC>();
-	static const int occ = resident_ctas(p3d_induce_kernel<R, VEL, DV, TPT, NT>, NT, smem);
+	static const int occ = resident_ctas(InduceKernel<R, VEL, DV, TPT, NT>::get(), NT, smem);
 	const size_t per_split = size_t(NC) * size_t(p.n_tgt) * sizeof(double);
 	size_t cap = env.ws_bytes / per_split;
 	cap = cap < 1 ? 1 : (cap > 64 ? 64 : cap);
@@ -582,7 +767,7 @@ cudaError_t launch_induce_bounded(const P3DInduceProblem& p, const LaunchEnv& en
 	if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
 	const InduceConsts kc = make_induce_consts(int(R), p.sigma);
 	double* partial = static_cast<double*>(env.ws);
-	p3d_induce_kernel<R, VEL, DV, TPT, NT><<<dim3(pl.n_tblocks, pl.n_split), NT, pl.smem,
+	InduceKernel<R, VEL, DV, TPT, NT>::get()<<<dim3(pl.n_tblocks, pl.n_split), NT, pl.smem,
 		env.stream>>>(p, kc, partial, pl.src_per_split, env.err);
 	count_launch();
 	if (pl.n_split > 1) {

@@ -32,25 +32,32 @@ __global__ void __launch_bounds__(256) fma_probe_kernel(float* out, float a, flo
 	if (s == 1.2345f) out[threadIdx.x] = s;   // keeps the chains live
 }
 
-}  // namespace
-}  // namespace cvtx
+// The same with packed two-wide FP32 FMAs (fma.rn.f32x2): one instruction
+// performs two FMAs, so the FMA peak is reached with half the issue slots.
+__global__ void __launch_bounds__(256) fma2_probe_kernel(float* out, float a, float b) {
+	float2 x[kChains / 2];
+	const float2 a2 = make_float2(a, a), b2 = make_float2(b, b);
+#pragma unroll
+	for (int c = 0; c < kChains / 2; ++c) x[c] = make_float2(float(threadIdx.x + c), float(c));
+#pragma unroll 4
+	for (int i = 0; i < kIters; ++i) {
+#pragma unroll
+		for (int c = 0; c < kChains / 2; ++c) x[c] = __ffma2_rn(x[c], a2, b2);
+	}
+	float s = 0.f;
+#pragma unroll
+	for (int c = 0; c < kChains / 2; ++c) s += x[c].x + x[c].y;
+	if (s == 1.2345f) out[threadIdx.x] = s;
+}
 
-extern "C" CVTX_EXPORT int cvtx_gb300_probe_fp32_tflops(int repeats, double* tflops) {
-	using namespace cvtx;
-	if (!tflops || repeats < 1) return -1;
-	std::lock_guard<std::recursive_mutex> g(Runtime::get().lock());
-	DeviceContext* c = Runtime::get().active_context();
-	if (!c) return -3;
-	float* out = nullptr;
-	cudaEvent_t e0 = nullptr, e1 = nullptr;
-	cudaError_t e = cudaMalloc(&out, 256 * sizeof(float));
-	if (e == cudaSuccess) e = cudaEventCreate(&e0);
-	if (e == cudaSuccess) e = cudaEventCreate(&e1);
+double run_probe(DeviceContext* c, float* out, cudaEvent_t e0, cudaEvent_t e1, int repeats,
+	bool packed, cudaError_t& e) {
 	const int blocks = c->num_sms * 8;
 	double best = 0.0;
 	for (int r = 0; r <= repeats && e == cudaSuccess; ++r) {
 		cudaEventRecord(e0, c->stream);
-		fma_probe_kernel<<<blocks, 256, 0, c->stream>>>(out, 0.999f, 1e-3f);
+		if (packed) fma2_probe_kernel<<<blocks, 256, 0, c->stream>>>(out, 0.999f, 1e-3f);
+		else fma_probe_kernel<<<blocks, 256, 0, c->stream>>>(out, 0.999f, 1e-3f);
 		count_launch();
 		cudaEventRecord(e1, c->stream);
 		e = cudaEventSynchronize(e1);
@@ -59,13 +66,45 @@ extern "C" CVTX_EXPORT int cvtx_gb300_probe_fp32_tflops(int repeats, double* tfl
 		const double flops = 2.0 * kChains * double(kIters) * 256.0 * blocks;
 		if (r > 0 && ms > 0.f) best = std::max(best, flops / (double(ms) * 1e-3) / 1e12);
 	}
+	return best;
+}
+
+}  // namespace
+}  // namespace cvtx
+
+// Both probes, best of `repeats` timed launches each (2 flops per FMA).
+extern "C" CVTX_EXPORT int cvtx_gb300_probe_fp32_detail(int repeats, double* scalar_fma,
+	double* packed_fma) {
+	using namespace cvtx;
+	if (!scalar_fma || !packed_fma || repeats < 1) return -1;
+	std::lock_guard<std::recursive_mutex> g(Runtime::get().lock());
+	DeviceContext* c = Runtime::get().active_context();
+	if (!c) return -3;
+	float* out = nullptr;
+	cudaEvent_t e0 = nullptr, e1 = nullptr;
+	cudaError_t e = cudaMalloc(&out, 256 * sizeof(float));
+	if (e == cudaSuccess) e = cudaEventCreate(&e0);
+	if (e == cudaSuccess) e = cudaEventCreate(&e1);
+	double scalar = 0.0, packed = 0.0;
+	if (e == cudaSuccess) scalar = run_probe(c, out, e0, e1, repeats, false, e);
+	if (e == cudaSuccess) packed = run_probe(c, out, e0, e1, repeats, true, e);
 	if (e0) cudaEventDestroy(e0);
 	if (e1) cudaEventDestroy(e1);
 	if (out) cudaFree(out);
 	if (e != cudaSuccess) {
-		set_error(std::string("cvtx_gb300_probe_fp32_tflops: ") + cudaGetErrorString(e));
+		set_error(std::string("cvtx_gb300_probe_fp32: ") + cudaGetErrorString(e));
 		return -2;
 	}
-	*tflops = best;
+	*scalar_fma = scalar;
+	*packed_fma = packed;
 	return 0;
+}
+
+// The FP32 FMA peak: the larger of the two probes.
+extern "C" CVTX_EXPORT int cvtx_gb300_probe_fp32_tflops(int repeats, double* tflops) {
+	if (!tflops) return -1;
+	double a = 0.0, b = 0.0;
+	const int rc = cvtx_gb300_probe_fp32_detail(repeats, &a, &b);
+	if (rc == 0) *tflops = a > b ? a : b;
+	return rc;
 }

@@ -183,6 +183,30 @@ template <> struct RegP3D<Reg::Gaussian> {
 	}
 };
 
+// ---- packed (f32x2) evaluation for two targets at once ---------------------
+// Blackwell executes fma/mul/add on float2 as one instruction (two FP32 ops),
+// halving the issue slots of the per-pair arithmetic. gk2 evaluates Gs, Ks
+// for the two halves of r2; the default runs the scalar code per half, the
+// Winckelmans specialisation stays packed except for the two rsqrt.
+__device__ __forceinline__ float2 bc2(float v) { return make_float2(v, v); }
+
+template <Reg R> struct RegP3D2 {
+	__device__ __forceinline__ static void gk2(float2 r2, const RegConsts& c, float2& G, float2& K) {
+		RegP3D<R>::gk(r2.x, c, G.x, K.x);
+		RegP3D<R>::gk(r2.y, c, G.y, K.y);
+	}
+};
+template <> struct RegP3D2<Reg::Winckelmans> {
+	__device__ __forceinline__ static void gk2(float2 r2, const RegConsts& c, float2& G, float2& K) {
+		const float2 q = __ffma2_rn(r2, bc2(c.inv_s2), bc2(1.f));
+		const float2 s = make_float2(rsqrt_approx(q.x), rsqrt_approx(q.y));
+		const float2 s2 = __fmul2_rn(s, s);
+		const float2 s3 = __fmul2_rn(s2, s);
+		G = __fmul2_rn(s3, __ffma2_rn(bc2(1.5f), s2, bc2(1.f)));
+		K = __fmul2_rn(__fmul2_rn(s3, s2), __ffma2_rn(bc2(7.5f), s2, bc2(3.f)));
+	}
+};
+
 // ---- 2D ------------------------------------------------------------------
 template <Reg R> struct RegP2D;
 

@@ -46,9 +46,13 @@ CVTX_EXPORT float cvtx_gb300_gaussian_rho_c(void);
 CVTX_EXPORT void cvtx_gb300_set_gaussian_rho_c(float rho_c);
 
 /* Measured FP32 FMA throughput (TFLOP/s, best of `repeats` timed launches of
- * a pure-FMA kernel filling every SM) of the first enabled accelerator: the
- * roofline denominator of the all-pairs kernels, which are FP32-pipe bound. */
+ * pure-FMA kernels filling every SM) of the first enabled accelerator: the
+ * roofline denominator of the all-pairs kernels, which are FP32-pipe bound.
+ * _tflops gives the larger of the scalar-FMA and packed (f32x2) FMA probes;
+ * _detail gives both. */
 CVTX_EXPORT int cvtx_gb300_probe_fp32_tflops(int repeats, double* tflops);
+CVTX_EXPORT int cvtx_gb300_probe_fp32_detail(int repeats, double* scalar_fma,
+	double* packed_fma);
 
 /* Velocity at and vortex stretching of every particle of one set, in one
  * pass over the pairs: equivalent to cvtx_P3D_M2M_vel(p, n, coords(p), n,
