@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--reg", default="winckelmans", choices=list(REG))
     ap.add_argument("--quick", action="store_true", help="skip the extra measurements")
     ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--serve-requests", type=int, default=64,
+                    help="requests per arrival rate in the served-stream measurement")
     return ap.parse_args()
 
 
@@ -277,6 +279,7 @@ def run_ours(args):
     }
     if rank == 0 and not args.quick:
         out["e2e"] = e2e_abi(cv, p, args)
+        out["serving"] = serve_extra(cv, lib, count=args.serve_requests)
         out["extras"] = extras(cv, lib, args, torch, sh, peak.value)
     if rank == 0 and world == 1:
         out["cpu_baseline"] = cpu_baseline(p, args.reg)
@@ -376,6 +379,7 @@ def extras(cv, lib, args, torch, sh, peak):
                                                o.data_ptr(), 3, SIGMA, sh)
     ms = timed_dev(f, torch, 5)
     res["p2d_patch200k_gaussian_vel"] = {"ginter_s": len(q) ** 2 / ms / 1e6}
+    res["batch512"] = batch_extra(cv, lib, torch, sh)
     m = 1_000_000
     big = workloads.uniform_cube(m)
     rb = torch.from_numpy(p3d_records(big).reshape(m, 8)).cuda()
@@ -387,6 +391,167 @@ def extras(cv, lib, args, torch, sh, peak):
     res["cube1M_winckelmans_veldvort"] = {
         "ginter_s": m * m / ms / 1e6, "ms": ms,
         "fp32_frac": 61 * m * m / (ms * 1e-3) / 1e12 / peak}
+    return res
+
+
+def batch_extra(cv, lib, torch, sh, count=512):
+    """512 independent vel+dvort problems (uniform cube each, Winckelmans,
+    sigma 0.05), sizes log-uniform in [1,000, 50,000]: one plain device call
+    per problem vs the batched persistent launch (autotuned, graph-captured)."""
+    from cvortex_gb300 import abi, workloads
+    sizes = workloads.batch_sizes(count)
+    keep, probs = [], []
+    for i, n in enumerate(sizes):
+        n = int(n)
+        p = workloads.uniform_cube(n, seed=10_000 + i)
+        rec = torch.from_numpy(p3d_records(p).reshape(n, 8)).cuda()
+        v = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+        d = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+        keep.append((n, rec, v, d))
+        probs.append(abi.cvtx_gb300_p3d_problem(rec.data_ptr(), n, rec.data_ptr(), 2, n,
+                                                v.data_ptr(), d.data_ptr(), SIGMA))
+    pairs = float(sum(int(n) * int(n) for n in sizes))
+
+    def plain():
+        for n, rec, v, d in keep:
+            rc = lib.cvtx_gb300_dev_P3D_M2M(rec.data_ptr(), n, rec.data_ptr(), 2, n, v.data_ptr(),
+                                            d.data_ptr(), 1, SIGMA, sh)
+            if rc != 0:
+                raise RuntimeError(cv.last_error())
+
+    ms_plain = timed_dev(plain, torch, 2)
+    arr = (abi.cvtx_gb300_p3d_problem * count)(*probs)
+    b = lib.cvtx_gb300_batch_create(arr, count, 1, 3)
+    if not b:
+        raise RuntimeError(cv.last_error())
+    try:
+        t0 = time.perf_counter()
+        if lib.cvtx_gb300_batch_tune(b, 1) != 0 or lib.cvtx_gb300_batch_capture(b) != 0:
+            raise RuntimeError(cv.last_error())
+        tune_s = time.perf_counter() - t0
+
+        def batched():
+            if lib.cvtx_gb300_batch_run(b, sh) != 0:
+                raise RuntimeError(cv.last_error())
+
+        ms_batch = timed_dev(batched, torch, 3)
+        if lib.cvtx_gb300_batch_status(b) != 0:
+            raise RuntimeError(cv.last_error())
+        tpt, nt, chunk, items, graph = (C.c_int() for _ in range(5))
+        lib.cvtx_gb300_batch_info(b, C.byref(tpt), C.byref(nt), C.byref(chunk), C.byref(items),
+                                  C.byref(graph), None)
+    finally:
+        lib.cvtx_gb300_batch_destroy(b)
+    return {"problems": count, "interactions": pairs,
+            "sizes": [int(sizes.min()), int(sizes.max())],
+            "plain_ms": ms_plain, "plain_ginter_s": pairs / ms_plain / 1e6,
+            "batched_ms": ms_batch, "batched_ginter_s": pairs / ms_batch / 1e6,
+            "speedup": ms_plain / ms_batch, "tuned_shape": [tpt.value, nt.value],
+            "tuned_chunk": chunk.value, "items": items.value, "graph": bool(graph.value),
+            "tune_s": tune_s}
+
+
+SERVE_RATES = (100, 300, 1000, 3000, 5000)
+
+
+def serve_extra(cv, lib, count=64, steps=10, dt=1e-3, rates=SERVE_RATES):
+    """Served mixed-size stream vs plain per-request ABI calls.
+
+    Stream: Poisson arrivals, 60% P3D vel+dvort (uniform cube, Winckelmans,
+    sigma 0.05), 25% P2D vel (Gaussian patch, Winckelmans), 15% F3D vel (wake
+    sheet on as many tracer points), sizes log-uniform on [500, 200,000],
+    `steps` resident forward-Euler steps per client. The same requests are
+    replayed at every rate (arrivals scale with 1/rate).
+
+    served: the serving loop, latency = submit -> results in host memory.
+    plain:  one request at a time through the reference ABI with host
+            buffers (cvtx_P3D_M2M_vel + cvtx_P3D_M2M_dvort / cvtx_P2D_M2M_vel /
+            cvtx_F3D_M2M_vel per step, Euler update on the host); its
+            latencies at each rate are those of a FIFO queue fed the same
+            arrivals, with each request's measured service time.
+    """
+    from cvortex_gb300 import serve, workloads
+    arrival, kinds, sizes, seeds = workloads.serve_stream(count, rate=1.0)
+    inputs = [workloads.serve_request_arrays(int(k), int(n), int(sd))
+              for k, n, sd in zip(kinds, sizes, seeds)]
+
+    def build():
+        out = []
+        for k, (a, b) in zip(kinds, inputs):
+            kw = dict(n_steps=steps, dt=dt)
+            out.append(serve.Request.p3d(a, **kw) if k == 0 else
+                       serve.Request.p2d(a, **kw) if k == 1 else serve.Request.f3d(a, b, **kw))
+        return out
+
+    pairs = float(sum(r.interactions for r in build()))
+    res = {"requests": count, "steps_per_client": steps,
+           "mix": {"p3d_vel_dvort": int((kinds == 0).sum()), "p2d_vel": int((kinds == 1).sum()),
+                   "f3d_vel": int((kinds == 2).sum())},
+           "sizes": [int(sizes.min()), int(sizes.max())], "interactions": pairs, "rates": {}}
+    srv = serve.Server(lib, n_slots=16)
+    try:
+        warm = build()[:4]                        # first-use costs out of the timed runs
+        for r in warm:
+            srv.submit(r)
+        srv.drain()
+        for rate in rates:
+            srv.reset_stats()
+            reqs = build()
+            srv.replay(reqs, arrival / rate)
+            if not srv.drain(600_000):
+                raise RuntimeError("serving drain timed out")
+            st = srv.stats()
+            if st["completed"] != count:
+                raise RuntimeError(f"served {st['completed']}/{count}: {cv.last_error()}")
+            res["rates"][str(rate)] = {
+                "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
+                "queue_p50_ms": st["queue_p50_ms"], "span_s": st["span_s"],
+                "ginter_s": st["interactions"] / st["span_s"] / 1e9,
+                "hbm_peak_bytes": st["hbm_peak"], "gpu_launches": st["kernel_launches"]}
+    finally:
+        srv.close()
+
+    # plain per-request ABI calls, each request's service time measured once
+    svc = []
+    for k, (a, b) in zip(kinds, inputs):
+        t0 = time.perf_counter()
+        if k == 0:
+            q = a.copy()
+            for _ in range(steps):
+                u = cv.p3d_vel(q, q["coord"], "winckelmans", SIGMA)
+                w = cv.p3d_dvort(q, q, "winckelmans", SIGMA, same=True)
+                q["coord"] += np.float32(dt) * u
+                q["vorticity"] += np.float32(dt) * w
+        elif k == 1:
+            q = a.copy()
+            for _ in range(steps):
+                u = cv.p2d_vel(q, q["coord"], "winckelmans", SIGMA)
+                q["coord"] += np.float32(dt) * u
+        else:
+            x = b.copy()
+            for _ in range(steps):
+                u = cv.f3d_vel(a, x)
+                x += np.float32(dt) * u
+        svc.append(time.perf_counter() - t0)
+    if cv.last_error():
+        raise RuntimeError(cv.last_error())
+    svc = np.array(svc)
+    plain = {"ginter_s_busy": pairs / svc.sum() / 1e9, "service_s_total": float(svc.sum()),
+             "rates": {}}
+    for rate in rates:
+        arr = arrival / rate
+        end, lat = 0.0, []
+        for t, s in zip(arr, svc):
+            end = max(end, t) + s
+            lat.append(end - t)
+        lat = np.array(lat) * 1e3
+        plain["rates"][str(rate)] = {
+            "p50_ms": float(np.percentile(lat, 50, method="inverted_cdf")),
+            "p99_ms": float(np.percentile(lat, 99, method="inverted_cdf")),
+            "ginter_s": pairs / (end - arr[0]) / 1e9}
+    res["plain"] = plain
+    res["speedup_ginter_s"] = {r: res["rates"][r]["ginter_s"] / plain["rates"][r]["ginter_s"]
+                               for r in res["rates"]}
     return res
 
 

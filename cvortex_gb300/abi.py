@@ -122,6 +122,32 @@ _SIGS = {
     "cvtx_P2D_redistribute_on_grid": (_i, [_vp, _i, _vp, _i, _vp, _f, _f]),
 }
 
+class cvtx_gb300_p3d_problem(C.Structure):
+    _fields_ = [("src", C.c_void_p), ("n_src", C.c_int), ("tgt", C.c_void_p),
+                ("tgt_stride", C.c_int), ("n_tgt", C.c_int), ("vel_out", C.c_void_p),
+                ("dvort_out", C.c_void_p), ("sigma", C.c_float)]
+
+
+class cvtx_gb300_request(C.Structure):
+    _fields_ = [("kind", C.c_int), ("reg", C.c_int), ("sigma", C.c_float), ("dt", C.c_float),
+                ("n_steps", C.c_int), ("n", C.c_int), ("n_tgt", C.c_int),
+                ("state_in", C.c_void_p), ("tgt_in", C.c_void_p),
+                ("state_out", C.c_void_p), ("vel_out", C.c_void_p)]
+
+
+class cvtx_gb300_server_stats(C.Structure):
+    _fields_ = [(k, C.c_ulonglong) for k in
+                ("submitted", "completed", "rejected", "failed", "queued", "in_flight")] + \
+               [(k, C.c_double) for k in
+                ("p50_ms", "p99_ms", "mean_ms", "max_ms", "queue_p50_ms", "queue_p99_ms",
+                 "interactions", "span_s")] + \
+               [(k, C.c_ulonglong) for k in
+                ("hbm_budget", "hbm_used", "hbm_peak", "kernel_launches")]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 # GB300 extensions (include/cvortex/cvtx_gb300.h).
 _EXT_SIGS = {
     "cvtx_gb300_last_error": (C.c_char_p, []),
@@ -135,6 +161,33 @@ _EXT_SIGS = {
     "cvtx_gb300_dev_P2D_M2M_vel": (_i, [_vp, _i, _vp, _i, _vp, _i, _f, _vp]),
     "cvtx_gb300_dev_F3D_M2M_vel": (_i, [_vp, _i, _vp, _i, _i, _vp, _vp]),
     "cvtx_gb300_dev_P3D_M2M_noalloc": (_i, [_vp, _i, _vp, _i, _i, _vp, _vp, _i, _f, _vp]),
+    "cvtx_gb300_p3d_num_configs": (_i, []),
+    "cvtx_gb300_p3d_config_info": (_i, [_i, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i)]),
+    "cvtx_gb300_size_bucket": (_i, [_i]),
+    "cvtx_gb300_p3d_set_tuned": (_i, [_i, _i, _i, _i]),
+    "cvtx_gb300_p3d_current_config": (_i, [_i, _i, _i]),
+    "cvtx_gb300_batch_create": (_vp, [C.POINTER(cvtx_gb300_p3d_problem), _i, _i, _i]),
+    "cvtx_gb300_batch_tune": (_i, [_vp, _i]),
+    "cvtx_gb300_batch_capture": (_i, [_vp]),
+    "cvtx_gb300_batch_run": (_i, [_vp, _vp]),
+    "cvtx_gb300_batch_status": (_i, [_vp]),
+    "cvtx_gb300_batch_info": (_i, [_vp, C.POINTER(_i), C.POINTER(_i), C.POINTER(_i),
+                                   C.POINTER(_i), C.POINTER(_i), C.POINTER(C.c_double)]),
+    "cvtx_gb300_batch_destroy": (None, [_vp]),
+    "cvtx_gb300_dev_P3D_step": (_i, [_vp, _i, _vp, _vp, _i, _f, _f, _vp]),
+    "cvtx_gb300_server_create": (_vp, [_i, C.c_ulonglong, _i]),
+    "cvtx_gb300_server_submit": (C.c_ulonglong, [_vp, C.POINTER(cvtx_gb300_request)]),
+    "cvtx_gb300_server_replay": (_i, [_vp, C.POINTER(cvtx_gb300_request),
+                                      C.POINTER(C.c_double), _i, C.POINTER(C.c_ulonglong)]),
+    "cvtx_gb300_server_wait": (_i, [_vp, C.c_ulonglong, C.c_double]),
+    "cvtx_gb300_server_drain": (_i, [_vp, C.c_double]),
+    "cvtx_gb300_server_request_info": (_i, [_vp, C.c_ulonglong, C.POINTER(C.c_double),
+                                            C.POINTER(C.c_double)]),
+    "cvtx_gb300_server_stats_get": (_i, [_vp, C.POINTER(cvtx_gb300_server_stats)]),
+    "cvtx_gb300_server_reset_stats": (None, [_vp]),
+    "cvtx_gb300_server_inject_alloc_failures": (None, [_vp, _i]),
+    "cvtx_gb300_server_destroy": (None, [_vp]),
+    "cvtx_gb300_selftest_withheld_wait": (_i, [C.c_double]),
     "cvtx_gb300_dev_status": (_i, [_vp]),
     "cvtx_gb300_probe_fp32_tflops": (_i, [_i, C.POINTER(C.c_double)]),
     "cvtx_gb300_probe_fp32_detail": (_i, [_i, C.POINTER(C.c_double), C.POINTER(C.c_double)]),

@@ -107,8 +107,7 @@ class GpuJob {
 		check(cudaMemcpyAsync(ctx_->h_err, ctx_->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx_->stream), "D2H error word");
 		check(cudaStreamSynchronize(ctx_->stream), "stream synchronize");
 		if (status_ == 0 && *ctx_->h_err != 0u) {
-			set_error(std::string(what_) + ": device-side wait expired (code " +
-				std::to_string(*ctx_->h_err) + ")");
+			set_error(std::string(what_) + ": " + device_error_text(*ctx_->h_err));
 			status_ = -4;
 		}
 		return status_ == 0;

@@ -18,6 +18,9 @@ enum : unsigned {
 	kErrNone = 0u,
 	kErrPipelineTimeout = 1u,   // an mbarrier wait exceeded its deadline
 	kErrDrainTimeout = 2u,      // draining in-flight copies after an error timed out
+	kErrBadCopy = 4u,           // a bulk copy had a misaligned address or size (skipped)
+	kErrBadLaunch = 8u,         // launch shape or shared-memory base not as the kernel expects
+	kErrBadWork = 16u,          // a work item out of range (skipped)
 };
 
 // Deadline for one mbarrier wait: source tiles land in microseconds, so two
@@ -78,14 +81,21 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 	return ok != 0u;
 }
 
-// Bounded wait for phase `parity` of `bar`. Returns false on deadline expiry.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+// Wait for phase `parity` of `bar` for at most `limit_ns`. Returns false on
+// expiry.
+__device__ __forceinline__ bool mbar_wait_for(uint64_t* bar, uint32_t parity,
+	unsigned long long limit_ns) {
 	if (mbar_try_wait(bar, parity)) return true;
 	const unsigned long long t0 = globaltimer_ns();
 	while (true) {
 		if (mbar_try_wait(bar, parity)) return true;
-		if (globaltimer_ns() - t0 > kWaitDeadlineNs) return false;
+		if (globaltimer_ns() - t0 > limit_ns) return false;
 	}
+}
+
+// Bounded wait for phase `parity` of `bar`. Returns false on deadline expiry.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+	return mbar_wait_for(bar, parity, kWaitDeadlineNs);
 }
 
 __device__ __forceinline__ float rsqrt_approx(float x) {

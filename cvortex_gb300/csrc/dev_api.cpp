@@ -82,6 +82,26 @@ CVTX_EXPORT int cvtx_gb300_dev_P3D_M2M(const void* src, int n_src, const void* t
 	return c.done(p3d_induce(reg, ops, p, c.env()), "cvtx_gb300_dev_P3D_M2M");
 }
 
+CVTX_EXPORT int cvtx_gb300_dev_P3D_step(void* rec, int n, float* vel, float* dvort, int reg,
+	float sigma, float dt, void* stream)
+{
+	if (n <= 0) return 0;
+	if (!rec || !vel || !dvort || bad_reg(reg)) return -1;
+	DevCall c(stream);
+	const unsigned ops = kOpVel | kOpDvort;
+	int st = c.prepare(p3d_induce_ws_bytes(reg, ops, n, n, c.ctx ? c.ctx->num_sms : 1),
+		"cvtx_gb300_dev_P3D_step");
+	if (st) return st;
+	float4* r = static_cast<float4*>(rec);
+	P3DInduceProblem p;
+	p.src = r; p.n_src = n;
+	p.tgt = r; p.tstride = 2; p.n_tgt = n;
+	p.out_vel = vel; p.out_dvort = dvort; p.sigma = sigma;
+	cudaError_t e = p3d_induce(reg, ops, p, c.env());
+	if (e == cudaSuccess) e = advance_p3d(r, n, vel, dvort, dt, c.stream);
+	return c.done(e, "cvtx_gb300_dev_P3D_step");
+}
+
 CVTX_EXPORT int cvtx_gb300_dev_P3D_M2M_visc(const void* src, int n_src, const void* tgt,
 	int tgt_stride, int n_tgt, float* out, int reg, float sigma, float nu, void* stream)
 {
@@ -159,7 +179,7 @@ CVTX_EXPORT int cvtx_gb300_dev_status(void* stream) {
 	if (cudaMemcpy(&w, c->d_err, sizeof w, cudaMemcpyDeviceToHost) != cudaSuccess) return -2;
 	if (cudaMemset(c->d_err, 0, sizeof w) != cudaSuccess) return -2;
 	if (w) {
-		set_error("device-side wait expired (code " + std::to_string(w) + ")");
+		set_error(device_error_text(w));
 		return -4;
 	}
 	return 0;

@@ -293,21 +293,22 @@ constexpr size_t smem_bytes() {
 }
 
 template <int TPT, int NT>
-Plan plan_vel(int n_fil, int n_tgt, int num_sms) {
+Plan plan_vel(int n_fil, int n_tgt, int num_sms, int max_split = 64) {
 	constexpr size_t smem = smem_bytes<TPT, NT>();
 	static const int occ = resident_ctas(f3d_vel_kernel<TPT, NT>, NT, smem);
-	return make_plan(n_fil, n_tgt, TPT * NT, kTile, 3, num_sms * occ, smem);
+	return make_plan(n_fil, n_tgt, TPT * NT, kTile, 3, num_sms * occ, smem, max_split);
 }
 template <int TPT, int NT>
-Plan plan_dvort(int n_fil, int n_tgt, int num_sms) {
+Plan plan_dvort(int n_fil, int n_tgt, int num_sms, int max_split = 64) {
 	constexpr size_t smem = smem_bytes<TPT, NT>();
 	static const int occ = resident_ctas(f3d_dvort_kernel<TPT, NT>, NT, smem);
-	return make_plan(n_fil, n_tgt, TPT * NT, kTile, 3, num_sms * occ, smem);
+	return make_plan(n_fil, n_tgt, TPT * NT, kTile, 3, num_sms * occ, smem, max_split);
 }
 
 template <int TPT, int NT>
 cudaError_t launch_vel(const F3DVelProblem& p, const LaunchEnv& env) {
-	const Plan pl = plan_vel<TPT, NT>(p.n_fil, p.n_tgt, env.num_sms);
+	const Plan pl = plan_vel<TPT, NT>(p.n_fil, p.n_tgt, env.num_sms,
+		env.cap_to_ws ? split_cap_for(env.ws_bytes, 3, p.n_tgt) : 64);
 	if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
 	double* partial = static_cast<double*>(env.ws);
 	f3d_vel_kernel<TPT, NT><<<dim3(pl.n_tblocks, pl.n_split), NT, pl.smem, env.stream>>>(
@@ -321,7 +322,8 @@ cudaError_t launch_vel(const F3DVelProblem& p, const LaunchEnv& env) {
 }
 template <int TPT, int NT>
 cudaError_t launch_dvort(const F3DDvortProblem& p, const LaunchEnv& env) {
-	const Plan pl = plan_dvort<TPT, NT>(p.n_fil, p.n_tgt, env.num_sms);
+	const Plan pl = plan_dvort<TPT, NT>(p.n_fil, p.n_tgt, env.num_sms,
+		env.cap_to_ws ? split_cap_for(env.ws_bytes, 3, p.n_tgt) : 64);
 	if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
 	double* partial = static_cast<double*>(env.ws);
 	f3d_dvort_kernel<TPT, NT><<<dim3(pl.n_tblocks, pl.n_split), NT, pl.smem, env.stream>>>(

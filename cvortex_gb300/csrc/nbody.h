@@ -85,7 +85,17 @@ struct LaunchEnv {
 	unsigned* err;       // device error word (0 = ok)
 	cudaStream_t stream;
 	int num_sms;
+	// When set, launchers cap the number of source splits so that the split
+	// partials fit ws_bytes (for callers with a fixed-size workspace).
+	bool cap_to_ws = false;
 };
+
+// Largest split count whose FP64 partials (nc sums per target) fit `ws_bytes`.
+inline int split_cap_for(size_t ws_bytes, int nc, int n_tgt) {
+	const size_t per = size_t(nc) * size_t(n_tgt > 0 ? n_tgt : 1) * sizeof(double);
+	const size_t cap = ws_bytes / per;
+	return cap < 1 ? 1 : (cap > 64 ? 64 : int(cap));
+}
 
 // Kernel-launch counter shared by every launcher (for the launch statistics
 // exposed by the library).
@@ -107,6 +117,19 @@ cudaError_t p3d_induce(int reg, unsigned ops, const P3DInduceProblem& p, const L
 // fit env.ws_bytes (a fixed scratch area); never needs more than that.
 cudaError_t p3d_induce_bounded(int reg, unsigned ops, const P3DInduceProblem& p,
 	const LaunchEnv& env);
+
+// Launch configurations of the induce kernels (targets per thread, threads
+// per CTA, packed f32x2 arithmetic) and the tuning table that selects one per
+// (regularisation, ops, target-count bucket).
+constexpr int kNumSizeBuckets = 6;
+inline int size_bucket(int n_tgt) {
+	return n_tgt < 8192 ? 0 : n_tgt < 32768 ? 1 : n_tgt < 131072 ? 2 : n_tgt < 524288 ? 3
+		: n_tgt < 2097152 ? 4 : 5;
+}
+int p3d_induce_num_configs();
+bool p3d_induce_config(int cfg, int* tpt, int* nt, int* packed);
+bool p3d_induce_set_tuned(int reg, unsigned ops, int bucket, int cfg);
+int p3d_induce_current_config(int reg, unsigned ops, int n_tgt);
 
 size_t p3d_visc_ws_bytes(int reg, int n_src, int n_tgt, int num_sms);
 cudaError_t p3d_visc(int reg, const P3DViscProblem& p, const LaunchEnv& env);
@@ -136,5 +159,13 @@ cudaError_t pack_v3(const void* v12, int n, float4* out, cudaStream_t s);
 cudaError_t pack_v2(const void* v8, int n, float4* out, cudaStream_t s);
 // Gather through a device-visible array of record pointers.
 cudaError_t gather_p3d(const void* const* ptrs, int n, float4* out, cudaStream_t s);
+
+// Forward-Euler update of resident state (advance.cu): positions move by
+// dt * vel (packed float3 / float2); P3D vorticity moves by dt * dvort when
+// dvort is non-null.
+cudaError_t advance_p3d(float4* rec, int n, const float* vel, const float* dvort, float dt,
+	cudaStream_t s);
+cudaError_t advance_p2d(float4* rec, int n, const float* vel, float dt, cudaStream_t s);
+cudaError_t advance_points(float4* pts, int n, const float* vel, float dt, cudaStream_t s);
 
 }  // namespace cvtx

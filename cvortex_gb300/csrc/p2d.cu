@@ -194,10 +194,10 @@ constexpr size_t smem_bytes() {
 }
 
 template <Reg R, int TPT, int NT>
-Plan plan_vel(int n_src, int n_tgt, int num_sms) {
+Plan plan_vel(int n_src, int n_tgt, int num_sms, int max_split = 64) {
 	constexpr size_t smem = smem_bytes<TPT, NT, 2>();
 	static const int occ = resident_ctas(p2d_vel_kernel<R, TPT, NT>, NT, smem);
-	return make_plan(n_src, n_tgt, TPT * NT, kTile, 2, num_sms * occ, smem);
+	return make_plan(n_src, n_tgt, TPT * NT, kTile, 2, num_sms * occ, smem, max_split);
 }
 
 // Reference scale 1/(2 pi) (src/P2D.cpp:118); Winckelmans and Gaussian H are
@@ -211,7 +211,8 @@ double vel_scale(int reg, float sigma) {
 
 template <Reg R, int TPT, int NT>
 cudaError_t launch_vel(const P2DVelProblem& p, const LaunchEnv& env) {
-	const Plan pl = plan_vel<R, TPT, NT>(p.n_src, p.n_tgt, env.num_sms);
+	const Plan pl = plan_vel<R, TPT, NT>(p.n_src, p.n_tgt, env.num_sms,
+		env.cap_to_ws ? split_cap_for(env.ws_bytes, 2, p.n_tgt) : 64);
 	if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
 	const RegConsts rc = make_reg_consts_host(p.sigma);
 	const double scale = vel_scale(int(R), p.sigma);
@@ -228,15 +229,16 @@ cudaError_t launch_vel(const P2DVelProblem& p, const LaunchEnv& env) {
 }
 
 template <Reg R, int TPT, int NT>
-Plan plan_visc(int n_src, int n_tgt, int num_sms) {
+Plan plan_visc(int n_src, int n_tgt, int num_sms, int max_split = 64) {
 	constexpr size_t smem = smem_bytes<TPT, NT, 1>();
 	static const int occ = resident_ctas(p2d_visc_kernel<R, TPT, NT>, NT, smem);
-	return make_plan(n_src, n_tgt, TPT * NT, kTile, 1, num_sms * occ, smem);
+	return make_plan(n_src, n_tgt, TPT * NT, kTile, 1, num_sms * occ, smem, max_split);
 }
 
 template <Reg R, int TPT, int NT>
 cudaError_t launch_visc(const P2DViscProblem& p, const LaunchEnv& env) {
-	const Plan pl = plan_visc<R, TPT, NT>(p.n_src, p.n_tgt, env.num_sms);
+	const Plan pl = plan_visc<R, TPT, NT>(p.n_src, p.n_tgt, env.num_sms,
+		env.cap_to_ws ? split_cap_for(env.ws_bytes, 1, p.n_tgt) : 64);
 	if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
 	const RegConsts rc = make_reg_consts_host(p.sigma);
 	const double scale = 2.0 * double(p.nu) / (double(p.sigma) * double(p.sigma));

@@ -16,11 +16,13 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <atomic>
 #include <mutex>
+#include <type_traits>
 #include "nbody.h"
 #include "plan.cuh"
 #include "regfuncs.cuh"
-#include "tile_stream.cuh"
+#include "p3d_induce.cuh"
 
 namespace cvtx {
 
@@ -40,19 +42,13 @@ RegConsts make_reg_consts_host(float sigma) {
 
 namespace {
 
-constexpr int kTile = 256;
-constexpr int kStages = 2;
-using Stream2 = TileStream<2, kTile, kStages>;
-
-template <Reg R> struct FiniteAtZero { static constexpr bool value = true; };
-template <> struct FiniteAtZero<Reg::Singular> { static constexpr bool value = false; };
-
-struct InduceConsts {
-	RegConsts rc;
-	double s_vel, s_dv, k_scale;
-};
+constexpr int kTile = kP3DTile;
+using Stream2 = P3DStream;
 
 RegConsts make_reg_consts(float sigma) { return make_reg_consts_host(sigma); }
+
+
+}  // namespace
 
 // Per-regularisation output scales (see regfuncs.cuh). Reference: vel uses
 // 1/(4 pi) with rho = r/|sigma| (src/P3D.cpp:239,250); dvort uses the signed
@@ -71,7 +67,12 @@ InduceConsts make_induce_consts(int reg, float sigma) {
 		k.s_dv = sgn * inv4pi;
 		k.k_scale = 3.0;
 		break;
-	default:  // Winckelmans, Gaussian: rho-normalised G and K
+	case int(Reg::Winckelmans):  // rho-normalised G, K/3
+		k.s_vel = -inv4pi / (as * as * as);
+		k.s_dv = inv4pi / (s * s * s);
+		k.k_scale = 3.0 / (s * s);
+		break;
+	default:  // Gaussian: rho-normalised G and K
 		k.s_vel = -inv4pi / (as * as * as);
 		k.s_dv = inv4pi / (s * s * s);
 		k.k_scale = 1.0 / (s * s);
@@ -80,29 +81,7 @@ InduceConsts make_induce_consts(int reg, float sigma) {
 	return k;
 }
 
-template <bool VEL, bool DV>
-__device__ __forceinline__ void write_induce(const P3DInduceProblem& p,
-	const InduceConsts& kc, int t, const double* s, float ax, float ay, float az)
-{
-	int o = 0;
-	if (VEL) {
-		float* v = p.out_vel + 3 * size_t(t);
-		v[0] = float(kc.s_vel * s[0]);
-		v[1] = float(kc.s_vel * s[1]);
-		v[2] = float(kc.s_vel * s[2]);
-		o = 3;
-	}
-	if (DV) {
-		const double Ax = s[o], Ay = s[o + 1], Az = s[o + 2];
-		const double cx = double(ay) * Az - double(az) * Ay;
-		const double cy = double(az) * Ax - double(ax) * Az;
-		const double cz = double(ax) * Ay - double(ay) * Ax;
-		float* w = p.out_dvort + 3 * size_t(t);
-		w[0] = float(kc.s_dv * (cx + kc.k_scale * s[o + 3]));
-		w[1] = float(kc.s_dv * (cy + kc.k_scale * s[o + 4]));
-		w[2] = float(kc.s_dv * (cz + kc.k_scale * s[o + 5]));
-	}
-}
+namespace {
 
 // Accumulators per target (registers, FP32, reset every tile):
 //   VEL only : u  = sum G c,            c  = d x alpha_s
@@ -264,165 +243,31 @@ p3d_induce_kernel(const P3DInduceProblem p, const InduceConsts kc,
 	}
 }
 
-// Packed variant of p3d_induce_kernel for VEL+DV and DV with an even number
-// of targets per thread: targets (2h, 2h+1) of a thread share one float2 lane
-// pair, so every per-pair FP32 operation (except rsqrt and the coincidence
-// select) is one f32x2 instruction for two interactions. Same sums, same
-// order of operations per target as the scalar kernel.
-__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
-
+// Packed variant of p3d_induce_kernel (two targets per f32x2 lane pair; see
+// induce2_block in p3d_induce.cuh). CTA (x, y) = (target block, source split).
 template <Reg R, bool VEL, bool DV, int TPT, int NT>
 __global__ void __launch_bounds__(NT)
 p3d_induce2_kernel(const P3DInduceProblem p, const InduceConsts kc,
 	double* __restrict__ partial, int src_per_split, unsigned* err)
 {
-	static_assert(DV && TPT % 2 == 0, "packed kernel: stretching, even TPT");
-	constexpr int H = TPT / 2;
-	constexpr int NC = (VEL ? 3 : 0) + 6;
-	constexpr int NR = (VEL ? 6 : 0) + 6;
-	constexpr bool kFinite = FiniteAtZero<R>::value;
+	constexpr int NC = InduceNC<VEL, DV>::value;
 	extern __shared__ __align__(16) unsigned char smem[];
-	float* hi = reinterpret_cast<float*>(smem + Stream2::kSmemBytes);
-	float* lo = hi + NC * TPT * NT;
-
-	const int tid = threadIdx.x;
-	const int tbase = blockIdx.x * (TPT * NT);
+	if (!P3DStream::init(smem, err)) return;
+	unsigned tcount = 0;
 	const int s_begin = blockIdx.y * src_per_split;
 	int n_s = p.n_src - s_begin;
 	n_s = n_s < src_per_split ? n_s : src_per_split;
 	n_s = n_s > 0 ? n_s : 0;
-
-	float2 tx[H], ty[H], tz[H], ax[H], ay[H], az[H];
-#pragma unroll
-	for (int h = 0; h < H; ++h) {
-		float4 q[2], v[2];
-#pragma unroll
-		for (int e = 0; e < 2; ++e) {
-			int t = tbase + (2 * h + e) * NT + tid;
-			t = t < p.n_tgt ? t : p.n_tgt - 1;
-			q[e] = p.tgt[size_t(t) * p.tstride];
-			v[e] = p.tgt[size_t(t) * p.tstride + 1];
-		}
-		tx[h] = make_float2(q[0].x, q[1].x); ty[h] = make_float2(q[0].y, q[1].y);
-		tz[h] = make_float2(q[0].z, q[1].z);
-		ax[h] = make_float2(v[0].x, v[1].x); ay[h] = make_float2(v[0].y, v[1].y);
-		az[h] = make_float2(v[0].z, v[1].z);
-	}
-#pragma unroll
-	for (int i = 0; i < NC * TPT; ++i) { hi[i * NT + tid] = 0.f; lo[i * NT + tid] = 0.f; }
-
-	auto tile_fn = [&](const float4* __restrict__ st, int cnt) {
-		float2 acc[NR][H];
-#pragma unroll
-		for (int c = 0; c < NR; ++c)
-#pragma unroll
-			for (int h = 0; h < H; ++h) acc[c][h] = make_float2(0.f, 0.f);
-
-		auto body = [&](int j) {
-			const float4 sp = st[2 * j];
-			const float4 sv = st[2 * j + 1];
-			const float2 nsx = bc2(-sp.x), nsy = bc2(-sp.y), nsz = bc2(-sp.z);
-			const float2 wx = bc2(sv.x), wy = bc2(sv.y), wz = bc2(sv.z);
-#pragma unroll
-			for (int h = 0; h < H; ++h) {
-				const float2 dx = __fadd2_rn(tx[h], nsx);
-				const float2 dy = __fadd2_rn(ty[h], nsy);
-				const float2 dz = __fadd2_rn(tz[h], nsz);
-				const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
-				// da = alpha_s - alpha_t, c' = d x da
-				const float2 ex = __ffma2_rn(ax[h], bc2(-1.f), wx);
-				const float2 ey = __ffma2_rn(ay[h], bc2(-1.f), wy);
-				const float2 ez = __ffma2_rn(az[h], bc2(-1.f), wz);
-				const float2 cx = __ffma2_rn(dy, ez, neg2(__fmul2_rn(dz, ey)));
-				const float2 cy = __ffma2_rn(dz, ex, neg2(__fmul2_rn(dx, ez)));
-				const float2 cz = __ffma2_rn(dx, ey, neg2(__fmul2_rn(dy, ex)));
-				float2 G, K;
-				RegP3D2<R>::gk2(r2, kc.rc, G, K);
-				G.x = r2.x > 0.f ? G.x : 0.f;
-				G.y = r2.y > 0.f ? G.y : 0.f;
-				if (!kFinite) {
-					K.x = r2.x > 0.f ? K.x : 0.f;
-					K.y = r2.y > 0.f ? K.y : 0.f;
-				}
-				constexpr int o = VEL ? 6 : 0;
-				if (VEL) {
-					acc[0][h] = __ffma2_rn(G, cx, acc[0][h]);
-					acc[1][h] = __ffma2_rn(G, cy, acc[1][h]);
-					acc[2][h] = __ffma2_rn(G, cz, acc[2][h]);
-					acc[3][h] = __ffma2_rn(G, dx, acc[3][h]);
-					acc[4][h] = __ffma2_rn(G, dy, acc[4][h]);
-					acc[5][h] = __ffma2_rn(G, dz, acc[5][h]);
-				}
-				acc[o + 0][h] = __ffma2_rn(G, ex, acc[o + 0][h]);
-				acc[o + 1][h] = __ffma2_rn(G, ey, acc[o + 1][h]);
-				acc[o + 2][h] = __ffma2_rn(G, ez, acc[o + 2][h]);
-				const float2 pd = __ffma2_rn(az[h], cz, __ffma2_rn(ay[h], cy, __fmul2_rn(ax[h], cx)));
-				const float2 kk = __fmul2_rn(K, pd);
-				acc[o + 3][h] = __ffma2_rn(kk, dx, acc[o + 3][h]);
-				acc[o + 4][h] = __ffma2_rn(kk, dy, acc[o + 4][h]);
-				acc[o + 5][h] = __ffma2_rn(kk, dz, acc[o + 5][h]);
-			}
-		};
-		if (cnt == kTile) {
-#pragma unroll 2
-			for (int j = 0; j < kTile; ++j) body(j);
-		} else {
-#pragma unroll 1
-			for (int j = 0; j < cnt; ++j) body(j);
-		}
-		if (VEL) {
-#pragma unroll
-			for (int h = 0; h < H; ++h) {
-				const float2 wx_ = acc[3][h], wy_ = acc[4][h], wz_ = acc[5][h];
-				acc[0][h] = __fadd2_rn(acc[0][h], __ffma2_rn(wy_, az[h], neg2(__fmul2_rn(wz_, ay[h]))));
-				acc[1][h] = __fadd2_rn(acc[1][h], __ffma2_rn(wz_, ax[h], neg2(__fmul2_rn(wx_, az[h]))));
-				acc[2][h] = __fadd2_rn(acc[2][h], __ffma2_rn(wx_, ay[h], neg2(__fmul2_rn(wy_, ax[h]))));
-			}
-		}
-#pragma unroll
-		for (int c = 0; c < NC; ++c) {
-			const int src_c = (VEL && c >= 3) ? c + 3 : c;
-#pragma unroll
-			for (int h = 0; h < H; ++h) {
-#pragma unroll
-				for (int e = 0; e < 2; ++e) {
-					const int k = 2 * h + e;
-					const int i = (c * TPT + k) * NT + tid;
-					float hh = hi[i], ll = lo[i];
-					fold_twosum(hh, ll, e == 0 ? acc[src_c][h].x : acc[src_c][h].y);
-					hi[i] = hh; lo[i] = ll;
-				}
-			}
-		}
-	};
-
-	if (!Stream2::run(smem, p.src, s_begin, n_s, err, tile_fn)) return;
-
-#pragma unroll
-	for (int h = 0; h < H; ++h) {
-#pragma unroll
-		for (int e = 0; e < 2; ++e) {
-			const int k = 2 * h + e;
-			const int t = tbase + k * NT + tid;
-			if (t >= p.n_tgt) continue;
-			double sacc[NC];
-#pragma unroll
-			for (int c = 0; c < NC; ++c) {
-				const int i = (c * TPT + k) * NT + tid;
-				sacc[c] = double(hi[i]) + double(lo[i]);
-			}
-			const float tax = e == 0 ? ax[h].x : ax[h].y;
-			const float tay = e == 0 ? ay[h].x : ay[h].y;
-			const float taz = e == 0 ? az[h].x : az[h].y;
+	induce2_block<R, VEL, DV, TPT, NT>(p, kc, blockIdx.x * (TPT * NT), s_begin, n_s, smem, err,
+		tcount, [&](int t, const double* acc, float ax, float ay, float az) {
 			if (gridDim.y == 1) {
-				write_induce<VEL, DV>(p, kc, t, sacc, tax, tay, taz);
+				write_induce<VEL, DV>(p, kc, t, acc, ax, ay, az);
 			} else {
 #pragma unroll
 				for (int c = 0; c < NC; ++c)
-					partial[(size_t(blockIdx.y) * NC + c) * p.n_tgt + t] = sacc[c];
+					partial[(size_t(blockIdx.y) * NC + c) * p.n_tgt + t] = acc[c];
 			}
-		}
-	}
+		});
 }
 
 template <bool VEL, bool DV>
@@ -666,131 +511,132 @@ constexpr size_t smem_bytes() {
 	return Stream2::kSmemBytes + size_t(2) * NC * TPT * NT * sizeof(float);
 }
 
-// Targets per CTA: large problems use 4 targets per thread; small target
-// counts use 1 so that the source dimension can be split across more CTAs.
+// ---- induce launch configurations ------------------------------------------
+// A configuration is (targets per thread, threads per CTA, packed f32x2 or
+// scalar arithmetic). The table below is what the autotuner chooses from;
+// without a tuned entry, fewer than kSmallTargets targets use configuration 0
+// (one target per thread, so the source dimension can be split across more
+// CTAs) and larger problems use configuration 2.
 constexpr int kSmallTargets = 8192;
 
-// Packed (f32x2) kernel for stretching with an even number of targets per
-// thread; CVTX_GB300_SCALAR=1 in the environment selects the scalar kernel
-// (kept for comparison).
-bool use_packed() {
-	static const bool v = [] {
-		const char* e = std::getenv("CVTX_GB300_SCALAR");
-		return !(e && e[0] == '1');
+struct CfgSpec { int tpt, nt; bool packed; };
+constexpr CfgSpec kCfg[] = {
+	{1, 128, false}, {4, 128, false}, {4, 128, true}, {2, 128, true},
+	{4, 64, true},   {2, 256, true},  {6, 64, true},
+};
+constexpr int kNumCfg = int(sizeof(kCfg) / sizeof(kCfg[0]));
+
+template <Reg R, bool VEL, bool DV, int TPT, int NT, bool PK>
+struct InduceVariant {
+	static constexpr int NC = (VEL ? 3 : 0) + (DV ? 6 : 0);
+	static constexpr size_t kSmem = smem_bytes<TPT, NT, NC>();
+	using Fn = void (*)(const P3DInduceProblem, const InduceConsts, double*, int, unsigned*);
+	static Fn fn() {
+		if constexpr (PK) return p3d_induce2_kernel<R, VEL, DV, TPT, NT>;
+		else return p3d_induce_kernel<R, VEL, DV, TPT, NT>;
+	}
+	static int occupancy() {
+		static const int occ = resident_ctas(fn(), NT, kSmem);
+		return occ;
+	}
+	static Plan plan(int n_src, int n_tgt, int num_sms, int max_split) {
+		return make_plan(n_src, n_tgt, TPT * NT, kTile, NC, num_sms * occupancy(), kSmem, max_split);
+	}
+	static cudaError_t launch(const Plan& pl, const P3DInduceProblem& p, const LaunchEnv& env) {
+		if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
+		const InduceConsts kc = make_induce_consts(int(R), p.sigma);
+		double* partial = static_cast<double*>(env.ws);
+		fn()<<<dim3(pl.n_tblocks, pl.n_split), NT, pl.smem, env.stream>>>(
+			p, kc, partial, pl.src_per_split, env.err);
+		count_launch();
+		if (pl.n_split > 1) {
+			p3d_induce_finalize<VEL, DV><<<(p.n_tgt + 255) / 256, 256, 0, env.stream>>>(
+				p, kc, partial, pl.n_split);
+			count_launch();
+		}
+		return cudaGetLastError();
+	}
+};
+
+template <Reg R, bool VEL, bool DV, class F>
+auto with_cfg(int ci, F&& f) {
+	switch (ci) {
+	case 0: return f(InduceVariant<R, VEL, DV, 1, 128, false>{});
+	case 1: return f(InduceVariant<R, VEL, DV, 4, 128, false>{});
+	case 2: return f(InduceVariant<R, VEL, DV, 4, 128, true>{});
+	case 3: return f(InduceVariant<R, VEL, DV, 2, 128, true>{});
+	case 4: return f(InduceVariant<R, VEL, DV, 4, 64, true>{});
+	case 5: return f(InduceVariant<R, VEL, DV, 2, 256, true>{});
+	default: return f(InduceVariant<R, VEL, DV, 6, 64, true>{});
+	}
+}
+
+template <class F>
+auto with_reg_ops(int reg, unsigned ops, F&& f) {
+	auto by_ops = [&](auto rtag) {
+		constexpr Reg R = decltype(rtag)::value;
+		switch (ops) {
+		case kOpVel: return f(std::integral_constant<Reg, R>{}, std::true_type{}, std::false_type{});
+		case kOpDvort: return f(std::integral_constant<Reg, R>{}, std::false_type{}, std::true_type{});
+		default: return f(std::integral_constant<Reg, R>{}, std::true_type{}, std::true_type{});
+		}
+	};
+	switch (reg) {
+	case 0: return by_ops(std::integral_constant<Reg, Reg::Singular>{});
+	case 1: return by_ops(std::integral_constant<Reg, Reg::Winckelmans>{});
+	case 2: return by_ops(std::integral_constant<Reg, Reg::Planetary>{});
+	default: return by_ops(std::integral_constant<Reg, Reg::Gaussian>{});
+	}
+}
+
+// Tuned configuration per (regularisation, ops, size bucket); -1 = default.
+std::atomic<int> g_tuned[4][4][kNumSizeBuckets];
+const bool g_tuned_init = [] {
+	for (auto& a : g_tuned) for (auto& b : a) for (auto& c : b) c.store(-1);
+	return true;
+}();
+
+int env_cfg() {
+	static const int v = [] {
+		const char* e = std::getenv("CVTX_GB300_P3D_CFG");
+		if (!e || !*e) return -1;
+		const int c = std::atoi(e);
+		return (c >= 0 && c < kNumCfg) ? c : -1;
 	}();
 	return v;
 }
 
-template <Reg R, bool VEL, bool DV, int TPT, int NT>
-struct InduceKernel {
-	using Fn = void (*)(const P3DInduceProblem, const InduceConsts, double*, int, unsigned*);
-	static constexpr bool kPackable = DV && (TPT % 2 == 0);
-	static Fn get() {
-		if constexpr (kPackable) {
-			if (use_packed()) return p3d_induce2_kernel<R, VEL, DV, TPT, NT>;
-		}
-		return p3d_induce_kernel<R, VEL, DV, TPT, NT>;
-	}
-};
-
-template <Reg R, bool VEL, bool DV, int TPT, int NT>
-Plan plan_induce(int n_src, int n_tgt, int num_sms) {
-	constexpr int NC = (VEL ? 3 : 0) + (DV ? 6 : 0);
-	constexpr size_t smem = smem_bytes<TPT, NT, NC>();
-	static const int occ = resident_ctas(InduceKernel<R, VEL, DV, TPT, NT>::get(), NT, smem);
-	return make_plan(n_src, n_tgt, TPT * NT, kTile, NC, num_sms * occ, smem);
+int choose_cfg(int reg, unsigned ops, int n_tgt) {
+	const int forced = env_cfg();
+	if (forced >= 0) return forced;
+	const int t = g_tuned[reg & 3][ops & 3][size_bucket(n_tgt)].load(std::memory_order_relaxed);
+	if (t >= 0 && t < kNumCfg) return t;
+	return n_tgt < kSmallTargets ? 0 : 2;
 }
 
-template <Reg R, bool VEL, bool DV, int TPT, int NT>
-cudaError_t launch_induce(const P3DInduceProblem& p, const LaunchEnv& env) {
-	constexpr int NC = (VEL ? 3 : 0) + (DV ? 6 : 0);
-	const Plan pl = plan_induce<R, VEL, DV, TPT, NT>(p.n_src, p.n_tgt, env.num_sms);
-	if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
-	const InduceConsts kc = make_induce_consts(int(R), p.sigma);
-	double* partial = static_cast<double*>(env.ws);
-	dim3 grid(pl.n_tblocks, pl.n_split);
-	InduceKernel<R, VEL, DV, TPT, NT>::get()<<<grid, NT, pl.smem, env.stream>>>(
-		p, kc, partial, pl.src_per_split, env.err);
-	count_launch();
-	if (pl.n_split > 1) {
-		p3d_induce_finalize<VEL, DV><<<(p.n_tgt + 255) / 256, 256, 0, env.stream>>>(
-			p, kc, partial, pl.n_split);
-		count_launch();
-	}
-	(void)NC;
-	return cudaGetLastError();
+size_t induce_ws(int reg, unsigned ops, int n_src, int n_tgt, int num_sms, int cfg) {
+	return with_reg_ops(reg, ops, [&](auto rt, auto vt, auto dt) {
+		constexpr Reg R = decltype(rt)::value;
+		constexpr bool VEL = decltype(vt)::value, DV = decltype(dt)::value;
+		return with_cfg<R, VEL, DV>(cfg, [&](auto var) {
+			return decltype(var)::plan(n_src, n_tgt, num_sms, 64).ws_bytes;
+		});
+	});
 }
 
-template <Reg R, bool VEL, bool DV>
-size_t ws_induce_r(int n_src, int n_tgt, int num_sms) {
-	if (n_tgt < kSmallTargets) return plan_induce<R, VEL, DV, 1, 128>(n_src, n_tgt, num_sms).ws_bytes;
-	return plan_induce<R, VEL, DV, 4, 128>(n_src, n_tgt, num_sms).ws_bytes;
-}
-
-template <Reg R, bool VEL, bool DV>
-cudaError_t induce_r(const P3DInduceProblem& p, const LaunchEnv& env) {
-	if (p.n_tgt < kSmallTargets) return launch_induce<R, VEL, DV, 1, 128>(p, env);
-	return launch_induce<R, VEL, DV, 4, 128>(p, env);
-}
-
-template <Reg R>
-size_t ws_induce_ops(unsigned ops, int n_src, int n_tgt, int num_sms) {
-	switch (ops) {
-	case kOpVel: return ws_induce_r<R, true, false>(n_src, n_tgt, num_sms);
-	case kOpDvort: return ws_induce_r<R, false, true>(n_src, n_tgt, num_sms);
-	default: return ws_induce_r<R, true, true>(n_src, n_tgt, num_sms);
-	}
-}
-
-template <Reg R>
-cudaError_t induce_ops(unsigned ops, const P3DInduceProblem& p, const LaunchEnv& env) {
-	switch (ops) {
-	case kOpVel: return induce_r<R, true, false>(p, env);
-	case kOpDvort: return induce_r<R, false, true>(p, env);
-	default: return induce_r<R, true, true>(p, env);
-	}
-}
-
-// The same launch with the number of source splits capped so that the FP64
-// split partials fit the workspace the caller supplies (env.ws_bytes), for
-// callers that provide a fixed scratch area instead of a sized one.
-template <Reg R, bool VEL, bool DV, int TPT, int NT>
-cudaError_t launch_induce_bounded(const P3DInduceProblem& p, const LaunchEnv& env) {
-	constexpr int NC = (VEL ? 3 : 0) + (DV ? 6 : 0);
-	constexpr size_t smem = smem_bytes<TPT, NT, NC>();
-	static const int occ = resident_ctas(InduceKernel<R, VEL, DV, TPT, NT>::get(), NT, smem);
-	const size_t per_split = size_t(NC) * size_t(p.n_tgt) * sizeof(double);
-	size_t cap = env.ws_bytes / per_split;
-	cap = cap < 1 ? 1 : (cap > 64 ? 64 : cap);
-	const Plan pl = make_plan(p.n_src, p.n_tgt, TPT * NT, kTile, NC, env.num_sms * occ, smem,
-		int(cap));
-	if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
-	const InduceConsts kc = make_induce_consts(int(R), p.sigma);
-	double* partial = static_cast<double*>(env.ws);
-	InduceKernel<R, VEL, DV, TPT, NT>::get()<<<dim3(pl.n_tblocks, pl.n_split), NT, pl.smem,
-		env.stream>>>(p, kc, partial, pl.src_per_split, env.err);
-	count_launch();
-	if (pl.n_split > 1) {
-		p3d_induce_finalize<VEL, DV><<<(p.n_tgt + 255) / 256, 256, 0, env.stream>>>(
-			p, kc, partial, pl.n_split);
-		count_launch();
-	}
-	return cudaGetLastError();
-}
-
-template <Reg R, bool VEL, bool DV>
-cudaError_t induce_bounded_r(const P3DInduceProblem& p, const LaunchEnv& env) {
-	if (p.n_tgt < kSmallTargets) return launch_induce_bounded<R, VEL, DV, 1, 128>(p, env);
-	return launch_induce_bounded<R, VEL, DV, 4, 128>(p, env);
-}
-
-template <Reg R>
-cudaError_t induce_bounded_ops(unsigned ops, const P3DInduceProblem& p, const LaunchEnv& env) {
-	switch (ops) {
-	case kOpVel: return induce_bounded_r<R, true, false>(p, env);
-	case kOpDvort: return induce_bounded_r<R, false, true>(p, env);
-	default: return induce_bounded_r<R, true, true>(p, env);
-	}
+cudaError_t induce_launch(int reg, unsigned ops, const P3DInduceProblem& p, const LaunchEnv& env,
+	int cfg, bool bounded) {
+	return with_reg_ops(reg, ops, [&](auto rt, auto vt, auto dt) {
+		constexpr Reg R = decltype(rt)::value;
+		constexpr bool VEL = decltype(vt)::value, DV = decltype(dt)::value;
+		return with_cfg<R, VEL, DV>(cfg, [&](auto var) {
+			using V = decltype(var);
+			// capped: the FP64 split partials must fit env.ws_bytes
+			const int max_split = (bounded || env.cap_to_ws)
+				? split_cap_for(env.ws_bytes, V::NC, p.n_tgt) : 64;
+			return V::launch(V::plan(p.n_src, p.n_tgt, env.num_sms, max_split), p, env);
+		});
+	});
 }
 
 template <Reg R, int TPT, int NT>
@@ -853,35 +699,39 @@ cudaError_t launch_vort(const P3DVortProblem& p, const LaunchEnv& env) {
 
 size_t p3d_induce_ws_bytes(int reg, unsigned ops, int n_src, int n_tgt, int num_sms) {
 	if (n_tgt <= 0) return 0;
-	switch (reg) {
-	case 0: return ws_induce_ops<Reg::Singular>(ops, n_src, n_tgt, num_sms);
-	case 1: return ws_induce_ops<Reg::Winckelmans>(ops, n_src, n_tgt, num_sms);
-	case 2: return ws_induce_ops<Reg::Planetary>(ops, n_src, n_tgt, num_sms);
-	default: return ws_induce_ops<Reg::Gaussian>(ops, n_src, n_tgt, num_sms);
-	}
+	return induce_ws(reg, ops, n_src, n_tgt, num_sms, choose_cfg(reg, ops, n_tgt));
 }
 
 cudaError_t p3d_induce(int reg, unsigned ops, const P3DInduceProblem& p, const LaunchEnv& env) {
 	if (p.n_tgt <= 0) return cudaSuccess;
-	switch (reg) {
-	case 0: return induce_ops<Reg::Singular>(ops, p, env);
-	case 1: return induce_ops<Reg::Winckelmans>(ops, p, env);
-	case 2: return induce_ops<Reg::Planetary>(ops, p, env);
-	case 3: return induce_ops<Reg::Gaussian>(ops, p, env);
-	default: return cudaErrorInvalidValue;
-	}
+	if (reg < 0 || reg > 3 || ops < 1 || ops > 3) return cudaErrorInvalidValue;
+	return induce_launch(reg, ops, p, env, choose_cfg(reg, ops, p.n_tgt), false);
 }
 
 cudaError_t p3d_induce_bounded(int reg, unsigned ops, const P3DInduceProblem& p,
 	const LaunchEnv& env) {
 	if (p.n_tgt <= 0) return cudaSuccess;
-	switch (reg) {
-	case 0: return induce_bounded_ops<Reg::Singular>(ops, p, env);
-	case 1: return induce_bounded_ops<Reg::Winckelmans>(ops, p, env);
-	case 2: return induce_bounded_ops<Reg::Planetary>(ops, p, env);
-	case 3: return induce_bounded_ops<Reg::Gaussian>(ops, p, env);
-	default: return cudaErrorInvalidValue;
-	}
+	if (reg < 0 || reg > 3 || ops < 1 || ops > 3) return cudaErrorInvalidValue;
+	return induce_launch(reg, ops, p, env, choose_cfg(reg, ops, p.n_tgt), true);
+}
+
+int p3d_induce_num_configs() { return kNumCfg; }
+
+bool p3d_induce_config(int cfg, int* tpt, int* nt, int* packed) {
+	if (cfg < 0 || cfg >= kNumCfg) return false;
+	*tpt = kCfg[cfg].tpt; *nt = kCfg[cfg].nt; *packed = kCfg[cfg].packed ? 1 : 0;
+	return true;
+}
+
+bool p3d_induce_set_tuned(int reg, unsigned ops, int bucket, int cfg) {
+	if (reg < 0 || reg > 3 || ops < 1 || ops > 3 || bucket < 0 || bucket >= kNumSizeBuckets ||
+		cfg < -1 || cfg >= kNumCfg) return false;
+	g_tuned[reg][ops][bucket].store(cfg);
+	return true;
+}
+
+int p3d_induce_current_config(int reg, unsigned ops, int n_tgt) {
+	return choose_cfg(reg & 3, ops & 3, n_tgt);
 }
 
 size_t p3d_visc_ws_bytes(int reg, int n_src, int n_tgt, int num_sms) {

@@ -22,8 +22,9 @@
 // (r2 == 0) are masked to zero by the callers, as the reference does.
 //
 // Winckelmans, rewritten with q = x2 + 1 and s = q^-1/2 (no cancellation):
-//   g/rho^3 = (q + 1.5) s^5 = s^3 (1 + 1.5 s^2),
-//   (3 g/rho^3 - zeta)/rho^2 = (3 q + 7.5) s^7 = s^5 (3 + 7.5 s^2),
+//   g/rho^3 = (q + 1.5) s^5 = s^3 + 1.5 s^5,
+//   (3 g/rho^3 - zeta)/rho^2 = (3 q + 7.5) s^7 = 3 s^5 (1 + 2.5 s^2)
+//   (the kernels carry K/3 and fold the 3 into the per-call scale),
 //   eta3 = 52.5 s^9,  g2/rho^2 = (q + 1) s^4.
 // Gaussian 3D: the reference's Abramowitz & Stegun 7.1.26 erf (with g = 1 for
 // rho > 6) is used for rho >= rho_c; below rho_c, where erf minus its
@@ -72,15 +73,16 @@ template <> struct RegP3D<Reg::Singular> {
 
 // ---- Winckelmans (high-order algebraic) ---------------------------------
 template <> struct RegP3D<Reg::Winckelmans> {
-	// Gs = (q+1.5) s^5 = s^3 (1 + 1.5 s^2), Ks = (3q+7.5) s^7 = s^5 (3 + 7.5 s^2)
-	// (q s^2 = 1; K_scale = 1/sigma^2)
+	// Gs = (q+1.5) s^5 = s^3 + 1.5 s^5, Ks = (3q+7.5) s^7 / 3 = s^5 (1 + 2.5 s^2)
+	// (q s^2 = 1; K_scale = 3/sigma^2)
 	__device__ __forceinline__ static void gk(float r2, const RegConsts& c, float& G, float& K) {
 		const float q = fmaf(r2, c.inv_s2, 1.f);
 		const float s = rsqrt_approx(q);
 		const float s2 = s * s;
 		const float s3 = s2 * s;
-		G = s3 * fmaf(1.5f, s2, 1.f);
-		K = (s3 * s2) * fmaf(7.5f, s2, 3.f);
+		const float s5 = s3 * s2;
+		G = fmaf(1.5f, s5, s3);
+		K = s5 * fmaf(2.5f, s2, 1.f);
 	}
 	__device__ __forceinline__ static float g(float r2, const RegConsts& c) {
 		const float q = fmaf(r2, c.inv_s2, 1.f);
@@ -195,6 +197,9 @@ template <Reg R> struct RegP3D2 {
 		RegP3D<R>::gk(r2.x, c, G.x, K.x);
 		RegP3D<R>::gk(r2.y, c, G.y, K.y);
 	}
+	__device__ __forceinline__ static float2 g2(float2 r2, const RegConsts& c) {
+		return make_float2(RegP3D<R>::g(r2.x, c), RegP3D<R>::g(r2.y, c));
+	}
 };
 template <> struct RegP3D2<Reg::Winckelmans> {
 	__device__ __forceinline__ static void gk2(float2 r2, const RegConsts& c, float2& G, float2& K) {
@@ -202,8 +207,15 @@ template <> struct RegP3D2<Reg::Winckelmans> {
 		const float2 s = make_float2(rsqrt_approx(q.x), rsqrt_approx(q.y));
 		const float2 s2 = __fmul2_rn(s, s);
 		const float2 s3 = __fmul2_rn(s2, s);
-		G = __fmul2_rn(s3, __ffma2_rn(bc2(1.5f), s2, bc2(1.f)));
-		K = __fmul2_rn(__fmul2_rn(s3, s2), __ffma2_rn(bc2(7.5f), s2, bc2(3.f)));
+		const float2 s5 = __fmul2_rn(s3, s2);
+		G = __ffma2_rn(bc2(1.5f), s5, s3);
+		K = __fmul2_rn(s5, __ffma2_rn(bc2(2.5f), s2, bc2(1.f)));
+	}
+	__device__ __forceinline__ static float2 g2(float2 r2, const RegConsts& c) {
+		const float2 q = __ffma2_rn(r2, bc2(c.inv_s2), bc2(1.f));
+		const float2 s = make_float2(rsqrt_approx(q.x), rsqrt_approx(q.y));
+		const float2 s2 = __fmul2_rn(s, s);
+		return __fmul2_rn(__fmul2_rn(s2, s), __ffma2_rn(bc2(1.5f), s2, bc2(1.f)));
 	}
 };
 

@@ -227,6 +227,22 @@ DeviceContext* Runtime::active_context() {
 }
 
 // ---- error reporting -------------------------------------------------------
+std::string device_error_text(unsigned w) {
+	std::string t;
+	auto add = [&](unsigned bit, const char* what) {
+		if (!(w & bit)) return;
+		if (!t.empty()) t += ", ";
+		t += what;
+	};
+	add(1u, "a device-side wait expired");
+	add(2u, "draining copies after an expired wait timed out");
+	add(4u, "a misaligned bulk copy was skipped");
+	add(8u, "launch shape or shared-memory alignment not as expected");
+	add(16u, "a work item was out of range");
+	if (t.empty()) t = "device error";
+	return t + " (code " + std::to_string(w) + ")";
+}
+
 static std::mutex g_err_mu;
 static std::string g_err;
 

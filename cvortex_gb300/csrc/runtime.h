@@ -81,6 +81,8 @@ class Runtime {
 };
 
 // Error reporting for the GPU path (the reference ABI functions return void).
+// Text of a nonzero device error word (the kErr* bits of common.cuh).
+std::string device_error_text(unsigned word);
 void set_error(const std::string& msg);
 void clear_error();
 const char* last_error();

@@ -15,6 +15,10 @@ benchmark workloads (no public dataset is involved; all inputs are generated).
   uniform direction (exercises rho << 1 pairs).
 * wake_sheet: straight filament segments of length 0.02 tiling a 1 x 0.2
   sheet, strength N(0, 1).
+* serve_stream: the served mixed-size request stream (Poisson arrivals; 60%
+  P3D vel+dvort on uniform_cube, 25% P2D vel on gaussian_patch_2d, 15% F3D
+  vel of a wake_sheet on as many tracer points in its box inflated by 0.1;
+  sizes log-uniform on [500, 200,000]).
 """
 from __future__ import annotations
 
@@ -92,3 +96,38 @@ def sheet_targets(n: int, seed: int = SEEDS["sheet"] + 100):
 def batch_sizes(count: int = 512, lo: int = 1000, hi: int = 50000, seed: int = SEEDS["batch"]):
     rng = np.random.Generator(np.random.PCG64(seed))
     return np.exp(rng.uniform(math.log(lo), math.log(hi), count)).astype(np.int64)
+
+
+# ---- served request stream ---------------------------------------------------
+SERVE_KINDS = ("p3d", "p2d", "f3d")
+SERVE_MIX = (0.60, 0.25, 0.15)
+
+
+def serve_stream(count: int, rate: float, lo: int = 500, hi: int = 200_000,
+                 seed: int = SEEDS["serve"]):
+    """Poisson arrivals at `rate` requests/s of a 60/25/15 mix of P3D vel+dvort,
+    P2D vel and F3D vel requests, sizes log-uniform on [lo, hi].
+
+    Returns (arrival_s, kinds, sizes, seeds); request i is built by
+    serve_request_arrays(kinds[i], sizes[i], seeds[i]).
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    gaps = rng.exponential(1.0 / rate, count)
+    arrival = np.cumsum(gaps) - gaps[0]
+    kinds = rng.choice(len(SERVE_KINDS), size=count, p=SERVE_MIX)
+    sizes = np.exp(rng.uniform(math.log(lo), math.log(hi), count)).astype(np.int64)
+    seeds = rng.integers(0, 2**31 - 1, count)
+    return arrival, kinds, sizes, seeds
+
+
+def serve_request_arrays(kind: int, n: int, seed: int):
+    """Inputs of one served request: (particles or filaments, tracer points).
+
+    P3D: uniform_cube; P2D: gaussian_patch_2d; F3D: wake_sheet filaments with
+    n tracer points from sheet_targets."""
+    n = int(n)
+    if kind == 0:
+        return uniform_cube(n, int(seed)), None
+    if kind == 1:
+        return gaussian_patch_2d(n, int(seed)), None
+    return wake_sheet(n, int(seed)), sheet_targets(n, int(seed) + 1)

@@ -54,6 +54,17 @@ CVTX_EXPORT int cvtx_gb300_probe_fp32_tflops(int repeats, double* tflops);
 CVTX_EXPORT int cvtx_gb300_probe_fp32_detail(int repeats, double* scalar_fma,
 	double* packed_fma);
 
+/* Launch configurations of the P3D velocity / stretching kernels (targets
+ * per thread, threads per CTA, packed two-wide FP32 arithmetic or scalar) and
+ * the table that selects one per (reg, ops, target-count bucket); ops: 1 vel,
+ * 2 dvort, 3 both; cfg -1 restores the built-in choice. The autotuner in
+ * cvortex_gb300/autotune.py fills the table. */
+CVTX_EXPORT int cvtx_gb300_p3d_num_configs(void);
+CVTX_EXPORT int cvtx_gb300_p3d_config_info(int cfg, int* tpt, int* nt, int* packed);
+CVTX_EXPORT int cvtx_gb300_size_bucket(int n_targets);
+CVTX_EXPORT int cvtx_gb300_p3d_set_tuned(int reg, int ops, int bucket, int cfg);
+CVTX_EXPORT int cvtx_gb300_p3d_current_config(int reg, int ops, int n_targets);
+
 /* Velocity at and vortex stretching of every particle of one set, in one
  * pass over the pairs: equivalent to cvtx_P3D_M2M_vel(p, n, coords(p), n,
  * vel) followed by cvtx_P3D_M2M_dvort(p, n, p, n, dvort). Either output may
@@ -88,6 +99,143 @@ CVTX_EXPORT int cvtx_gb300_dev_F3D_M2M_vel(const void* fil, int n_fil,
 CVTX_EXPORT int cvtx_gb300_dev_P3D_M2M_noalloc(const void* src, int n_src,
 	const void* tgt, int tgt_stride, int n_tgt, float* vel_out,
 	float* dvort_out, int reg, float regularisation_radius, void* stream);
+/* ---- batched form: many independent P3D problems in one launch ----------
+ * Each problem is a device-pointer problem as for cvtx_gb300_dev_P3D_M2M
+ * (records as above; dvort needs tgt_stride >= 2). All problems of a batch
+ * share the regularisation and ops (1 vel, 2 dvort, 3 both); sigma is per
+ * problem. The batch is cut into (problem, target block, source chunk)
+ * work items that persistent CTAs claim largest-first, so uneven sizes share
+ * the GPU in one launch; results are deterministic. cvtx_gb300_batch_tune
+ * times every launch shape x source chunk on the batch and keeps the
+ * fastest; cvtx_gb300_batch_capture records the run as a CUDA graph that
+ * cvtx_gb300_batch_run then replays. Inputs and outputs must stay valid
+ * while the batch exists. */
+typedef struct {
+	const void* src; int n_src;
+	const void* tgt; int tgt_stride; int n_tgt;
+	float* vel_out; float* dvort_out;
+	float sigma;
+} cvtx_gb300_p3d_problem;
+typedef struct cvtx_gb300_batch cvtx_gb300_batch;
+CVTX_EXPORT cvtx_gb300_batch* cvtx_gb300_batch_create(
+	const cvtx_gb300_p3d_problem* problems, int n_problems, int reg, int ops);
+CVTX_EXPORT int cvtx_gb300_batch_tune(cvtx_gb300_batch* batch, int repeats);
+CVTX_EXPORT int cvtx_gb300_batch_capture(cvtx_gb300_batch* batch);
+CVTX_EXPORT int cvtx_gb300_batch_run(cvtx_gb300_batch* batch, void* stream);
+CVTX_EXPORT int cvtx_gb300_batch_status(cvtx_gb300_batch* batch);
+CVTX_EXPORT int cvtx_gb300_batch_info(const cvtx_gb300_batch* batch, int* tpt,
+	int* nt, int* chunk, int* n_items, int* graph, double* interactions);
+CVTX_EXPORT void cvtx_gb300_batch_destroy(cvtx_gb300_batch* batch);
+
+/* ---- device-resident time step -------------------------------------------
+ * One forward-Euler step of a P3D particle set held on the device as records
+ * (stride 2): computes the induced velocity and vorticity rate of every
+ * particle (as cvtx_P3D_M2M_vel + cvtx_P3D_M2M_dvort with the set as both
+ * sources and targets), then x += dt u, alpha += dt dalpha in place. vel and
+ * dvort (3 * n floats each, device) receive the rates at the start of the
+ * step. No counterpart in the reference, whose callers integrate on the host. */
+CVTX_EXPORT int cvtx_gb300_dev_P3D_step(void* rec, int n, float* vel, float* dvort,
+	int reg, float regularisation_radius, float dt, void* stream);
+
+/* ---- serving loop: continuous batching of M2M requests ------------------
+ * Requests arrive from any thread (cvtx_gb300_server_submit). A scheduler
+ * thread admits them in arrival order as slots and device memory free up:
+ * each admitted request takes one slot (a CUDA stream pair and a fixed
+ * workspace) and a range of one device arena sized by the HBM budget; a
+ * request that could never fit the budget is rejected. Its state is copied in
+ * once, stays resident for all n_steps time steps (M2M + Euler update on the
+ * device), and is copied out once; requests on different slots overlap on the
+ * GPU. Results depend only on the request (fixed partition and reduction
+ * order), never on what else is in flight. Kinds:
+ *   CVTX_GB300_REQ_P3D: state = n P3D records (8 floats: x,y,z,vol, a_x,a_y,a_z,0);
+ *       each step vel + dvort of the set on itself, x += dt u, a += dt da.
+ *   CVTX_GB300_REQ_P2D: state = n P2D records (4 floats: x,y,Gamma,area);
+ *       each step vel of the set on itself, x += dt u.
+ *   CVTX_GB300_REQ_F3D: state = n filaments (8 floats: start, strength, end, 0)
+ *       fixed, and n_tgt tracer points (4 floats: x,y,z,0) advected by the
+ *       filaments' velocity.
+ * state_out (same layout as state_in, or the tracer points for F3D) and
+ * vel_out (velocity of the last step: 3 or 2 floats per particle / point, or
+ * NULL) are written when the request completes. Host buffers may be pageable
+ * (staged through pinned memory) or pinned; they must stay valid until the
+ * request completes. */
+enum {
+	CVTX_GB300_REQ_P3D = 0, CVTX_GB300_REQ_P2D = 1, CVTX_GB300_REQ_F3D = 2
+};
+/* request status */
+enum {
+	CVTX_GB300_ST_DONE = 0, CVTX_GB300_ST_PENDING = 1, CVTX_GB300_ST_RUNNING = 2,
+	CVTX_GB300_ST_REJECTED = -1,      /* larger than the whole HBM budget, or invalid */
+	CVTX_GB300_ST_OOM = -2,           /* device memory could not be had */
+	CVTX_GB300_ST_FAILED = -3,        /* a CUDA call failed */
+	CVTX_GB300_ST_TIMEOUT = -4,       /* a device-side wait expired */
+	CVTX_GB300_ST_UNKNOWN = -5        /* no such request */
+};
+typedef struct {
+	int kind;          /* CVTX_GB300_REQ_* */
+	int reg;           /* 0 singular, 1 winckelmans, 2 planetary, 3 gaussian */
+	float sigma;       /* regularisation radius */
+	float dt;          /* time step */
+	int n_steps;
+	int n;             /* particles, or filaments for F3D */
+	int n_tgt;         /* F3D tracer points (ignored otherwise) */
+	const float* state_in;
+	const float* tgt_in;   /* F3D tracer points */
+	float* state_out;
+	float* vel_out;
+} cvtx_gb300_request;
+typedef struct {
+	unsigned long long submitted, completed, rejected, failed, queued, in_flight;
+	double p50_ms, p99_ms, mean_ms, max_ms;     /* submit -> results in host memory */
+	double queue_p50_ms, queue_p99_ms;          /* submit -> admission */
+	double interactions;       /* source x target pairs of completed requests */
+	double span_s;             /* first submit -> last completion */
+	unsigned long long hbm_budget, hbm_used, hbm_peak;
+	unsigned long long kernel_launches;
+} cvtx_gb300_server_stats;
+typedef struct cvtx_gb300_server cvtx_gb300_server;
+/* n_slots: concurrent requests (0 = 16). hbm_bytes: arena size (0 = half of
+ * the free device memory, at most 64 GiB). flags: CVTX_GB300_SERVER_DRY_RUN
+ * runs the scheduler without a GPU (requests complete at admission without
+ * computing; for testing admission logic). */
+enum { CVTX_GB300_SERVER_DRY_RUN = 1 };
+CVTX_EXPORT cvtx_gb300_server* cvtx_gb300_server_create(int n_slots,
+	unsigned long long hbm_bytes, int flags);
+/* Returns a request id (> 0), or 0 if the request is invalid. */
+CVTX_EXPORT unsigned long long cvtx_gb300_server_submit(cvtx_gb300_server* srv,
+	const cvtx_gb300_request* req);
+/* Submit reqs[i] at arrival_s[i] seconds after the call (non-decreasing),
+ * from the calling thread; ids_out[i] receives the ids. Returns once every
+ * request is submitted (not completed). */
+CVTX_EXPORT int cvtx_gb300_server_replay(cvtx_gb300_server* srv,
+	const cvtx_gb300_request* reqs, const double* arrival_s, int n,
+	unsigned long long* ids_out);
+/* Wait up to timeout_ms (< 0: no limit) for one request; returns its status. */
+CVTX_EXPORT int cvtx_gb300_server_wait(cvtx_gb300_server* srv,
+	unsigned long long id, double timeout_ms);
+/* Wait for every submitted request; returns 0, or 1 on timeout. */
+CVTX_EXPORT int cvtx_gb300_server_drain(cvtx_gb300_server* srv, double timeout_ms);
+/* Latency (submit -> done) and queueing delay of a finished request. */
+CVTX_EXPORT int cvtx_gb300_server_request_info(cvtx_gb300_server* srv,
+	unsigned long long id, double* latency_ms, double* queue_ms);
+CVTX_EXPORT int cvtx_gb300_server_stats_get(cvtx_gb300_server* srv,
+	cvtx_gb300_server_stats* out);
+/* Restart the statistics and forget finished requests (their ids become
+ * unknown); call it while no thread waits on a request. */
+CVTX_EXPORT void cvtx_gb300_server_reset_stats(cvtx_gb300_server* srv);
+/* Host-side fault injection: the next `count` arena allocations fail as if
+ * the device were out of memory. */
+CVTX_EXPORT void cvtx_gb300_server_inject_alloc_failures(cvtx_gb300_server* srv,
+	int count);
+/* Drains, then frees every resource. */
+CVTX_EXPORT void cvtx_gb300_server_destroy(cvtx_gb300_server* srv);
+
+/* Failure-path self test: one CTA waits, for at most limit_ms (0 < limit_ms
+ * <= 1000), on an mbarrier that nothing completes, then records the expiry
+ * in an error word the way the all-pairs kernels do. Returns that word
+ * (1 = wait expired, the expected answer) or a negative code. */
+CVTX_EXPORT int cvtx_gb300_selftest_withheld_wait(double limit_ms);
+
 /* Synchronise `stream`, then read and reset the device error word. Returns 0
  * if no device-side wait expired since the previous check. */
 CVTX_EXPORT int cvtx_gb300_dev_status(void* stream);

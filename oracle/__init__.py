@@ -64,6 +64,7 @@ _SIGS = {
     "oracle_F3D_M2M_dvort": (None, [_vp, _i, _vp, _i, _vp]),
     "oracle_F3D_inf_mtrx": (None, [_vp, _i, _vp, _vp, _i, _vp]),
     "oracle_num_threads": (_i, []),
+    "oracle_exact_P3D_vel_dvort": (None, [_vp, _vp, _i, _vp, _vp, _i, _i, C.c_double, _vp, _vp]),
 }
 
 _lib = None
@@ -169,6 +170,23 @@ def f3d_inf_mtrx(fil, mes, dirs):
     out = np.zeros((mes.shape[0], len(fil)), np.float32)
     lib().oracle_F3D_inf_mtrx(_a(p), len(fil), _a(mes), _a(dirs), mes.shape[0], _a(out))
     return out
+
+
+def exact_p3d_vel_dvort(src, tgt_xyz, tgt_alpha, reg, sigma, want_vel=True, want_dvort=True):
+    """FP64 exact-math velocity / stretching (compiled, OpenMP); see
+    oracle_exact_P3D_vel_dvort in cvtx_oracle.c."""
+    sx = np.ascontiguousarray(src["coord"], np.float64)
+    sa = np.ascontiguousarray(src["vorticity"], np.float64)
+    tx = np.ascontiguousarray(tgt_xyz, np.float64)
+    ta = None if tgt_alpha is None else np.ascontiguousarray(tgt_alpha, np.float64)
+    m = tx.shape[0]
+    vel = np.zeros((m, 3)) if want_vel else None
+    dv = np.zeros((m, 3)) if want_dvort else None
+    lib().oracle_exact_P3D_vel_dvort(_a(sx), _a(sa), len(sx), _a(tx),
+                                     None if ta is None else _a(ta), m, REG[reg], float(sigma),
+                                     None if vel is None else _a(vel),
+                                     None if dv is None else _a(dv))
+    return vel, dv
 
 
 def regfunc(reg: str, which: str, rho: float) -> float:

@@ -453,3 +453,88 @@ int oracle_num_threads(void) {
 	return 1;
 #endif
 }
+
+/* ---- FP64 exact-math evaluation (the "error vs FP64" reference) ----------
+ * Same formulas as oracle/exact.py, in double precision with the C library's
+ * erf, for large error reports: P3D velocity and stretching at n_tgt targets
+ * from n_src sources (arrays of xyz triples), OpenMP over targets.
+ * G = g/rho^3 and K = (3G - zeta)/rho^2 come from their Taylor series for
+ * the Gaussian below rho = 0.5 (the closed forms cancel there). */
+static void ex_gk(int reg, double rho, double* G, double* K) {
+	const double x = rho * rho;
+	const double sq2pi = 0.79788456080286535588;
+	switch (reg) {
+	case 0: *G = 1.0 / (x * rho); *K = 3.0 * *G / x; return;
+	case 1: {
+		const double q = x + 1.0;
+		*G = (q + 1.5) * pow(q, -2.5);
+		*K = (3.0 * q + 7.5) * pow(q, -3.5);
+		return;
+	}
+	case 2:
+		if (rho < 1.0) { *G = 1.0; *K = 0.0; }
+		else { *G = 1.0 / (x * rho); *K = 3.0 / (x * x * rho); }
+		return;
+	default:
+		if (rho < 0.5) {
+			double g = 0.0, k = 0.0, fact = 1.0, p2 = 1.0, xn = 1.0;
+			for (int n = 0; n < 16; ++n) {
+				if (n > 0) { fact *= n; p2 *= 2.0; }
+				g += ((n & 1) ? -1.0 : 1.0) * xn / (p2 * fact * (2 * n + 3));
+				xn *= x;
+			}
+			fact = 1.0; p2 = 1.0; xn = 1.0;
+			for (int n = 1; n < 17; ++n) {
+				fact *= n; p2 *= 2.0;
+				k += ((n & 1) ? 1.0 : -1.0) * 2.0 * n * xn / (p2 * fact * (2 * n + 3));
+				xn *= x;
+			}
+			*G = sq2pi * g;
+			*K = sq2pi * k;
+		} else {
+			const double e = exp(-0.5 * x);
+			const double g = erf(rho / sqrt(2.0)) - rho * sq2pi * e;
+			*G = g / (x * rho);
+			*K = (3.0 * *G - sq2pi * e) / x;
+		}
+		return;
+	}
+}
+
+void oracle_exact_P3D_vel_dvort(const double* sx, const double* sa, int n_src,
+	const double* tx, const double* ta, int n_tgt, int reg, double sigma,
+	double* vel, double* dvort)
+{
+	const double pi = 3.14159265358979323846;
+	const double as = fabs(sigma);
+	long i;
+#pragma omp parallel for schedule(dynamic, 16)
+	for (i = 0; i < n_tgt; ++i) {
+		double v[3] = {0, 0, 0}, w[3] = {0, 0, 0};
+		const double* t = tx + 3 * i;
+		const double* at = ta ? ta + 3 * i : 0;
+		for (long j = 0; j < n_src; ++j) {
+			const double* s = sx + 3 * j;
+			const double* a = sa + 3 * j;
+			const double d[3] = {t[0] - s[0], t[1] - s[1], t[2] - s[2]};
+			const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+			if (r2 == 0.0) continue;
+			double G, K;
+			ex_gk(reg, sqrt(r2) / as, &G, &K);
+			if (vel) {
+				const double c[3] = {d[1] * a[2] - d[2] * a[1], d[2] * a[0] - d[0] * a[2],
+					d[0] * a[1] - d[1] * a[0]};
+				for (int k = 0; k < 3; ++k) v[k] += G * c[k];
+			}
+			if (dvort && at) {
+				const double co[3] = {at[1] * a[2] - at[2] * a[1], at[2] * a[0] - at[0] * a[2],
+					at[0] * a[1] - at[1] * a[0]};
+				const double dco = d[0] * co[0] + d[1] * co[1] + d[2] * co[2];
+				for (int k = 0; k < 3; ++k)
+					w[k] += G * co[k] - K * dco * d[k] / (sigma * sigma);
+			}
+		}
+		if (vel) for (int k = 0; k < 3; ++k) vel[3 * i + k] = -v[k] / (4 * pi * as * as * as);
+		if (dvort) for (int k = 0; k < 3; ++k) dvort[3 * i + k] = w[k] / (4 * pi * sigma * sigma * sigma);
+	}
+}

@@ -12,7 +12,7 @@ import oracle
 from conftest import REGS
 from cvortex_gb300 import abi, workloads
 from oracle import exact
-from parity import check
+from parity import TOL, check
 
 pytestmark = pytest.mark.gpu
 
@@ -135,3 +135,15 @@ def test_vort_and_relaxation(gpu, reg):
     gpu.relax(b, 0.3, reg, 0.05)
     gpu.set_accelerated(True)
     close(a["vorticity"], b["vorticity"], 1e-5)
+
+
+def test_withheld_doorbell_reports_timeout(gpu):
+    """A wait on an mbarrier that nothing completes runs out after its limit,
+    the kernel records the expiry and returns, and the context keeps working."""
+    import time
+    t0 = time.perf_counter()
+    assert gpu.lib.cvtx_gb300_selftest_withheld_wait(50.0) == 1
+    assert time.perf_counter() - t0 < 5.0
+    p = workloads.uniform_cube(500, seed=3)
+    vel = gpu.p3d_vel(p, p["coord"], "winckelmans", 0.05)
+    assert exact.rel_l2(vel, oracle.p3d_vel(p, p["coord"], "winckelmans", 0.05)) <= TOL
