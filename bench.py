@@ -68,6 +68,21 @@ def parse():
     return ap.parse_args()
 
 
+def profiled_traffic(n, reg):
+    """DRAM bytes per launch of the benchmark kernel from the committed ncu
+    summary (profiles/), when it covers this workload; else None."""
+    if n != 100_000 or reg != "winckelmans":
+        return None
+    f = ROOT / "profiles" / "p3d_induce2_ring100k_launches.md"
+    try:
+        for line in f.read_text().splitlines():
+            if line.startswith("traffic_bytes_per_launch:"):
+                return int(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
 def dist_env():
     from cvortex_gb300.multi import dist_env as env
     return env()
@@ -265,7 +280,11 @@ def run_ours(args):
                    "interactions_per_step": pairs, "l2": "flushed between steps (256 MB write)",
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
-                     "frac": achieved / peak.value if peak.value else None, "traffic": None,
+                     "frac": achieved / peak.value if peak.value else None,
+                     "traffic": profiled_traffic(n, args.reg),
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
+                                       "launch (profiles/p3d_induce2_ring100k_launches.md); "
+                                       "algorithmic bytes 5.6 MB, the rest FP64 split partials",
                      "peak_source": "measured FP32 FMA probe, max of scalar FFMA "
                                     f"{p_scalar.value:.2f} and packed f32x2 FFMA "
                                     f"{p_packed.value:.2f} TFLOP/s",

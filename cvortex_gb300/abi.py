@@ -191,6 +191,7 @@ _EXT_SIGS = {
     "cvtx_gb300_dev_status": (_i, [_vp]),
     "cvtx_gb300_probe_fp32_tflops": (_i, [_i, C.POINTER(C.c_double)]),
     "cvtx_gb300_probe_fp32_detail": (_i, [_i, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "cvtx_gb300_probe_fp32_mix": (_i, [_i, _i, _i, C.POINTER(C.c_double)]),
     "cvtx_gb300_dev_pack_P3D": (_i, [_vp, _i, _vp, _vp]),
     "cvtx_gb300_dev_pack_V3f": (_i, [_vp, _i, _vp, _vp]),
 }

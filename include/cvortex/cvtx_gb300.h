@@ -53,6 +53,10 @@ CVTX_EXPORT void cvtx_gb300_set_gaussian_rho_c(float rho_c);
 CVTX_EXPORT int cvtx_gb300_probe_fp32_tflops(int repeats, double* tflops);
 CVTX_EXPORT int cvtx_gb300_probe_fp32_detail(int repeats, double* scalar_fma,
 	double* packed_fma);
+/* FMA throughput with `packed` f32x2 and `scalar` FP32 FMA chains per thread
+ * issued together ((packed, scalar) from a fixed set; -1 otherwise). */
+CVTX_EXPORT int cvtx_gb300_probe_fp32_mix(int packed, int scalar, int repeats,
+	double* tflops);
 
 /* Launch configurations of the P3D velocity / stretching kernels (targets
  * per thread, threads per CTA, packed two-wide FP32 arithmetic or scalar) and
