@@ -122,6 +122,20 @@ def cpu_step(kind, ref, p, sub, reg):
         oracle.p3d_dvort(p, sub, reg, SIGMA)
 
 
+def cpu_model():
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu model")):
+                return line.split(":", 1)[1].strip()
+        out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
 def cpu_cores():
     try:
         return len(os.sched_getaffinity(0))
@@ -131,6 +145,7 @@ def cpu_cores():
 
 def cpu_baseline(p, reg, reps=3, sample=CPU_SAMPLE_TARGETS):
     os.environ.setdefault("OMP_NUM_THREADS", str(cpu_cores()))
+    os.environ.setdefault("OMP_PROC_BIND", "spread")
     kind, ref = cpu_reference()
     idx = np.random.Generator(np.random.PCG64(7)).choice(len(p), min(sample, len(p)), replace=False)
     sub = p[np.sort(idx)].copy()
@@ -141,7 +156,7 @@ def cpu_baseline(p, reg, reps=3, sample=CPU_SAMPLE_TARGETS):
     dt = time.perf_counter() - t0
     pairs = reps * len(sub) * len(p)
     return {"value": pairs / dt / 1e9, "unit": UNIT, "cores": int(os.environ["OMP_NUM_THREADS"]),
-            "kind": kind,
+            "kind": kind, "cpu_model": cpu_model(), "omp_proc_bind": os.environ["OMP_PROC_BIND"],
             "sample": f"{reps} x (vel + dvort) for {len(sub)} sampled targets x {len(p)} sources "
                       f"({dt:.1f} s of CPU time)"}
 
@@ -397,6 +412,7 @@ def extras(cv, lib, args, torch, sh, peak):
     ms = timed_dev(f, torch, 5)
     res["p2d_patch200k_gaussian_vel"] = {"ginter_s": len(q) ** 2 / ms / 1e6}
     res["batch512"] = batch_extra(cv, lib, torch, sh)
+    res["redistribute_ring200k_m4p"] = redistribute_extra(cv, lib)
     m = 1_000_000
     big = workloads.uniform_cube(m)
     rb = torch.from_numpy(p3d_records(big).reshape(m, 8)).cuda()
@@ -409,6 +425,39 @@ def extras(cv, lib, args, torch, sh, peak):
         "ginter_s": m * m / ms / 1e6, "ms": ms,
         "fp32_frac": 61 * m * m / (ms * 1e-3) / 1e12 / peak}
     return res
+
+
+def redistribute_extra(cv, lib, n=200_000, gd=0.01):
+    """cvtx_P3D_redistribute_on_grid (M4' stencil, 125 grid points per
+    particle) of a 200,000-particle vortex ring: the GPU path against this
+    library's host path (all host cores); both give identical particles.
+    (The reference's own implementation does not terminate when built with
+    GCC, so it has no time here.)"""
+    from cvortex_gb300 import abi, workloads
+    p = workloads.vortex_ring(n)
+    ptrs = abi.ptr_array(p)
+    cap = 4 * n * 8
+    out = np.zeros(cap, abi.P3D_DTYPE)
+    rf = lib.cvtx_RedistFunc_m4p()
+
+    def run():
+        t0 = time.perf_counter()
+        m = lib.cvtx_P3D_redistribute_on_grid(ptrs.ctypes.data, n, out.ctypes.data, cap,
+                                              C.byref(rf), gd, 1e-3)
+        return m, time.perf_counter() - t0
+
+    run()
+    m_gpu, t_gpu = min((run() for _ in range(3)), key=lambda x: x[1])
+    cv.set_accelerated(False)
+    try:
+        m_host, t_host = run()
+    finally:
+        cv.set_accelerated(True)
+    if m_gpu != m_host:
+        raise RuntimeError("redistribution: GPU and host paths disagree")
+    return {"particles_in": n, "particles_out": int(m_gpu), "grid_points_touched": n * 125,
+            "gpu_ms": t_gpu * 1e3, "host_ms": t_host * 1e3, "host_cores": cpu_cores(),
+            "speedup": t_host / t_gpu}
 
 
 def batch_extra(cv, lib, torch, sh, count=512):
@@ -437,6 +486,18 @@ def batch_extra(cv, lib, torch, sh, count=512):
                 raise RuntimeError(cv.last_error())
 
     ms_plain = timed_dev(plain, torch, 2)
+
+    def plain_separate():
+        for n, rec, v, d in keep:
+            for vel, dv in ((v, None), (None, d)):
+                rc = lib.cvtx_gb300_dev_P3D_M2M(rec.data_ptr(), n, rec.data_ptr(), 2, n,
+                                                vel.data_ptr() if vel is not None else None,
+                                                dv.data_ptr() if dv is not None else None,
+                                                1, SIGMA, sh)
+                if rc != 0:
+                    raise RuntimeError(cv.last_error())
+
+    ms_plain_sep = timed_dev(plain_separate, torch, 2)
     arr = (abi.cvtx_gb300_p3d_problem * count)(*probs)
     b = lib.cvtx_gb300_batch_create(arr, count, 1, 3)
     if not b:
@@ -462,18 +523,25 @@ def batch_extra(cv, lib, torch, sh, count=512):
     return {"problems": count, "interactions": pairs,
             "sizes": [int(sizes.min()), int(sizes.max())],
             "plain_ms": ms_plain, "plain_ginter_s": pairs / ms_plain / 1e6,
+            "plain_separate_ms": ms_plain_sep,
+            "plain_separate_ginter_s": pairs / ms_plain_sep / 1e6,
+            "plain_note": "plain = one fused vel+dvort device call per problem; plain_separate = "
+                          "a vel call then a dvort call per problem",
             "batched_ms": ms_batch, "batched_ginter_s": pairs / ms_batch / 1e6,
-            "speedup": ms_plain / ms_batch, "tuned_shape": [tpt.value, nt.value],
+            "speedup": ms_plain / ms_batch, "speedup_vs_separate": ms_plain_sep / ms_batch,
+            "tuned_shape": [tpt.value, nt.value],
             "tuned_chunk": chunk.value, "items": items.value, "graph": bool(graph.value),
             "tune_s": tune_s}
 
 
-def precision_extra(lib, torch, sh, n=1_000_000, sigma=0.01, n_random=1024, n_twin=512):
+def precision_extra(lib, torch, sh, n=1_000_000, sigma=0.01, n_random=6144, n_twin=1024,
+                    n_ref=2048):
     """Gaussian vel + dvort at N = 1M (uniform cube, sigma 0.01, 1% of the
     particles are twins at separation < 1e-3 sigma): the GPU path over all
     targets, checked on a seeded sample against the FP64 oracle (exact erf,
     series below rho = 0.5) over all sources. The sample holds n_random
-    random targets plus n_twin twins and their originals. Reported per
+    random targets plus n_twin twins and their originals (about 8,000); the
+    reference formulation is evaluated on a random n_ref of them. Reported per
     output: relative L2 and max relative error (per target vector, over
     targets whose FP64 value exceeds 1e-6 of the sample's RMS) of the GPU
     and of the reference CPU formulation (oracle restatement, FP32 pairs with
@@ -502,8 +570,11 @@ def precision_extra(lib, torch, sh, n=1_000_000, sigma=0.01, n_random=1024, n_tw
     t0 = time.perf_counter()
     v64, d64 = oracle.exact_p3d_vel_dvort(p, sub["coord"], sub["vorticity"], "gaussian", sigma)
     fp64_s = time.perf_counter() - t0
-    v_ref = oracle.p3d_vel(p, sub["coord"], "gaussian", sigma)
-    d_ref = oracle.p3d_dvort(p, sub, "gaussian", sigma)
+    # the reference formulation on a random n_ref of the sample targets (CPU time)
+    rsel = np.sort(rng.choice(len(idx), min(n_ref, len(idx)), replace=False))
+    rsub = sub[rsel].copy()
+    v_ref = oracle.p3d_vel(p, rsub["coord"], "gaussian", sigma)
+    d_ref = oracle.p3d_dvort(p, rsub, "gaussian", sigma)
 
     def errs(a, b):
         rms = float(np.sqrt(np.mean(np.sum(np.asarray(b) ** 2, axis=1))))
@@ -511,8 +582,11 @@ def precision_extra(lib, torch, sh, n=1_000_000, sigma=0.01, n_random=1024, n_tw
 
     return {"workload": f"uniform cube N={n}, 1% twins at < 1e-3 sigma, gaussian, sigma={sigma}",
             "sample_targets": int(len(idx)), "gpu_all_targets_s": gpu_s, "fp64_oracle_s": fp64_s,
-            "vel": {"gpu_vs_fp64": errs(v_gpu, v64), "reference_vs_fp64": errs(v_ref, v64)},
-            "dvort": {"gpu_vs_fp64": errs(d_gpu, d64), "reference_vs_fp64": errs(d_ref, d64)},
+            "reference_sample_targets": int(len(rsub)),
+            "vel": {"gpu_vs_fp64": errs(v_gpu, v64),
+                    "reference_vs_fp64": errs(v_ref, v64[rsel])},
+            "dvort": {"gpu_vs_fp64": errs(d_gpu, d64),
+                      "reference_vs_fp64": errs(d_ref, d64[rsel])},
             "rho_c": float(lib.cvtx_gb300_gaussian_rho_c())}
 
 
@@ -627,6 +701,7 @@ def run_reference(args):
         return
     from cvortex_gb300 import workloads
     os.environ.setdefault("OMP_NUM_THREADS", str(cpu_cores()))
+    os.environ.setdefault("OMP_PROC_BIND", "spread")
     kind, ref = cpu_reference()
     p = workloads.vortex_ring(args.n)
     idx = np.random.Generator(np.random.PCG64(7)).choice(args.n, min(CPU_SAMPLE_TARGETS, args.n),
@@ -650,6 +725,7 @@ def run_reference(args):
                       "interactions_per_step": float(len(sub)) * len(p),
                       "parallelism": f"{cores} host threads (OpenMP)"},
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+                            "cpu_model": cpu_model(),
                             "sample": f"each step: vel + dvort for {len(sub)} sampled targets x "
                                       f"{len(p)} sources"},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

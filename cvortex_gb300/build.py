@@ -68,6 +68,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> Path:
         cu_flags += ["-Xptxas", "-v"]
     cxx = os.environ.get("CXX", "g++")
     cpp_flags = [cxx, "-O3", "-fPIC", "-fopenmp", "-fvisibility=hidden", "-std=c++17", "-Wall",
+                 "-ffp-contract=off",
                  "-Wno-unused-function",
                  *inc, "-I", str(cuda / "include")]
     jobs = []

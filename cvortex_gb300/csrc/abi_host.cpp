@@ -18,6 +18,7 @@
 
 #include "cvortex/libcvtx.h"
 #include "host_paths.h"
+#include "redist.h"
 
 namespace {
 
@@ -106,6 +107,22 @@ float m4p(float u) {
 cvtx_RedistFunc make_rf(float (*f)(float), float r) {
 	cvtx_RedistFunc x; x.func = f; x.radius = r; return x;
 }
+
+}  // namespace
+
+namespace cvtx {
+int redist_kind(const cvtx_RedistFunc* f) {
+	if (!f) return -1;
+	if (f->func == lambda0) return 0;
+	if (f->func == lambda1) return 1;
+	if (f->func == lambda2) return 2;
+	if (f->func == lambda3) return 3;
+	if (f->func == m4p) return 4;
+	return -1;
+}
+}  // namespace cvtx
+
+namespace {
 
 // ---- small vector helpers --------------------------------------------------
 inline bsv_V3f v3(float x, float y, float z) { bsv_V3f r = {{x, y, z}}; return r; }

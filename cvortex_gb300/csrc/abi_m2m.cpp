@@ -477,20 +477,6 @@ CVTX_EXPORT void cvtx_F3D_inf_mtrx(const cvtx_F3D** fil, const int n, const bsv_
 	if (st != 0) fill_nan(out, size_t(m) * size_t(n));
 }
 
-// ---- redistribution (out of scope for this build) ----------------------------
-CVTX_EXPORT int cvtx_P3D_redistribute_on_grid(const cvtx_P3D**, const int, cvtx_P3D*, int,
-	const cvtx_RedistFunc*, float, float)
-{
-	set_error("cvtx_P3D_redistribute_on_grid is not implemented in this build");
-	return 0;
-}
-CVTX_EXPORT int cvtx_P2D_redistribute_on_grid(const cvtx_P2D**, const int, cvtx_P2D*, int,
-	const cvtx_RedistFunc*, float, float)
-{
-	set_error("cvtx_P2D_redistribute_on_grid is not implemented in this build");
-	return 0;
-}
-
 // ---- GB300 extensions with host pointers --------------------------------------
 CVTX_EXPORT int cvtx_gb300_P3D_M2M_vel_dvort(const cvtx_P3D** src, int n, bsv_V3f* vel,
 	bsv_V3f* dvort, const cvtx_VortFunc* kernel, float sigma)

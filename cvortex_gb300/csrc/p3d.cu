@@ -516,7 +516,8 @@ constexpr size_t smem_bytes() {
 // scalar arithmetic). The table below is what the autotuner chooses from;
 // without a tuned entry, fewer than kSmallTargets targets use configuration 0
 // (one target per thread, so the source dimension can be split across more
-// CTAs) and larger problems use configuration 2.
+// CTAs) and larger problems the measured per-(regularisation, ops) choice of
+// kMidCfg / kLargeCfg below.
 constexpr int kSmallTargets = 8192;
 
 struct CfgSpec { int tpt, nt; bool packed; };
@@ -606,12 +607,23 @@ int env_cfg() {
 	return v;
 }
 
+// Built-in choice per (regularisation, ops) for 8,192-32,767 targets and for
+// 32,768 or more, from timings of every configuration on a GB300 (vortex
+// ring, sigma 0.05; 20,000 and 100,000 / 400,000 targets). Below 8,192
+// targets configuration 0 was fastest for every regularisation and op.
+// Index: [reg: singular, winckelmans, planetary, gaussian][ops: -, vel, dvort, both].
+constexpr signed char kMidCfg[4][4] = {
+	{2, 3, 5, 3}, {2, 3, 0, 2}, {2, 3, 5, 3}, {2, 3, 0, 0}};
+constexpr signed char kLargeCfg[4][4] = {
+	{2, 3, 5, 3}, {2, 3, 5, 2}, {2, 3, 5, 3}, {2, 3, 5, 3}};
+
 int choose_cfg(int reg, unsigned ops, int n_tgt) {
 	const int forced = env_cfg();
 	if (forced >= 0) return forced;
 	const int t = g_tuned[reg & 3][ops & 3][size_bucket(n_tgt)].load(std::memory_order_relaxed);
 	if (t >= 0 && t < kNumCfg) return t;
-	return n_tgt < kSmallTargets ? 0 : 2;
+	if (n_tgt < kSmallTargets) return 0;
+	return n_tgt < 32768 ? kMidCfg[reg & 3][ops & 3] : kLargeCfg[reg & 3][ops & 3];
 }
 
 size_t induce_ws(int reg, unsigned ops, int n_src, int n_tgt, int num_sms, int cfg) {
