@@ -104,6 +104,18 @@ __device__ __forceinline__ float rsqrt_approx(float x) {
 	return y;
 }
 
+// 2^x and 1/x from the special-function unit (a few ulp; ftz).
+__device__ __forceinline__ float ex2_approx(float x) {
+	float y;
+	asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+	return y;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+	float y;
+	asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+	return y;
+}
+
 // rsqrt with one Newton step, y (1.5 - 0.5 x y^2): about half an ulp, for
 // kernels whose per-pair weights are high powers of 1/r (errors triple in 1/r^3).
 __device__ __forceinline__ float rsqrt_refined(float x) {

@@ -6,6 +6,8 @@
 // exchange). Same CTA shape as p3d.cu; a P2D source record is one float4
 // (x, y, Gamma, area), so a 512-record tile is 8 KB.
 #include <cmath>
+#include <cstdlib>
+#include <type_traits>
 #include "nbody.h"
 #include "plan.cuh"
 #include "regfuncs.cuh"
@@ -102,6 +104,97 @@ p2d_vel_kernel(const P2DVelProblem p, const RegConsts rc, double scale,
 	}
 }
 
+// Packed velocity kernel: targets 2h and 2h+1 of a thread share one f32x2
+// lane pair (as the P3D packed kernel), 1/x from rcp + one Newton step.
+template <Reg R, int TPT, int NT>
+__global__ void __launch_bounds__(NT)
+p2d_vel2_kernel(const P2DVelProblem p, const RegConsts rc, double scale,
+	double* __restrict__ partial, int src_per_split, unsigned* err)
+{
+	static_assert(TPT % 2 == 0, "packed kernel: even TPT");
+	constexpr int NC = 2, H = TPT / 2;
+	extern __shared__ __align__(16) unsigned char smem[];
+	float* hi = reinterpret_cast<float*>(smem + Stream1::kSmemBytes);
+	float* lo = hi + NC * TPT * NT;
+	const int tid = threadIdx.x;
+	const int tbase = blockIdx.x * (TPT * NT);
+	const int s_begin = blockIdx.y * src_per_split;
+	int n_s = p.n_src - s_begin;
+	n_s = n_s < src_per_split ? n_s : src_per_split;
+	n_s = n_s > 0 ? n_s : 0;
+	float2 tx[H], ty[H];
+#pragma unroll
+	for (int h = 0; h < H; ++h) {
+		float4 q[2];
+#pragma unroll
+		for (int e = 0; e < 2; ++e) {
+			int t = tbase + (2 * h + e) * NT + tid;
+			t = t < p.n_tgt ? t : p.n_tgt - 1;
+			q[e] = p.tgt[t];
+		}
+		tx[h] = make_float2(q[0].x, q[1].x);
+		ty[h] = make_float2(q[0].y, q[1].y);
+	}
+#pragma unroll
+	for (int i = 0; i < NC * TPT; ++i) { hi[i * NT + tid] = 0.f; lo[i * NT + tid] = 0.f; }
+	auto tile_fn = [&](const float4* __restrict__ st, int cnt) {
+		float2 acc[NC][H];
+#pragma unroll
+		for (int c = 0; c < NC; ++c)
+#pragma unroll
+			for (int h = 0; h < H; ++h) acc[c][h] = make_float2(0.f, 0.f);
+		auto body = [&](int j) {
+			const float4 s = st[j];
+			const float2 nsx = bc2(-s.x), nsy = bc2(-s.y), g = bc2(s.z);
+#pragma unroll
+			for (int h = 0; h < H; ++h) {
+				const float2 dx = __fadd2_rn(tx[h], nsx);
+				const float2 dy = __fadd2_rn(ty[h], nsy);
+				const float2 r2 = __ffma2_rn(dy, dy, __fmul2_rn(dx, dx));
+				float2 hh = RegP2D2<R>::h2(r2, rc);
+				if (!HFinite<R>::value) {
+					hh.x = r2.x > 0.f ? hh.x : 0.f;
+					hh.y = r2.y > 0.f ? hh.y : 0.f;
+				}
+				const float2 hg = __fmul2_rn(hh, g);
+				acc[0][h] = __ffma2_rn(hg, dy, acc[0][h]);
+				acc[1][h] = __ffma2_rn(make_float2(-hg.x, -hg.y), dx, acc[1][h]);
+			}
+		};
+		if (cnt == kTile) {
+#pragma unroll 4
+			for (int j = 0; j < kTile; ++j) body(j);
+		} else {
+#pragma unroll 1
+			for (int j = 0; j < cnt; ++j) body(j);
+		}
+#pragma unroll
+		for (int c = 0; c < NC; ++c)
+#pragma unroll
+			for (int h = 0; h < H; ++h)
+#pragma unroll
+				for (int e = 0; e < 2; ++e) {
+					const int i = (c * TPT + 2 * h + e) * NT + tid;
+					float hv = hi[i], lv = lo[i];
+					fold_twosum(hv, lv, e == 0 ? acc[c][h].x : acc[c][h].y);
+					hi[i] = hv; lo[i] = lv;
+				}
+	};
+	if (!Stream1::run(smem, p.src, s_begin, n_s, err, tile_fn)) return;
+#pragma unroll
+	for (int k = 0; k < TPT; ++k) {
+		const int t = tbase + k * NT + tid;
+		if (t >= p.n_tgt) continue;
+#pragma unroll
+		for (int c = 0; c < NC; ++c) {
+			const int i = (c * TPT + k) * NT + tid;
+			const double sum = double(hi[i]) + double(lo[i]);
+			if (gridDim.y == 1) p.out[2 * size_t(t) + c] = float(scale * sum);
+			else partial[(size_t(blockIdx.y) * NC + c) * p.n_tgt + t] = sum;
+		}
+	}
+}
+
 // Viscous exchange: out = S * sum_s Es (Gamma_s A_t - Gamma_t A_s).
 template <Reg R, int TPT, int NT>
 __global__ void __launch_bounds__(NT)
@@ -193,10 +286,16 @@ constexpr size_t smem_bytes() {
 	return Stream1::kSmemBytes + size_t(2) * NC * TPT * NT * sizeof(float);
 }
 
-template <Reg R, int TPT, int NT>
+template <Reg R, int TPT, int NT, bool PK>
+auto vel_kernel() {
+	if constexpr (PK) return p2d_vel2_kernel<R, TPT, NT>;
+	else return p2d_vel_kernel<R, TPT, NT>;
+}
+
+template <Reg R, int TPT, int NT, bool PK>
 Plan plan_vel(int n_src, int n_tgt, int num_sms, int max_split = 64) {
 	constexpr size_t smem = smem_bytes<TPT, NT, 2>();
-	static const int occ = resident_ctas(p2d_vel_kernel<R, TPT, NT>, NT, smem);
+	static const int occ = resident_ctas(vel_kernel<R, TPT, NT, PK>(), NT, smem);
 	return make_plan(n_src, n_tgt, TPT * NT, kTile, 2, num_sms * occ, smem, max_split);
 }
 
@@ -209,15 +308,15 @@ double vel_scale(int reg, float sigma) {
 	return inv2pi;
 }
 
-template <Reg R, int TPT, int NT>
+template <Reg R, int TPT, int NT, bool PK>
 cudaError_t launch_vel(const P2DVelProblem& p, const LaunchEnv& env) {
-	const Plan pl = plan_vel<R, TPT, NT>(p.n_src, p.n_tgt, env.num_sms,
+	const Plan pl = plan_vel<R, TPT, NT, PK>(p.n_src, p.n_tgt, env.num_sms,
 		env.cap_to_ws ? split_cap_for(env.ws_bytes, 2, p.n_tgt) : 64);
 	if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
 	const RegConsts rc = make_reg_consts_host(p.sigma);
 	const double scale = vel_scale(int(R), p.sigma);
 	double* partial = static_cast<double*>(env.ws);
-	p2d_vel_kernel<R, TPT, NT><<<dim3(pl.n_tblocks, pl.n_split), NT, pl.smem, env.stream>>>(
+	vel_kernel<R, TPT, NT, PK>()<<<dim3(pl.n_tblocks, pl.n_split), NT, pl.smem, env.stream>>>(
 		p, rc, scale, partial, pl.src_per_split, env.err);
 	count_launch();
 	if (pl.n_split > 1) {
@@ -254,14 +353,48 @@ cudaError_t launch_visc(const P2DViscProblem& p, const LaunchEnv& env) {
 	return cudaGetLastError();
 }
 
+// Velocity launch configurations: 0 scalar (1 target/thread, 128 threads),
+// 1 scalar (4, 128), 2 packed (4, 128), 3 packed (2, 128), 4 packed (8, 128),
+// 5 packed (4, 256). Default from GB300 timings (Gaussian patch, 20,000 and
+// 200,000 targets): 0 below kSmallTargets targets, 3 up to 65,535, else 2;
+// CVTX_GB300_P2D_CFG forces one.
+int p2d_env_cfg() {
+	static const int v = [] {
+		const char* e = std::getenv("CVTX_GB300_P2D_CFG");
+		if (!e || !*e) return -1;
+		const int c = std::atoi(e);
+		return (c >= 0 && c <= 5) ? c : -1;
+	}();
+	return v;
+}
+int vel_cfg(int n_tgt) {
+	const int f = p2d_env_cfg();
+	if (f >= 0) return f;
+	return n_tgt < kSmallTargets ? 0 : n_tgt < 65536 ? 3 : 2;
+}
+template <Reg R, class F>
+auto with_vel_cfg(int cfg, F&& f) {
+	switch (cfg) {
+	case 0: return f(std::integral_constant<int, 1>{}, std::integral_constant<int, 128>{}, std::false_type{});
+	case 1: return f(std::integral_constant<int, 4>{}, std::integral_constant<int, 128>{}, std::false_type{});
+	case 2: return f(std::integral_constant<int, 4>{}, std::integral_constant<int, 128>{}, std::true_type{});
+	case 3: return f(std::integral_constant<int, 2>{}, std::integral_constant<int, 128>{}, std::true_type{});
+	case 4: return f(std::integral_constant<int, 8>{}, std::integral_constant<int, 128>{}, std::true_type{});
+	default: return f(std::integral_constant<int, 4>{}, std::integral_constant<int, 256>{}, std::true_type{});
+	}
+}
 template <Reg R>
 size_t ws_vel_r(int n_src, int n_tgt, int num_sms) {
-	return n_tgt < kSmallTargets ? plan_vel<R, 1, 128>(n_src, n_tgt, num_sms).ws_bytes
-	                             : plan_vel<R, 4, 128>(n_src, n_tgt, num_sms).ws_bytes;
+	return with_vel_cfg<R>(vel_cfg(n_tgt), [&](auto t, auto n, auto pk) {
+		return plan_vel<R, decltype(t)::value, decltype(n)::value, decltype(pk)::value>(
+			n_src, n_tgt, num_sms).ws_bytes;
+	});
 }
 template <Reg R>
 cudaError_t vel_r(const P2DVelProblem& p, const LaunchEnv& env) {
-	return p.n_tgt < kSmallTargets ? launch_vel<R, 1, 128>(p, env) : launch_vel<R, 4, 128>(p, env);
+	return with_vel_cfg<R>(vel_cfg(p.n_tgt), [&](auto t, auto n, auto pk) {
+		return launch_vel<R, decltype(t)::value, decltype(n)::value, decltype(pk)::value>(p, env);
+	});
 }
 template <Reg R>
 size_t ws_visc_r(int n_src, int n_tgt, int num_sms) {

@@ -613,9 +613,9 @@ int env_cfg() {
 // targets configuration 0 was fastest for every regularisation and op.
 // Index: [reg: singular, winckelmans, planetary, gaussian][ops: -, vel, dvort, both].
 constexpr signed char kMidCfg[4][4] = {
-	{2, 3, 5, 3}, {2, 3, 0, 2}, {2, 3, 5, 3}, {2, 3, 0, 0}};
+	{2, 3, 5, 3}, {2, 3, 0, 2}, {2, 3, 0, 2}, {2, 6, 5, 3}};
 constexpr signed char kLargeCfg[4][4] = {
-	{2, 3, 5, 3}, {2, 3, 5, 2}, {2, 3, 5, 3}, {2, 3, 5, 3}};
+	{2, 3, 5, 3}, {2, 3, 5, 2}, {2, 4, 2, 2}, {2, 6, 5, 3}};
 
 int choose_cfg(int reg, unsigned ops, int n_tgt) {
 	const int forced = env_cfg();

@@ -219,6 +219,83 @@ template <> struct RegP3D2<Reg::Winckelmans> {
 	}
 };
 
+// Gaussian, packed. For rho >= rho_c the reference's A&S form as in
+// RegP3D<Gaussian>, with exp(-x2/2) from ex2 and t = 1/(1 + p rho/sqrt2)
+// from rcp refined by one Newton step (both within a few ulp; the A&S
+// formula's own error, 1.5e-7 in erf, is larger). The series branch runs only
+// when some lane of the warp has a pair below rho_c (a warp vote), and then
+// for both halves with a per-element select, so warps never diverge.
+template <> struct RegP3D2<Reg::Gaussian> {
+	static constexpr float kNegHalfLog2e = -0.72134752044448170f;   // -log2(e)/2
+	__device__ __forceinline__ static float2 neg(float2 a) { return make_float2(-a.x, -a.y); }
+	// A&S branch: G (and K when want_k) for both halves of x2
+	template <bool WANT_K>
+	__device__ __forceinline__ static void as2(float2 x2, float2& G, float2& K) {
+		const float a1 = 0.254829592f, a2 = -0.284496736f, a3 = 1.421413741f;
+		const float a4 = -1.453152027f, a5 = 1.061405429f, p = 0.3275911f;
+		const float2 s = make_float2(rsqrt_approx(x2.x), rsqrt_approx(x2.y));   // 1/rho
+		const float2 s2 = __fmul2_rn(s, s);
+		const float2 rho = __fmul2_rn(x2, s);
+		const float2 ea = __fmul2_rn(x2, bc2(kNegHalfLog2e));
+		const float2 e = make_float2(ex2_approx(ea.x), ex2_approx(ea.y));
+		const float2 u = __ffma2_rn(rho, bc2(p * kRecipSqrt2), bc2(1.f));
+		float2 t = make_float2(rcp_approx(u.x), rcp_approx(u.y));
+		t = __fmul2_rn(t, __ffma2_rn(neg(u), t, bc2(2.f)));
+		float2 q = __ffma2_rn(t, bc2(a5), bc2(a4));
+		q = __ffma2_rn(t, q, bc2(a3));
+		q = __ffma2_rn(t, q, bc2(a2));
+		q = __ffma2_rn(t, q, bc2(a1));
+		const float2 poly = __fmul2_rn(t, q);
+		float2 g = __ffma2_rn(neg(poly), e, bc2(1.f));
+		g = __ffma2_rn(neg(__fmul2_rn(rho, bc2(kSqrt2OverPi))), e, g);
+		g.x = rho.x > 6.f ? 1.f : g.x;
+		g.y = rho.y > 6.f ? 1.f : g.y;
+		G = __fmul2_rn(g, __fmul2_rn(s2, s));
+		if (WANT_K)
+			K = __fmul2_rn(__ffma2_rn(bc2(3.f), G, __fmul2_rn(bc2(-kSqrt2OverPi), e)), s2);
+	}
+	__device__ __forceinline__ static float2 seriesG(float2 x) {
+		float2 q = __ffma2_rn(x, bc2(1.f / 691200.f), bc2(-1.f / 49920.f));
+		q = __ffma2_rn(q, x, bc2(1.f / 4224.f));
+		q = __ffma2_rn(q, x, bc2(-1.f / 432.f));
+		q = __ffma2_rn(q, x, bc2(1.f / 56.f));
+		q = __ffma2_rn(q, x, bc2(-1.f / 10.f));
+		q = __ffma2_rn(q, x, bc2(1.f / 3.f));
+		return __fmul2_rn(bc2(kSqrt2OverPi), q);
+	}
+	__device__ __forceinline__ static float2 seriesK(float2 x) {
+		float2 q = __ffma2_rn(x, bc2(1.f / 783360.f), bc2(-1.f / 57600.f));
+		q = __ffma2_rn(q, x, bc2(1.f / 4992.f));
+		q = __ffma2_rn(q, x, bc2(-1.f / 528.f));
+		q = __ffma2_rn(q, x, bc2(1.f / 72.f));
+		q = __ffma2_rn(q, x, bc2(-1.f / 14.f));
+		q = __ffma2_rn(q, x, bc2(1.f / 5.f));
+		return __fmul2_rn(bc2(kSqrt2OverPi), q);
+	}
+	__device__ __forceinline__ static void gk2(float2 r2, const RegConsts& c, float2& G, float2& K) {
+		const float2 x2 = __fmul2_rn(r2, bc2(c.inv_s2));
+		const bool sx = x2.x < c.rho_c2, sy = x2.y < c.rho_c2;
+		as2<true>(x2, G, K);
+		if (__any_sync(0xffffffffu, sx || sy)) {
+			const float2 gs = seriesG(x2), ks = seriesK(x2);
+			if (sx) { G.x = gs.x; K.x = ks.x; }
+			if (sy) { G.y = gs.y; K.y = ks.y; }
+		}
+	}
+	__device__ __forceinline__ static float2 g2(float2 r2, const RegConsts& c) {
+		const float2 x2 = __fmul2_rn(r2, bc2(c.inv_s2));
+		const bool sx = x2.x < c.rho_c2, sy = x2.y < c.rho_c2;
+		float2 G, K;
+		as2<false>(x2, G, K);
+		if (__any_sync(0xffffffffu, sx || sy)) {
+			const float2 gs = seriesG(x2);
+			if (sx) G.x = gs.x;
+			if (sy) G.y = gs.y;
+		}
+		return G;
+	}
+};
+
 // ---- 2D ------------------------------------------------------------------
 template <Reg R> struct RegP2D;
 
@@ -269,6 +346,54 @@ template <> struct RegP2D<Reg::Gaussian> {
 	}
 	__device__ __forceinline__ static float eta(float r2, const RegConsts& c) {
 		return exp2f(r2 * c.exp2_half);
+	}
+};
+
+// ---- 2D, packed (two targets per f32x2 lane pair) ----------------------------
+// 1/x from rcp refined by one Newton step, t (2 - x t): within an ulp.
+__device__ __forceinline__ float2 rcp2(float2 x) {
+	float2 t = make_float2(rcp_approx(x.x), rcp_approx(x.y));
+	return __fmul2_rn(t, __ffma2_rn(make_float2(-x.x, -x.y), t, bc2(2.f)));
+}
+
+template <Reg R> struct RegP2D2;
+template <> struct RegP2D2<Reg::Singular> {
+	__device__ __forceinline__ static float2 h2(float2 r2, const RegConsts&) { return rcp2(r2); }
+};
+template <> struct RegP2D2<Reg::Winckelmans> {
+	__device__ __forceinline__ static float2 h2(float2 r2, const RegConsts& c) {
+		const float2 q = __ffma2_rn(r2, bc2(c.inv_s2), bc2(1.f));
+		const float2 rq = rcp2(q);
+		return __fmul2_rn(__fadd2_rn(q, bc2(1.f)), __fmul2_rn(rq, rq));
+	}
+};
+template <> struct RegP2D2<Reg::Planetary> {
+	__device__ __forceinline__ static float2 h2(float2 r2, const RegConsts& c) {
+		const float2 o = rcp2(r2);
+		return make_float2(r2.x < c.s2 ? c.inv_s2 : o.x, r2.y < c.s2 ? c.inv_s2 : o.y);
+	}
+};
+template <> struct RegP2D2<Reg::Gaussian> {
+	// (1 - exp(-y)) / x2, y = x2/2; the series of RegP2D<Gaussian> below
+	// y = 0.1, evaluated when some lane of the warp needs it (warp vote)
+	__device__ __forceinline__ static float2 h2(float2 r2, const RegConsts& c) {
+		const float2 x2 = __fmul2_rn(r2, bc2(c.inv_s2));
+		const float2 ny = __fmul2_rn(x2, bc2(-0.72134752044448170f));   // -y log2(e)
+		const float2 e = make_float2(ex2_approx(ny.x), ex2_approx(ny.y));
+		float2 h = __fmul2_rn(__fadd2_rn(bc2(1.f), make_float2(-e.x, -e.y)), rcp2(x2));
+		const float2 y = __fmul2_rn(bc2(0.5f), x2);
+		const bool sx = y.x < 0.1f, sy = y.y < 0.1f;
+		if (__any_sync(0xffffffffu, sx || sy)) {
+			float2 p = __ffma2_rn(y, bc2(-1.f / 720.f), bc2(1.f / 120.f));
+			p = __ffma2_rn(p, y, bc2(-1.f / 24.f));
+			p = __ffma2_rn(p, y, bc2(1.f / 6.f));
+			p = __ffma2_rn(p, y, bc2(-0.5f));
+			p = __ffma2_rn(p, y, bc2(1.f));
+			p = __fmul2_rn(bc2(0.5f), p);
+			if (sx) h.x = p.x;
+			if (sy) h.y = p.y;
+		}
+		return h;
 	}
 };
 

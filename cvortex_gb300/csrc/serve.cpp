@@ -6,8 +6,8 @@
 // kinds and sizes arrive from any thread and share one GPU:
 //
 //  * Admission. A scheduler thread takes requests in arrival order. A request
-//    needs one slot (a high- and a low-priority CUDA stream, a fixed split-sum
-//    workspace and an error word) and one range of the device arena, a single
+//    needs one slot (CUDA streams, a fixed split-sum workspace and an error
+//    word) and one range of the device arena, a single
 //    allocation made at start-up whose size is the HBM budget. While no slot
 //    or no arena range is free the queue waits; it resumes as running
 //    requests complete. A request larger than the whole budget is rejected.
@@ -15,9 +15,12 @@
 //    the device for all of its time steps (all-pairs M2M, then a forward-Euler
 //    update) and downloaded once.
 //  * Overlap. Every slot runs on its own streams, so requests admitted while
-//    others are on the GPU run beside them; small requests go on the
-//    high-priority stream, so the block scheduler serves their CTAs ahead of
-//    the waves of a large request.
+//    others are on the GPU run beside them. A slot has one stream per CUDA
+//    stream priority level, and a request runs at a priority set by its
+//    work per step (smaller = higher), so the block scheduler serves the CTAs
+//    of small requests ahead of the waves of large ones. (More streams than
+//    hardware queues alias onto shared queues: serving processes should set
+//    CUDA_DEVICE_MAX_CONNECTIONS=32 before CUDA starts.)
 //  * Determinism. A launch's source partition and reduction order depend only
 //    on its problem size and the slot workspace size (equal for all slots),
 //    never on what else is in flight, so a result is bit-identical alone and
@@ -58,7 +61,7 @@ constexpr size_t kAlign = 256;
 constexpr size_t kSlotWsBytes = size_t(64) << 20;        // split partials per slot
 constexpr size_t kStagingBytes = size_t(1) << 30;        // pinned staging arena
 constexpr size_t kDefaultMaxHbm = size_t(64) << 30;
-constexpr double kSmallPairs = double(1 << 30);           // high-priority below this
+constexpr int kMaxLevels = 8;                              // stream priority levels used
 inline size_t up(size_t b) { return (b + kAlign - 1) & ~(kAlign - 1); }
 
 // First-fit range allocator over [0, cap) with coalescing of free ranges.
@@ -187,7 +190,7 @@ class Server;
 struct Slot {
 	Server* srv = nullptr;
 	int index = 0;
-	cudaStream_t hi = nullptr, lo = nullptr;
+	cudaStream_t st[kMaxLevels] = {};   // one stream per priority level, highest first
 	void* ws = nullptr;
 	unsigned* d_err = nullptr;
 	unsigned* h_err = nullptr;      // pinned
@@ -231,7 +234,18 @@ class Server {
 		return !queue_.empty() && !free_slots_.empty() && !mem_blocked_;
 	}
 
+	// Priority level of a request: the highest for under 2^24 pairs per step,
+	// one level lower for every further factor of 16 (shortest work first at
+	// the block scheduler, without reordering the admission queue).
+	int level_of(double pairs_per_step) const {
+		int l = 0;
+		double lim = double(1 << 24);
+		while (l + 1 < levels_ && pairs_per_step >= lim) { ++l; lim *= 16.0; }
+		return l;
+	}
+
 	bool dry_ = false;
+	int levels_ = 1;
 	int device_ = 0, num_sms_ = 1;
 	void* d_arena_ = nullptr;
 	unsigned char* h_stage_ = nullptr;
@@ -266,7 +280,7 @@ void CUDART_CB on_slot_done(void* p) {
 
 bool Server::open(int n_slots, size_t hbm, bool dry, std::string* why) {
 	dry_ = dry;
-	if (n_slots <= 0) n_slots = 16;
+	if (n_slots <= 0) n_slots = 64;
 	if (n_slots > 256) n_slots = 256;
 	slots_.resize(size_t(n_slots));
 	if (!dry_) {
@@ -291,10 +305,13 @@ bool Server::open(int n_slots, size_t hbm, bool dry, std::string* why) {
 			cudaHostAllocDefault);
 		int lo_pri = 0, hi_pri = 0;
 		if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&lo_pri, &hi_pri);
+		// numerically lower = higher priority; hi_pri <= lo_pri
+		levels_ = std::min(kMaxLevels, lo_pri - hi_pri + 1);
+		if (levels_ < 1) levels_ = 1;
 		for (int i = 0; e == cudaSuccess && i < n_slots; ++i) {
 			Slot& s = slots_[size_t(i)];
-			e = cudaStreamCreateWithPriority(&s.hi, cudaStreamNonBlocking, hi_pri);
-			if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s.lo, cudaStreamNonBlocking, lo_pri);
+			for (int l = 0; e == cudaSuccess && l < levels_; ++l)
+				e = cudaStreamCreateWithPriority(&s.st[l], cudaStreamNonBlocking, hi_pri + l);
 			if (e == cudaSuccess) e = cudaMalloc(&s.ws, kSlotWsBytes);
 			if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&s.d_err), sizeof(unsigned));
 			if (e == cudaSuccess) e = cudaHostAlloc(reinterpret_cast<void**>(&s.h_err), sizeof(unsigned),
@@ -328,10 +345,11 @@ void Server::shutdown() {
 	}
 	if (!dry_) {
 		for (Slot& s : slots_) {
-			if (s.hi) cudaStreamSynchronize(s.hi);
-			if (s.lo) cudaStreamSynchronize(s.lo);
-			if (s.hi) cudaStreamDestroy(s.hi);
-			if (s.lo) cudaStreamDestroy(s.lo);
+			for (cudaStream_t q : s.st)
+				if (q) {
+					cudaStreamSynchronize(q);
+					cudaStreamDestroy(q);
+				}
 			if (s.ws) cudaFree(s.ws);
 			if (s.d_err) cudaFree(s.d_err);
 			if (s.h_err) cudaFreeHost(s.h_err);
@@ -457,8 +475,8 @@ void Server::admit(std::unique_lock<std::mutex>& lk) {
 		lk.unlock();
 		sl.launch_error = launch(q, sl);
 		if (sl.launch_error != cudaSuccess) {
-			cudaStreamSynchronize(sl.hi);
-			cudaStreamSynchronize(sl.lo);
+			for (cudaStream_t q : sl.st)
+				if (q) cudaStreamSynchronize(q);
 			cudaGetLastError();
 		}
 		lk.lock();
@@ -469,7 +487,7 @@ void Server::admit(std::unique_lock<std::mutex>& lk) {
 cudaError_t Server::launch(Request& q, Slot& sl) {
 	const cvtx_gb300_request& r = q.r;
 	const Layout& L = q.L;
-	cudaStream_t st = pairs_of(r) / r.n_steps < kSmallPairs ? sl.hi : sl.lo;
+	cudaStream_t st = sl.st[level_of(pairs_of(r) / r.n_steps)];
 	unsigned char* base = static_cast<unsigned char*>(d_arena_) + q.dev_off;
 	float4* state = reinterpret_cast<float4*>(base + L.state);
 	float4* tgt = reinterpret_cast<float4*>(base + L.tgt);

@@ -144,8 +144,11 @@ CVTX_EXPORT int cvtx_gb300_dev_P3D_step(void* rec, int n, float* vel, float* dvo
 /* ---- serving loop: continuous batching of M2M requests ------------------
  * Requests arrive from any thread (cvtx_gb300_server_submit). A scheduler
  * thread admits them in arrival order as slots and device memory free up:
- * each admitted request takes one slot (a CUDA stream pair and a fixed
- * workspace) and a range of one device arena sized by the HBM budget; a
+ * each admitted request takes one slot (CUDA streams at every priority level
+ * and a fixed workspace) and a range of one device arena sized by the HBM
+ * budget, and runs at a stream priority set by its work per step (smaller
+ * runs first on the GPU; set CUDA_DEVICE_MAX_CONNECTIONS=32 before CUDA
+ * starts so that the many streams do not share few hardware queues); a
  * request that could never fit the budget is rejected. Its state is copied in
  * once, stays resident for all n_steps time steps (M2M + Euler update on the
  * device), and is copied out once; requests on different slots overlap on the
@@ -198,7 +201,7 @@ typedef struct {
 	unsigned long long kernel_launches;
 } cvtx_gb300_server_stats;
 typedef struct cvtx_gb300_server cvtx_gb300_server;
-/* n_slots: concurrent requests (0 = 16). hbm_bytes: arena size (0 = half of
+/* n_slots: concurrent requests (0 = 64). hbm_bytes: arena size (0 = half of
  * the free device memory, at most 64 GiB). flags: CVTX_GB300_SERVER_DRY_RUN
  * runs the scheduler without a GPU (requests complete at admission without
  * computing; for testing admission logic). */
