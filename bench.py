@@ -413,7 +413,29 @@ def extras(cv, lib, args, torch, sh, peak):
     f = lambda: lib.cvtx_gb300_dev_P2D_M2M_vel(rq.data_ptr(), len(q), rq.data_ptr(), len(q),
                                                o.data_ptr(), 3, SIGMA, sh)
     ms = timed_dev(f, torch, 5)
-    res["p2d_patch200k_gaussian_vel"] = {"ginter_s": len(q) ** 2 / ms / 1e6}
+    res["p2d_patch200k_gaussian_vel"] = {"ginter_s": len(q) ** 2 / ms / 1e6,
+                                         "fp32_frac": 13 * len(q) ** 2 / (ms * 1e-3) / 1e12 / peak}
+    f = lambda: lib.cvtx_gb300_dev_P2D_M2M_vel(rq.data_ptr(), len(q), rq.data_ptr(), len(q),
+                                               o.data_ptr(), 1, SIGMA, sh)
+    ms = timed_dev(f, torch, 5)
+    res["p2d_patch200k_winckelmans_vel"] = {"ginter_s": len(q) ** 2 / ms / 1e6,
+                                            "fp32_frac": 15 * len(q) ** 2 / (ms * 1e-3) / 1e12 / peak}
+    nf = 100_000
+    fil = workloads.wake_sheet(nf)
+    pts = workloads.sheet_targets(nf)
+    rf = np.zeros((nf, 8), np.float32)
+    rf[:, 0:3] = fil["start"]
+    rf[:, 3] = fil["strength"]
+    rf[:, 4:7] = fil["end"]
+    tf = np.zeros((nf, 4), np.float32)
+    tf[:, 0:3] = pts
+    rfd, tfd = torch.from_numpy(rf).cuda(), torch.from_numpy(tf).cuda()
+    of = torch.empty((nf, 3), dtype=torch.float32, device="cuda")
+    f = lambda: lib.cvtx_gb300_dev_F3D_M2M_vel(rfd.data_ptr(), nf, tfd.data_ptr(), 1, nf,
+                                               of.data_ptr(), sh)
+    ms = timed_dev(f, torch, 5)
+    res["f3d_sheet100k_vel"] = {"ginter_s": nf * nf / ms / 1e6,
+                                "fp32_frac": 51 * nf * nf / (ms * 1e-3) / 1e12 / peak}
     res["batch512"] = batch_extra(cv, lib, torch, sh)
     res["redistribute_ring200k_m4p"] = redistribute_extra(cv, lib)
     m = 1_000_000

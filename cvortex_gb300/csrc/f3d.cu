@@ -8,6 +8,8 @@
 // stretching term when it contains NaN. For stretching the 1/(4 pi) factor is
 // applied once per target.
 #include <cmath>
+#include <cstdlib>
+#include <type_traits>
 #include "nbody.h"
 #include "plan.cuh"
 #include "regfuncs.cuh"
@@ -107,6 +109,129 @@ f3d_vel_kernel(const F3DVelProblem p, double* __restrict__ partial, int src_per_
 				fold_twosum(h, l, acc[c][k]);
 				hi[i] = h; lo[i] = l;
 			}
+	};
+	if (!Stream2::run(smem, p.fil, s_begin, n_s, err, tile_fn)) return;
+#pragma unroll
+	for (int k = 0; k < TPT; ++k) {
+		const int t = tbase + k * NT + tid;
+		if (t >= p.n_tgt) continue;
+#pragma unroll
+		for (int c = 0; c < NC; ++c) {
+			const int i = (c * TPT + k) * NT + tid;
+			const double s = double(hi[i]) + double(lo[i]);
+			if (gridDim.y == 1) p.out[3 * size_t(t) + c] = float(s);
+			else partial[(size_t(blockIdx.y) * NC + c) * p.n_tgt + t] = s;
+		}
+	}
+}
+
+__device__ __forceinline__ float2 neg2f(float2 a) { return make_float2(-a.x, -a.y); }
+
+// f3d_vel_pair for two measurement points at once (f32x2), with the
+// division by |r1 x r2|^2 done as a reciprocal refined by one Newton step;
+// same guards.
+__device__ __forceinline__ void f3d_vel_pair2(float2 mx, float2 my, float2 mz,
+	const float4 a, const float4 b, float2& vx, float2& vy, float2& vz)
+{
+	const float2 r1x = __fadd2_rn(mx, bc2(-a.x)), r1y = __fadd2_rn(my, bc2(-a.y));
+	const float2 r1z = __fadd2_rn(mz, bc2(-a.z));
+	const float2 r2x = __fadd2_rn(mx, bc2(-b.x)), r2y = __fadd2_rn(my, bc2(-b.y));
+	const float2 r2z = __fadd2_rn(mz, bc2(-b.z));
+	const float2 r0x = __fadd2_rn(r1x, neg2f(r2x)), r0y = __fadd2_rn(r1y, neg2f(r2y));
+	const float2 r0z = __fadd2_rn(r1z, neg2f(r2z));
+	const float2 cx = __ffma2_rn(r1y, r2z, neg2f(__fmul2_rn(r1z, r2y)));
+	const float2 cy = __ffma2_rn(r1z, r2x, neg2f(__fmul2_rn(r1x, r2z)));
+	const float2 cz = __ffma2_rn(r1x, r2y, neg2f(__fmul2_rn(r1y, r2x)));
+	const float2 cc = __ffma2_rn(cz, cz, __ffma2_rn(cy, cy, __fmul2_rn(cx, cx)));
+	const float2 t1 = __fmul2_rn(bc2(a.w * kInv4PiF), rcp2(cc));
+	const float2 q1 = __ffma2_rn(r1z, r1z, __ffma2_rn(r1y, r1y, __fmul2_rn(r1x, r1x)));
+	const float2 q2 = __ffma2_rn(r2z, r2z, __ffma2_rn(r2y, r2y, __fmul2_rn(r2x, r2x)));
+	const float2 l1 = make_float2(rsqrt_approx(q1.x), rsqrt_approx(q1.y));
+	const float2 l2 = make_float2(rsqrt_approx(q2.x), rsqrt_approx(q2.y));
+	const float2 t21 = __fmul2_rn(__ffma2_rn(r1z, r0z, __ffma2_rn(r1y, r0y, __fmul2_rn(r1x, r0x))), l1);
+	const float2 t22 = __fmul2_rn(__ffma2_rn(r2z, r0z, __ffma2_rn(r2y, r0y, __fmul2_rn(r2x, r0x))), l2);
+	const float2 t2 = __fadd2_rn(t21, neg2f(t22));
+	const bool okx = fabsf(t1.x) <= kBig && fabsf(t2.x) <= kBig;
+	const bool oky = fabsf(t1.y) <= kBig && fabsf(t2.y) <= kBig;
+	float2 f = __fmul2_rn(t1, t2);
+	f.x = okx ? f.x : 0.f;
+	f.y = oky ? f.y : 0.f;
+	vx = __fmul2_rn(cx, f);
+	vy = __fmul2_rn(cy, f);
+	vz = __fmul2_rn(cz, f);
+	// a dropped term is exactly zero even where c is not finite
+	if (!okx) { vx.x = 0.f; vy.x = 0.f; vz.x = 0.f; }
+	if (!oky) { vx.y = 0.f; vy.y = 0.f; vz.y = 0.f; }
+}
+
+template <int TPT, int NT>
+__global__ void __launch_bounds__(NT)
+f3d_vel2_kernel(const F3DVelProblem p, double* __restrict__ partial, int src_per_split,
+	unsigned* err)
+{
+	static_assert(TPT % 2 == 0, "packed kernel: even TPT");
+	constexpr int NC = 3, H = TPT / 2;
+	extern __shared__ __align__(16) unsigned char smem[];
+	float* hi = reinterpret_cast<float*>(smem + Stream2::kSmemBytes);
+	float* lo = hi + NC * TPT * NT;
+	const int tid = threadIdx.x;
+	const int tbase = blockIdx.x * (TPT * NT);
+	const int s_begin = blockIdx.y * src_per_split;
+	int n_s = p.n_fil - s_begin;
+	n_s = n_s < src_per_split ? n_s : src_per_split;
+	n_s = n_s > 0 ? n_s : 0;
+	float2 tx[H], ty[H], tz[H];
+#pragma unroll
+	for (int h = 0; h < H; ++h) {
+		float4 q[2];
+#pragma unroll
+		for (int e = 0; e < 2; ++e) {
+			int t = tbase + (2 * h + e) * NT + tid;
+			t = t < p.n_tgt ? t : p.n_tgt - 1;
+			q[e] = p.tgt[size_t(t) * p.tstride];
+		}
+		tx[h] = make_float2(q[0].x, q[1].x);
+		ty[h] = make_float2(q[0].y, q[1].y);
+		tz[h] = make_float2(q[0].z, q[1].z);
+	}
+#pragma unroll
+	for (int i = 0; i < NC * TPT; ++i) { hi[i * NT + tid] = 0.f; lo[i * NT + tid] = 0.f; }
+	auto tile_fn = [&](const float4* __restrict__ st, int cnt) {
+		float2 acc[NC][H];
+#pragma unroll
+		for (int c = 0; c < NC; ++c)
+#pragma unroll
+			for (int h = 0; h < H; ++h) acc[c][h] = make_float2(0.f, 0.f);
+		auto body = [&](int j) {
+			const float4 a = st[2 * j];
+			const float4 b = st[2 * j + 1];
+#pragma unroll
+			for (int h = 0; h < H; ++h) {
+				float2 vx, vy, vz;
+				f3d_vel_pair2(tx[h], ty[h], tz[h], a, b, vx, vy, vz);
+				acc[0][h] = __fadd2_rn(acc[0][h], vx);
+				acc[1][h] = __fadd2_rn(acc[1][h], vy);
+				acc[2][h] = __fadd2_rn(acc[2][h], vz);
+			}
+		};
+		if (cnt == kTile) {
+#pragma unroll 2
+			for (int j = 0; j < kTile; ++j) body(j);
+		} else {
+#pragma unroll 1
+			for (int j = 0; j < cnt; ++j) body(j);
+		}
+#pragma unroll
+		for (int c = 0; c < NC; ++c)
+#pragma unroll
+			for (int h = 0; h < H; ++h)
+#pragma unroll
+				for (int e = 0; e < 2; ++e) {
+					const int i = (c * TPT + 2 * h + e) * NT + tid;
+					float hv = hi[i], lv = lo[i];
+					fold_twosum(hv, lv, e == 0 ? acc[c][h].x : acc[c][h].y);
+					hi[i] = hv; lo[i] = lv;
+				}
 	};
 	if (!Stream2::run(smem, p.fil, s_begin, n_s, err, tile_fn)) return;
 #pragma unroll
@@ -292,10 +417,16 @@ constexpr size_t smem_bytes() {
 	return Stream2::kSmemBytes + size_t(2) * 3 * TPT * NT * sizeof(float);
 }
 
-template <int TPT, int NT>
+template <int TPT, int NT, bool PK>
+auto vel_kernel() {
+	if constexpr (PK) return f3d_vel2_kernel<TPT, NT>;
+	else return f3d_vel_kernel<TPT, NT>;
+}
+
+template <int TPT, int NT, bool PK>
 Plan plan_vel(int n_fil, int n_tgt, int num_sms, int max_split = 64) {
 	constexpr size_t smem = smem_bytes<TPT, NT>();
-	static const int occ = resident_ctas(f3d_vel_kernel<TPT, NT>, NT, smem);
+	static const int occ = resident_ctas(vel_kernel<TPT, NT, PK>(), NT, smem);
 	return make_plan(n_fil, n_tgt, TPT * NT, kTile, 3, num_sms * occ, smem, max_split);
 }
 template <int TPT, int NT>
@@ -305,13 +436,13 @@ Plan plan_dvort(int n_fil, int n_tgt, int num_sms, int max_split = 64) {
 	return make_plan(n_fil, n_tgt, TPT * NT, kTile, 3, num_sms * occ, smem, max_split);
 }
 
-template <int TPT, int NT>
+template <int TPT, int NT, bool PK>
 cudaError_t launch_vel(const F3DVelProblem& p, const LaunchEnv& env) {
-	const Plan pl = plan_vel<TPT, NT>(p.n_fil, p.n_tgt, env.num_sms,
+	const Plan pl = plan_vel<TPT, NT, PK>(p.n_fil, p.n_tgt, env.num_sms,
 		env.cap_to_ws ? split_cap_for(env.ws_bytes, 3, p.n_tgt) : 64);
 	if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
 	double* partial = static_cast<double*>(env.ws);
-	f3d_vel_kernel<TPT, NT><<<dim3(pl.n_tblocks, pl.n_split), NT, pl.smem, env.stream>>>(
+	vel_kernel<TPT, NT, PK>()<<<dim3(pl.n_tblocks, pl.n_split), NT, pl.smem, env.stream>>>(
 		p, partial, pl.src_per_split, env.err);
 	count_launch();
 	if (pl.n_split > 1) {
@@ -338,14 +469,43 @@ cudaError_t launch_dvort(const F3DDvortProblem& p, const LaunchEnv& env) {
 
 }  // namespace
 
+// Velocity launch configurations: 0 scalar (1 target/thread, 128 threads),
+// 1 scalar (4, 128), 2 packed (4, 128), 3 packed (2, 128), 4 packed (2, 256).
+// Default from GB300 timings (wake sheet, 20,000 and 100,000 points): 0 below
+// kSmallTargets targets, else 4; CVTX_GB300_F3D_CFG forces one.
+int f3d_vel_cfg(int n_tgt) {
+	static const int forced = [] {
+		const char* e = std::getenv("CVTX_GB300_F3D_CFG");
+		if (!e || !*e) return -1;
+		const int c = std::atoi(e);
+		return (c >= 0 && c <= 4) ? c : -1;
+	}();
+	if (forced >= 0) return forced;
+	return n_tgt < kSmallTargets ? 0 : 4;
+}
+template <class F>
+auto with_vel_cfg(int cfg, F&& f) {
+	switch (cfg) {
+	case 0: return f(std::integral_constant<int, 1>{}, std::integral_constant<int, 128>{}, std::false_type{});
+	case 1: return f(std::integral_constant<int, 4>{}, std::integral_constant<int, 128>{}, std::false_type{});
+	case 2: return f(std::integral_constant<int, 4>{}, std::integral_constant<int, 128>{}, std::true_type{});
+	case 3: return f(std::integral_constant<int, 2>{}, std::integral_constant<int, 128>{}, std::true_type{});
+	default: return f(std::integral_constant<int, 2>{}, std::integral_constant<int, 256>{}, std::true_type{});
+	}
+}
+
 size_t f3d_vel_ws_bytes(int n_fil, int n_tgt, int num_sms) {
 	if (n_tgt <= 0) return 0;
-	return n_tgt < kSmallTargets ? plan_vel<1, 128>(n_fil, n_tgt, num_sms).ws_bytes
-	                             : plan_vel<4, 128>(n_fil, n_tgt, num_sms).ws_bytes;
+	return with_vel_cfg(f3d_vel_cfg(n_tgt), [&](auto t, auto n, auto pk) {
+		return plan_vel<decltype(t)::value, decltype(n)::value, decltype(pk)::value>(
+			n_fil, n_tgt, num_sms).ws_bytes;
+	});
 }
 cudaError_t f3d_vel(const F3DVelProblem& p, const LaunchEnv& env) {
 	if (p.n_tgt <= 0) return cudaSuccess;
-	return p.n_tgt < kSmallTargets ? launch_vel<1, 128>(p, env) : launch_vel<4, 128>(p, env);
+	return with_vel_cfg(f3d_vel_cfg(p.n_tgt), [&](auto t, auto n, auto pk) {
+		return launch_vel<decltype(t)::value, decltype(n)::value, decltype(pk)::value>(p, env);
+	});
 }
 size_t f3d_dvort_ws_bytes(int n_fil, int n_tgt, int num_sms) {
 	if (n_tgt <= 0) return 0;
