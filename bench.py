@@ -404,7 +404,9 @@ def extras(cv, lib, args, torch, sh, peak):
         if r in (1, 3):
             f = lambda: lib.cvtx_gb300_dev_P3D_M2M_visc(rec.data_ptr(), n, rec.data_ptr(), 2, n,
                                                         o1.data_ptr(), r, SIGMA, 1e-3, sh)
-            row["visc"] = {"ginter_s": n * n / timed_dev(f, torch, 5) / 1e6}
+            ms = timed_dev(f, torch, 5)
+            row["visc"] = {"ginter_s": n * n / ms / 1e6,
+                           "fp32_frac": (22 if r == 1 else 17) * n * n / (ms * 1e-3) / 1e12 / peak}
         res[f"ring{n}_{rname}"] = row
     q = workloads.gaussian_patch_2d(200_000)
     rq = torch.from_numpy(np.ascontiguousarray(

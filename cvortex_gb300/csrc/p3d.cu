@@ -385,6 +385,103 @@ p3d_visc_kernel(const P3DViscProblem p, const ViscConsts vc,
 	}
 }
 
+// Packed variant (two targets per f32x2 lane pair).
+template <Reg R, int TPT, int NT>
+__global__ void __launch_bounds__(NT)
+p3d_visc2_kernel(const P3DViscProblem p, const ViscConsts vc,
+	double* __restrict__ partial, int src_per_split, unsigned* err)
+{
+	static_assert(TPT % 2 == 0, "packed kernel: even TPT");
+	constexpr int NC = 3, H = TPT / 2;
+	extern __shared__ __align__(16) unsigned char smem[];
+	float* hi = reinterpret_cast<float*>(smem + Stream2::kSmemBytes);
+	float* lo = hi + NC * TPT * NT;
+	const int tid = threadIdx.x;
+	const int tbase = blockIdx.x * (TPT * NT);
+	const int s_begin = blockIdx.y * src_per_split;
+	int n_s = p.n_src - s_begin;
+	n_s = n_s < src_per_split ? n_s : src_per_split;
+	n_s = n_s > 0 ? n_s : 0;
+	float2 tx[H], ty[H], tz[H], tv[H], nax[H], nay[H], naz[H];
+#pragma unroll
+	for (int h = 0; h < H; ++h) {
+		float4 q[2], w[2];
+#pragma unroll
+		for (int e = 0; e < 2; ++e) {
+			int t = tbase + (2 * h + e) * NT + tid;
+			t = t < p.n_tgt ? t : p.n_tgt - 1;
+			q[e] = p.tgt[size_t(t) * p.tstride];
+			w[e] = p.tgt[size_t(t) * p.tstride + 1];
+		}
+		tx[h] = make_float2(q[0].x, q[1].x); ty[h] = make_float2(q[0].y, q[1].y);
+		tz[h] = make_float2(q[0].z, q[1].z); tv[h] = make_float2(q[0].w, q[1].w);
+		nax[h] = make_float2(-w[0].x, -w[1].x); nay[h] = make_float2(-w[0].y, -w[1].y);
+		naz[h] = make_float2(-w[0].z, -w[1].z);
+	}
+#pragma unroll
+	for (int i = 0; i < NC * TPT; ++i) { hi[i * NT + tid] = 0.f; lo[i * NT + tid] = 0.f; }
+	auto tile_fn = [&](const float4* __restrict__ st, int cnt) {
+		float2 acc[NC][H];
+#pragma unroll
+		for (int c = 0; c < NC; ++c)
+#pragma unroll
+			for (int h = 0; h < H; ++h) acc[c][h] = make_float2(0.f, 0.f);
+		auto body = [&](int j) {
+			const float4 sp = st[2 * j];
+			const float4 sv = st[2 * j + 1];
+			const float2 sx = bc2(sp.x), sy = bc2(sp.y), sz = bc2(sp.z), vs = bc2(sp.w);
+#pragma unroll
+			for (int h = 0; h < H; ++h) {
+				const float2 dx = __fadd2_rn(sx, make_float2(-tx[h].x, -tx[h].y));
+				const float2 dy = __fadd2_rn(sy, make_float2(-ty[h].x, -ty[h].y));
+				const float2 dz = __fadd2_rn(sz, make_float2(-tz[h].x, -tz[h].y));
+				const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+				float2 e = RegEta2<R>::eta2(r2, vc.rc);
+				e.x = r2.x > 0.f ? e.x : 0.f;
+				e.y = r2.y > 0.f ? e.y : 0.f;
+				// alpha_s V_t - alpha_t V_s
+				const float2 wx = __ffma2_rn(bc2(sv.x), tv[h], __fmul2_rn(nax[h], vs));
+				const float2 wy = __ffma2_rn(bc2(sv.y), tv[h], __fmul2_rn(nay[h], vs));
+				const float2 wz = __ffma2_rn(bc2(sv.z), tv[h], __fmul2_rn(naz[h], vs));
+				acc[0][h] = __ffma2_rn(e, wx, acc[0][h]);
+				acc[1][h] = __ffma2_rn(e, wy, acc[1][h]);
+				acc[2][h] = __ffma2_rn(e, wz, acc[2][h]);
+			}
+		};
+		if (cnt == kTile) {
+#pragma unroll 2
+			for (int j = 0; j < kTile; ++j) body(j);
+		} else {
+#pragma unroll 1
+			for (int j = 0; j < cnt; ++j) body(j);
+		}
+#pragma unroll
+		for (int c = 0; c < NC; ++c)
+#pragma unroll
+			for (int h = 0; h < H; ++h)
+#pragma unroll
+				for (int e = 0; e < 2; ++e) {
+					const int i = (c * TPT + 2 * h + e) * NT + tid;
+					float hv = hi[i], lv = lo[i];
+					fold_twosum(hv, lv, e == 0 ? acc[c][h].x : acc[c][h].y);
+					hi[i] = hv; lo[i] = lv;
+				}
+	};
+	if (!Stream2::run(smem, p.src, s_begin, n_s, err, tile_fn)) return;
+#pragma unroll
+	for (int k = 0; k < TPT; ++k) {
+		const int t = tbase + k * NT + tid;
+		if (t >= p.n_tgt) continue;
+#pragma unroll
+		for (int c = 0; c < NC; ++c) {
+			const int i = (c * TPT + k) * NT + tid;
+			const double s = double(hi[i]) + double(lo[i]);
+			if (gridDim.y == 1) p.out[3 * size_t(t) + c] = float(vc.scale * s);
+			else partial[(size_t(blockIdx.y) * NC + c) * p.n_tgt + t] = s;
+		}
+	}
+}
+
 __global__ void p3_finalize_scaled(float* __restrict__ out, int n_tgt,
 	const double* __restrict__ partial, int n_split, double scale)
 {
@@ -651,16 +748,23 @@ cudaError_t induce_launch(int reg, unsigned ops, const P3DInduceProblem& p, cons
 	});
 }
 
-template <Reg R, int TPT, int NT>
-Plan plan_visc(int n_src, int n_tgt, int num_sms) {
-	constexpr size_t smem = smem_bytes<TPT, NT, 3>();
-	static const int occ = resident_ctas(p3d_visc_kernel<R, TPT, NT>, NT, smem);
-	return make_plan(n_src, n_tgt, TPT * NT, kTile, 3, num_sms * occ, smem);
+template <Reg R, int TPT, int NT, bool PK>
+auto visc_kernel() {
+	if constexpr (PK) return p3d_visc2_kernel<R, TPT, NT>;
+	else return p3d_visc_kernel<R, TPT, NT>;
 }
 
-template <Reg R, int TPT, int NT>
+template <Reg R, int TPT, int NT, bool PK>
+Plan plan_visc(int n_src, int n_tgt, int num_sms, int max_split = 64) {
+	constexpr size_t smem = smem_bytes<TPT, NT, 3>();
+	static const int occ = resident_ctas(visc_kernel<R, TPT, NT, PK>(), NT, smem);
+	return make_plan(n_src, n_tgt, TPT * NT, kTile, 3, num_sms * occ, smem, max_split);
+}
+
+template <Reg R, int TPT, int NT, bool PK>
 cudaError_t launch_visc(const P3DViscProblem& p, const LaunchEnv& env) {
-	const Plan pl = plan_visc<R, TPT, NT>(p.n_src, p.n_tgt, env.num_sms);
+	const Plan pl = plan_visc<R, TPT, NT, PK>(p.n_src, p.n_tgt, env.num_sms,
+		env.cap_to_ws ? split_cap_for(env.ws_bytes, 3, p.n_tgt) : 64);
 	if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
 	ViscConsts vc;
 	vc.rc = make_reg_consts(p.sigma);
@@ -668,7 +772,7 @@ cudaError_t launch_visc(const P3DViscProblem& p, const LaunchEnv& env) {
 	vc.scale = base * (R == Reg::Winckelmans ? 52.5 : double(kSqrt2OverPi));
 	double* partial = static_cast<double*>(env.ws);
 	dim3 grid(pl.n_tblocks, pl.n_split);
-	p3d_visc_kernel<R, TPT, NT><<<grid, NT, pl.smem, env.stream>>>(
+	visc_kernel<R, TPT, NT, PK>()<<<grid, NT, pl.smem, env.stream>>>(
 		p, vc, partial, pl.src_per_split, env.err);
 	count_launch();
 	if (pl.n_split > 1) {
@@ -750,11 +854,11 @@ size_t p3d_visc_ws_bytes(int reg, int n_src, int n_tgt, int num_sms) {
 	if (n_tgt <= 0) return 0;
 	const bool small = n_tgt < kSmallTargets;
 	if (reg == int(Reg::Winckelmans))
-		return small ? plan_visc<Reg::Winckelmans, 1, 128>(n_src, n_tgt, num_sms).ws_bytes
-		             : plan_visc<Reg::Winckelmans, 4, 128>(n_src, n_tgt, num_sms).ws_bytes;
+		return small ? plan_visc<Reg::Winckelmans, 1, 128, false>(n_src, n_tgt, num_sms).ws_bytes
+		             : plan_visc<Reg::Winckelmans, 4, 128, true>(n_src, n_tgt, num_sms).ws_bytes;
 	if (reg == int(Reg::Gaussian))
-		return small ? plan_visc<Reg::Gaussian, 1, 128>(n_src, n_tgt, num_sms).ws_bytes
-		             : plan_visc<Reg::Gaussian, 4, 128>(n_src, n_tgt, num_sms).ws_bytes;
+		return small ? plan_visc<Reg::Gaussian, 1, 128, false>(n_src, n_tgt, num_sms).ws_bytes
+		             : plan_visc<Reg::Gaussian, 4, 128, true>(n_src, n_tgt, num_sms).ws_bytes;
 	return 0;
 }
 
@@ -764,11 +868,11 @@ cudaError_t p3d_visc(int reg, const P3DViscProblem& p, const LaunchEnv& env) {
 	if (p.n_tgt <= 0) return cudaSuccess;
 	const bool small = p.n_tgt < kSmallTargets;
 	if (reg == int(Reg::Winckelmans))
-		return small ? launch_visc<Reg::Winckelmans, 1, 128>(p, env)
-		             : launch_visc<Reg::Winckelmans, 4, 128>(p, env);
+		return small ? launch_visc<Reg::Winckelmans, 1, 128, false>(p, env)
+		             : launch_visc<Reg::Winckelmans, 4, 128, true>(p, env);
 	if (reg == int(Reg::Gaussian))
-		return small ? launch_visc<Reg::Gaussian, 1, 128>(p, env)
-		             : launch_visc<Reg::Gaussian, 4, 128>(p, env);
+		return small ? launch_visc<Reg::Gaussian, 1, 128, false>(p, env)
+		             : launch_visc<Reg::Gaussian, 4, 128, true>(p, env);
 	return cudaErrorInvalidValue;
 }
 

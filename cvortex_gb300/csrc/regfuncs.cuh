@@ -349,6 +349,25 @@ template <> struct RegP2D<Reg::Gaussian> {
 	}
 };
 
+// Viscous weights, packed: Winckelmans s^9 (times 52.5 on the host),
+// Gaussian exp(-x2/2) (times sqrt(2/pi) on the host).
+template <Reg R> struct RegEta2;
+template <> struct RegEta2<Reg::Winckelmans> {
+	__device__ __forceinline__ static float2 eta2(float2 r2, const RegConsts& c) {
+		const float2 q = __ffma2_rn(r2, bc2(c.inv_s2), bc2(1.f));
+		const float2 s = make_float2(rsqrt_approx(q.x), rsqrt_approx(q.y));
+		const float2 s2 = __fmul2_rn(s, s);
+		const float2 s4 = __fmul2_rn(s2, s2);
+		return __fmul2_rn(__fmul2_rn(s4, s4), s);
+	}
+};
+template <> struct RegEta2<Reg::Gaussian> {
+	__device__ __forceinline__ static float2 eta2(float2 r2, const RegConsts& c) {
+		const float2 a = __fmul2_rn(r2, bc2(c.exp2_half));
+		return make_float2(ex2_approx(a.x), ex2_approx(a.y));
+	}
+};
+
 // ---- 2D, packed (two targets per f32x2 lane pair) ----------------------------
 // 1/x from rcp refined by one Newton step, t (2 - x t): within an ulp.
 __device__ __forceinline__ float2 rcp2(float2 x) {
