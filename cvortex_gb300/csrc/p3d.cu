@@ -245,7 +245,7 @@ p3d_induce_kernel(const P3DInduceProblem p, const InduceConsts kc,
 
 // Packed variant of p3d_induce_kernel (two targets per f32x2 lane pair; see
 // induce2_block in p3d_induce.cuh). CTA (x, y) = (target block, source split).
-template <Reg R, bool VEL, bool DV, int TPT, int NT>
+template <Reg R, bool VEL, bool DV, int TPT, int NT, int UNROLL>
 __global__ void __launch_bounds__(NT)
 p3d_induce2_kernel(const P3DInduceProblem p, const InduceConsts kc,
 	double* __restrict__ partial, int src_per_split, unsigned* err)
@@ -258,7 +258,7 @@ p3d_induce2_kernel(const P3DInduceProblem p, const InduceConsts kc,
 	int n_s = p.n_src - s_begin;
 	n_s = n_s < src_per_split ? n_s : src_per_split;
 	n_s = n_s > 0 ? n_s : 0;
-	induce2_block<R, VEL, DV, TPT, NT>(p, kc, blockIdx.x * (TPT * NT), s_begin, n_s, smem, err,
+	induce2_block<R, VEL, DV, TPT, NT, UNROLL>(p, kc, blockIdx.x * (TPT * NT), s_begin, n_s, smem, err,
 		tcount, [&](int t, const double* acc, float ax, float ay, float az) {
 			if (gridDim.y == 1) {
 				write_induce<VEL, DV>(p, kc, t, acc, ax, ay, az);
@@ -620,17 +620,20 @@ constexpr int kSmallTargets = 8192;
 struct CfgSpec { int tpt, nt; bool packed; };
 constexpr CfgSpec kCfg[] = {
 	{1, 128, false}, {4, 128, false}, {4, 128, true}, {2, 128, true},
-	{4, 64, true},   {2, 256, true},  {6, 64, true},
+	{4, 64, true},   {2, 256, true},  {6, 64, true},  {4, 128, true},
+	{4, 128, true},  {2, 128, true},
 };
+// Configurations 7-9 repeat shapes with another source-loop unroll factor
+// (7: 1, 8 and 9: 4; all others 2).
 constexpr int kNumCfg = int(sizeof(kCfg) / sizeof(kCfg[0]));
 
-template <Reg R, bool VEL, bool DV, int TPT, int NT, bool PK>
+template <Reg R, bool VEL, bool DV, int TPT, int NT, bool PK, int UNROLL = 2>
 struct InduceVariant {
 	static constexpr int NC = (VEL ? 3 : 0) + (DV ? 6 : 0);
 	static constexpr size_t kSmem = smem_bytes<TPT, NT, NC>();
 	using Fn = void (*)(const P3DInduceProblem, const InduceConsts, double*, int, unsigned*);
 	static Fn fn() {
-		if constexpr (PK) return p3d_induce2_kernel<R, VEL, DV, TPT, NT>;
+		if constexpr (PK) return p3d_induce2_kernel<R, VEL, DV, TPT, NT, UNROLL>;
 		else return p3d_induce_kernel<R, VEL, DV, TPT, NT>;
 	}
 	static int occupancy() {
@@ -665,7 +668,10 @@ auto with_cfg(int ci, F&& f) {
 	case 3: return f(InduceVariant<R, VEL, DV, 2, 128, true>{});
 	case 4: return f(InduceVariant<R, VEL, DV, 4, 64, true>{});
 	case 5: return f(InduceVariant<R, VEL, DV, 2, 256, true>{});
-	default: return f(InduceVariant<R, VEL, DV, 6, 64, true>{});
+	case 6: return f(InduceVariant<R, VEL, DV, 6, 64, true>{});
+	case 7: return f(InduceVariant<R, VEL, DV, 4, 128, true, 1>{});
+	case 8: return f(InduceVariant<R, VEL, DV, 4, 128, true, 4>{});
+	default: return f(InduceVariant<R, VEL, DV, 2, 128, true, 4>{});
 	}
 }
 
@@ -712,7 +718,7 @@ int env_cfg() {
 constexpr signed char kMidCfg[4][4] = {
 	{2, 3, 5, 3}, {2, 3, 0, 2}, {2, 3, 0, 2}, {2, 6, 5, 3}};
 constexpr signed char kLargeCfg[4][4] = {
-	{2, 3, 5, 3}, {2, 3, 5, 2}, {2, 4, 2, 2}, {2, 6, 5, 3}};
+	{2, 3, 5, 3}, {2, 8, 6, 2}, {2, 4, 2, 2}, {2, 8, 5, 9}};
 
 int choose_cfg(int reg, unsigned ops, int n_tgt) {
 	const int forced = env_cfg();

@@ -76,7 +76,7 @@ __device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y
 // P3DStream::init; `tcount` carries the stage phase across calls). For every
 // valid target calls sink(t, sums[NC], alpha_t). Returns false if the tile
 // pipeline timed out (results were not produced).
-template <Reg R, bool VEL, bool DV, int TPT, int NT, class Sink>
+template <Reg R, bool VEL, bool DV, int TPT, int NT, int UNROLL = 2, class Sink>
 __device__ __forceinline__ bool induce2_block(const P3DInduceProblem& p, const InduceConsts& kc,
 	int tbase, int s_begin, int n_s, unsigned char* smem, unsigned* err, unsigned& tcount,
 	Sink&& sink)
@@ -178,7 +178,7 @@ __device__ __forceinline__ bool induce2_block(const P3DInduceProblem& p, const I
 			}
 		};
 		if (cnt == kP3DTile) {
-#pragma unroll 2
+#pragma unroll (UNROLL)
 			for (int j = 0; j < kP3DTile; ++j) body(j);
 		} else {
 #pragma unroll 1
