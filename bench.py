@@ -731,11 +731,17 @@ def run_reference(args):
     os.environ.setdefault("OMP_PROC_BIND", "spread")
     kind, ref = cpu_reference()
     p = workloads.vortex_ring(args.n)
-    idx = np.random.Generator(np.random.PCG64(7)).choice(args.n, min(CPU_SAMPLE_TARGETS, args.n),
-                                                         replace=False)
-    sub = p[np.sort(idx)].copy()
+    order = np.random.Generator(np.random.PCG64(7)).permutation(args.n)
+    # size each step's target sample so that all K steps take about a minute
+    probe = p[np.sort(order[:128])].copy()
     for _ in range(max(args.warmup, 1)):
-        cpu_step(kind, ref, p, sub[:128].copy(), args.reg)
+        t0 = time.perf_counter()
+        cpu_step(kind, ref, p, probe, args.reg)
+        per_target = (time.perf_counter() - t0) / len(probe)
+    budget_s = 60.0
+    m = int(budget_s / max(args.steps, 1) / max(per_target, 1e-9))
+    m = max(64, min(CPU_SAMPLE_TARGETS, m, args.n))
+    sub = p[np.sort(order[:m])].copy()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         cpu_step(kind, ref, p, sub, args.reg)
@@ -753,8 +759,9 @@ def run_reference(args):
                       "parallelism": f"{cores} host threads (OpenMP)"},
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
                             "cpu_model": cpu_model(),
-                            "sample": f"each step: vel + dvort for {len(sub)} sampled targets x "
-                                      f"{len(p)} sources"},
+                            "sample": f"each step: vel + dvort for {len(sub)} seeded targets x "
+                                      f"{len(p)} sources (sample sized for about "
+                                      f"{budget_s:.0f} s over {args.steps} steps)"},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 

@@ -180,3 +180,25 @@ def test_dev_p3d_step_matches_served_step(gpu, srv):
     # the device API plans its own split count, so agreement is to rounding
     assert exact.rel_l2(got, req.state_out) <= 1e-6
     assert exact.rel_l2(vel.cpu().numpy(), req.vel_out) <= TOL
+
+
+def test_admission_waits_for_memory(gpu):
+    """A budget that holds only a few requests at a time: the queue waits for
+    memory, every request completes, and results equal those of a roomy
+    server."""
+    roomy = [serve.Request.p3d(workloads.uniform_cube(6000 + 500 * i, seed=60 + i), n_steps=2)
+             for i in range(8)]
+    tight = [serve.Request.p3d(workloads.uniform_cube(6000 + 500 * i, seed=60 + i), n_steps=2)
+             for i in range(8)]
+    with serve.Server(gpu.lib, n_slots=8, hbm_bytes=1 << 30) as s:
+        for r in roomy:
+            s.submit(r)
+        assert s.drain(120_000)
+    with serve.Server(gpu.lib, n_slots=8, hbm_bytes=1 << 20) as s:     # ~2 requests fit
+        ids = [s.submit(r) for r in tight]
+        assert s.drain(120_000)
+        assert all(s.wait(i, 0) == 0 for i in ids)
+        st = s.stats()
+        assert st["completed"] == 8 and st["hbm_peak"] <= 1 << 20
+    for a, b in zip(roomy, tight):
+        assert np.array_equal(a.state_out, b.state_out)
