@@ -438,6 +438,13 @@ def extras(cv, lib, args, torch, sh, peak):
     ms = timed_dev(f, torch, 5)
     res["f3d_sheet100k_vel"] = {"ginter_s": nf * nf / ms / 1e6,
                                 "fp32_frac": 51 * nf * nf / (ms * 1e-3) / 1e12 / peak}
+    cube = workloads.uniform_cube(nf, seed=12)
+    rc = torch.from_numpy(p3d_records(cube).reshape(nf, 8)).cuda()
+    f = lambda: lib.cvtx_gb300_dev_F3D_M2M_dvort(rfd.data_ptr(), nf, rc.data_ptr(), 2, nf,
+                                                 of.data_ptr(), sh)
+    ms = timed_dev(f, torch, 3)
+    res["f3d_sheet100k_dvort_cube100k"] = {"ginter_s": nf * nf / ms / 1e6,
+                                           "fp32_frac": 62 * nf * nf / (ms * 1e-3) / 1e12 / peak}
     res["batch512"] = batch_extra(cv, lib, torch, sh)
     res["redistribute_ring200k_m4p"] = redistribute_extra(cv, lib)
     m = 1_000_000

@@ -155,6 +155,22 @@ CVTX_EXPORT int cvtx_gb300_dev_F3D_M2M_vel(const void* fil, int n_fil, const voi
 	return c.done(f3d_vel(p, c.env()), "cvtx_gb300_dev_F3D_M2M_vel");
 }
 
+CVTX_EXPORT int cvtx_gb300_dev_F3D_M2M_dvort(const void* fil, int n_fil, const void* tgt,
+	int tgt_stride, int n_tgt, float* out, void* stream)
+{
+	if (n_tgt <= 0) return 0;
+	if (n_fil < 0 || !tgt || !out || tgt_stride < 2) return -1;
+	DevCall c(stream);
+	int st = c.prepare(f3d_dvort_ws_bytes(n_fil, n_tgt, c.ctx ? c.ctx->num_sms : 1),
+		"cvtx_gb300_dev_F3D_M2M_dvort");
+	if (st) return st;
+	F3DDvortProblem p;
+	p.fil = static_cast<const float4*>(fil); p.n_fil = n_fil;
+	p.tgt = static_cast<const float4*>(tgt); p.tstride = tgt_stride; p.n_tgt = n_tgt;
+	p.out = out;
+	return c.done(f3d_dvort(p, c.env()), "cvtx_gb300_dev_F3D_M2M_dvort");
+}
+
 CVTX_EXPORT int cvtx_gb300_dev_pack_P3D(const cvtx_P3D* aos, int n, void* rec, void* stream) {
 	if (n < 0 || (n > 0 && (!aos || !rec))) return -1;
 	return pack_p3d(aos, n, static_cast<float4*>(rec), static_cast<cudaStream_t>(stream)) ==

@@ -90,6 +90,9 @@ CVTX_EXPORT int cvtx_gb300_dev_P2D_M2M_vel(const void* src, int n_src,
 	float regularisation_radius, void* stream);
 CVTX_EXPORT int cvtx_gb300_dev_F3D_M2M_vel(const void* fil, int n_fil,
 	const void* tgt, int tgt_stride, int n_tgt, float* out, void* stream);
+/* Stretching of P3D particles (records, tgt_stride >= 2) by filaments. */
+CVTX_EXPORT int cvtx_gb300_dev_F3D_M2M_dvort(const void* fil, int n_fil,
+	const void* tgt, int tgt_stride, int n_tgt, float* out, void* stream);
 /* cvtx_gb300_dev_P3D_M2M without any device allocation. It has no
  * counterpart in the reference. For callers that cannot let a library call
  * cudaMalloc: device memory owned by one pool reserved up front, or loops

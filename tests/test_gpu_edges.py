@@ -147,3 +147,20 @@ def test_withheld_doorbell_reports_timeout(gpu):
     p = workloads.uniform_cube(500, seed=3)
     vel = gpu.p3d_vel(p, p["coord"], "winckelmans", 0.05)
     assert exact.rel_l2(vel, oracle.p3d_vel(p, p["coord"], "winckelmans", 0.05)) <= TOL
+
+
+def test_dev_f3d_dvort_matches_oracle(gpu):
+    import torch
+    f = workloads.wake_sheet(3000, seed=5)
+    p = workloads.uniform_cube(9000, seed=6)
+    rf = np.zeros((len(f), 8), np.float32)
+    rf[:, 0:3], rf[:, 3], rf[:, 4:7] = f["start"], f["strength"], f["end"]
+    rp = np.zeros((len(p), 8), np.float32)
+    rp[:, 0:3], rp[:, 3], rp[:, 4:7] = p["coord"], p["volume"], p["vorticity"]
+    a, b = torch.from_numpy(rf).cuda(), torch.from_numpy(rp).cuda()
+    out = torch.empty((len(p), 3), dtype=torch.float32, device="cuda")
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert gpu.lib.cvtx_gb300_dev_F3D_M2M_dvort(a.data_ptr(), len(f), b.data_ptr(), 2, len(p),
+                                                out.data_ptr(), stream) == 0
+    assert gpu.lib.cvtx_gb300_dev_status(stream) == 0
+    close(out.cpu().numpy(), oracle.f3d_dvort(f, p))
