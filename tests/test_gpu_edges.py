@@ -164,3 +164,23 @@ def test_dev_f3d_dvort_matches_oracle(gpu):
                                                 out.data_ptr(), stream) == 0
     assert gpu.lib.cvtx_gb300_dev_status(stream) == 0
     close(out.cpu().numpy(), oracle.f3d_dvort(f, p))
+
+
+@pytest.mark.parametrize("n", [8192, 8193, 20001])
+def test_packed_p2d_f3d_ragged_sizes(gpu, n):
+    """The packed P2D / F3D velocity kernels (8,192 targets and up) on sizes
+    that do not fill the last target block, with coincident and on-axis
+    targets."""
+    q = workloads.gaussian_patch_2d(n, seed=9)
+    idx = np.r_[0:64, n - 64:n]
+    for reg in ("singular", "winckelmans", "gaussian", "planetary"):
+        got = gpu.p2d_vel(q, q["coord"], reg, 0.05)
+        close(got[idx], oracle.p2d_vel(q, q["coord"][idx], reg, 0.05))
+    f = workloads.wake_sheet(3000, seed=10)
+    pts = workloads.sheet_targets(n, seed=11)
+    pts[:40] = f["start"][:40]
+    pts[40:80] = 0.5 * (f["start"][40:80] + f["end"][40:80])
+    got = gpu.f3d_vel(f, pts)
+    assert np.all(np.isfinite(got))
+    sel = np.r_[0:128, n - 64:n]
+    close(got[sel], oracle.f3d_vel(f, pts[sel]))
