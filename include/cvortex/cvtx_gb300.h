@@ -11,7 +11,12 @@
  *     never falls back, it reports instead and writes NaN results);
  *   - a fused vel + dvort call over one particle set;
  *   - a device-pointer API that works on packed records already in GPU
- *     memory, on a caller-supplied CUDA stream (records: see below).
+ *     memory, on a caller-supplied CUDA stream (records: see below),
+ *     including a device-resident time step;
+ *   - many problems in one graph-captured launch (cvtx_gb300_batch_*);
+ *   - a serving loop for concurrent clients (cvtx_gb300_server_*);
+ *   - the launch-configuration table, FP32 peak probes and a self test of
+ *     the device-side failure path.
  *
  * Device record layouts (16-byte aligned arrays of float4):
  *   P3D  : 2 float4 per particle  (x, y, z, volume), (wx, wy, wz, 0)
