@@ -284,6 +284,138 @@ __device__ __forceinline__ void f3d_dvort_pair(float px, float py, float pz,
 	oz = ok ? vz : 0.f;
 }
 
+// f3d_dvort_pair for two particles at once (f32x2). |r1 x r0| comes from
+// X2 * rsqrt(X2) and the division by X2 from rcp refined by one Newton step.
+// The terms the reference keeps are kept with the same value to rounding; a
+// particle exactly on the filament's segment (X2 = 0, where the reference's
+// term is infinite or NaN) has its term dropped.
+__device__ __forceinline__ void f3d_dvort_pair2(float2 px, float2 py, float2 pz,
+	float2 wx, float2 wy, float2 wz, const float4 a, const float4 b,
+	float2& ox, float2& oy, float2& oz)
+{
+	const float2 r1x = __fadd2_rn(px, bc2(-a.x)), r1y = __fadd2_rn(py, bc2(-a.y));
+	const float2 r1z = __fadd2_rn(pz, bc2(-a.z));
+	const float2 r2x = __fadd2_rn(px, bc2(-b.x)), r2y = __fadd2_rn(py, bc2(-b.y));
+	const float2 r2z = __fadd2_rn(pz, bc2(-b.z));
+	const float2 r0x = __fadd2_rn(r1x, neg2f(r2x)), r0y = __fadd2_rn(r1y, neg2f(r2y));
+	const float2 r0z = __fadd2_rn(r1z, neg2f(r2z));
+	const float2 xx = __ffma2_rn(r1y, r0z, neg2f(__fmul2_rn(r1z, r0y)));
+	const float2 xy = __ffma2_rn(r1z, r0x, neg2f(__fmul2_rn(r1x, r0z)));
+	const float2 xz = __ffma2_rn(r1x, r0y, neg2f(__fmul2_rn(r1y, r0x)));
+	const float2 X2 = __ffma2_rn(xz, xz, __ffma2_rn(xy, xy, __fmul2_rn(xx, xx)));
+	const float2 iX = make_float2(rsqrt_approx(X2.x), rsqrt_approx(X2.y));
+	const float2 X = __fmul2_rn(X2, iX);
+	const float2 q1 = __ffma2_rn(r1z, r1z, __ffma2_rn(r1y, r1y, __fmul2_rn(r1x, r1x)));
+	const float2 q2 = __ffma2_rn(r2z, r2z, __ffma2_rn(r2y, r2y, __fmul2_rn(r2x, r2x)));
+	const float2 q0 = __ffma2_rn(r0z, r0z, __ffma2_rn(r0y, r0y, __fmul2_rn(r0x, r0x)));
+	const float2 il1 = make_float2(rsqrt_approx(q1.x), rsqrt_approx(q1.y));
+	const float2 il2 = make_float2(rsqrt_approx(q2.x), rsqrt_approx(q2.y));
+	const float2 il0 = make_float2(rsqrt_approx(q0.x), rsqrt_approx(q0.y));
+	const float2 d1 = __fmul2_rn(__ffma2_rn(r0z, r1z, __ffma2_rn(r0y, r1y, __fmul2_rn(r0x, r1x))), il1);
+	const float2 d2 = __fmul2_rn(__ffma2_rn(r0z, r2z, __ffma2_rn(r0y, r2y, __fmul2_rn(r0x, r2x))), il2);
+	const float2 t212 = __fadd2_rn(d1, neg2f(d2));
+	const float2 t222 = __fadd2_rn(__fmul2_rn(X, il1), neg2f(__fmul2_rn(X, il2)));
+	const float2 kA = __fmul2_rn(__fmul2_rn(bc2(-a.w), t212), rcp2(X2));
+	const float2 Ax = __fmul2_rn(r0x, kA), Ay = __fmul2_rn(r0y, kA), Az = __fmul2_rn(r0z, kA);
+	const float2 B = __fmul2_rn(__fmul2_rn(__fmul2_rn(bc2(3.f), il0), bc2(a.w)), t222);
+	const float2 vx = __ffma2_rn(wx, B, __ffma2_rn(Ay, wz, neg2f(__fmul2_rn(Az, wy))));
+	const float2 vy = __ffma2_rn(wy, B, __ffma2_rn(Az, wx, neg2f(__fmul2_rn(Ax, wz))));
+	const float2 vz = __ffma2_rn(wz, B, __ffma2_rn(Ax, wy, neg2f(__fmul2_rn(Ay, wx))));
+	const bool okx = X2.x > 0.f && (vx.x == vx.x) && (vy.x == vy.x) && (vz.x == vz.x) &&
+		(t222.x == t222.x) && (t212.x == t212.x);
+	const bool oky = X2.y > 0.f && (vx.y == vx.y) && (vy.y == vy.y) && (vz.y == vz.y) &&
+		(t222.y == t222.y) && (t212.y == t212.y);
+	ox = make_float2(okx ? vx.x : 0.f, oky ? vx.y : 0.f);
+	oy = make_float2(okx ? vy.x : 0.f, oky ? vy.y : 0.f);
+	oz = make_float2(okx ? vz.x : 0.f, oky ? vz.y : 0.f);
+}
+
+template <int TPT, int NT>
+__global__ void __launch_bounds__(NT)
+f3d_dvort2_kernel(const F3DDvortProblem p, double* __restrict__ partial, int src_per_split,
+	unsigned* err)
+{
+	static_assert(TPT % 2 == 0, "packed kernel: even TPT");
+	constexpr int NC = 3, H = TPT / 2;
+	extern __shared__ __align__(16) unsigned char smem[];
+	float* hi = reinterpret_cast<float*>(smem + Stream2::kSmemBytes);
+	float* lo = hi + NC * TPT * NT;
+	const int tid = threadIdx.x;
+	const int tbase = blockIdx.x * (TPT * NT);
+	const int s_begin = blockIdx.y * src_per_split;
+	int n_s = p.n_fil - s_begin;
+	n_s = n_s < src_per_split ? n_s : src_per_split;
+	n_s = n_s > 0 ? n_s : 0;
+	float2 tx[H], ty[H], tz[H], ax[H], ay[H], az[H];
+#pragma unroll
+	for (int h = 0; h < H; ++h) {
+		float4 q[2], v[2];
+#pragma unroll
+		for (int e = 0; e < 2; ++e) {
+			int t = tbase + (2 * h + e) * NT + tid;
+			t = t < p.n_tgt ? t : p.n_tgt - 1;
+			q[e] = p.tgt[size_t(t) * p.tstride];
+			v[e] = p.tgt[size_t(t) * p.tstride + 1];
+		}
+		tx[h] = make_float2(q[0].x, q[1].x); ty[h] = make_float2(q[0].y, q[1].y);
+		tz[h] = make_float2(q[0].z, q[1].z);
+		ax[h] = make_float2(v[0].x, v[1].x); ay[h] = make_float2(v[0].y, v[1].y);
+		az[h] = make_float2(v[0].z, v[1].z);
+	}
+#pragma unroll
+	for (int i = 0; i < NC * TPT; ++i) { hi[i * NT + tid] = 0.f; lo[i * NT + tid] = 0.f; }
+	auto tile_fn = [&](const float4* __restrict__ st, int cnt) {
+		float2 acc[NC][H];
+#pragma unroll
+		for (int c = 0; c < NC; ++c)
+#pragma unroll
+			for (int h = 0; h < H; ++h) acc[c][h] = make_float2(0.f, 0.f);
+		auto body = [&](int j) {
+			const float4 a = st[2 * j];
+			const float4 b = st[2 * j + 1];
+#pragma unroll
+			for (int h = 0; h < H; ++h) {
+				float2 vx, vy, vz;
+				f3d_dvort_pair2(tx[h], ty[h], tz[h], ax[h], ay[h], az[h], a, b, vx, vy, vz);
+				acc[0][h] = __fadd2_rn(acc[0][h], vx);
+				acc[1][h] = __fadd2_rn(acc[1][h], vy);
+				acc[2][h] = __fadd2_rn(acc[2][h], vz);
+			}
+		};
+		if (cnt == kTile) {
+#pragma unroll 2
+			for (int j = 0; j < kTile; ++j) body(j);
+		} else {
+#pragma unroll 1
+			for (int j = 0; j < cnt; ++j) body(j);
+		}
+#pragma unroll
+		for (int c = 0; c < NC; ++c)
+#pragma unroll
+			for (int h = 0; h < H; ++h)
+#pragma unroll
+				for (int e = 0; e < 2; ++e) {
+					const int i = (c * TPT + 2 * h + e) * NT + tid;
+					float hv = hi[i], lv = lo[i];
+					fold_twosum(hv, lv, e == 0 ? acc[c][h].x : acc[c][h].y);
+					hi[i] = hv; lo[i] = lv;
+				}
+	};
+	if (!Stream2::run(smem, p.fil, s_begin, n_s, err, tile_fn)) return;
+#pragma unroll
+	for (int k = 0; k < TPT; ++k) {
+		const int t = tbase + k * NT + tid;
+		if (t >= p.n_tgt) continue;
+#pragma unroll
+		for (int c = 0; c < NC; ++c) {
+			const int i = (c * TPT + k) * NT + tid;
+			const double s = double(hi[i]) + double(lo[i]);
+			if (gridDim.y == 1) p.out[3 * size_t(t) + c] = float(kInv4Pi * s);
+			else partial[(size_t(blockIdx.y) * NC + c) * p.n_tgt + t] = s;
+		}
+	}
+}
+
 template <int TPT, int NT>
 __global__ void __launch_bounds__(NT)
 f3d_dvort_kernel(const F3DDvortProblem p, double* __restrict__ partial, int src_per_split,
@@ -429,10 +561,16 @@ Plan plan_vel(int n_fil, int n_tgt, int num_sms, int max_split = 64) {
 	static const int occ = resident_ctas(vel_kernel<TPT, NT, PK>(), NT, smem);
 	return make_plan(n_fil, n_tgt, TPT * NT, kTile, 3, num_sms * occ, smem, max_split);
 }
-template <int TPT, int NT>
+template <int TPT, int NT, bool PK>
+auto dvort_kernel() {
+	if constexpr (PK) return f3d_dvort2_kernel<TPT, NT>;
+	else return f3d_dvort_kernel<TPT, NT>;
+}
+
+template <int TPT, int NT, bool PK>
 Plan plan_dvort(int n_fil, int n_tgt, int num_sms, int max_split = 64) {
 	constexpr size_t smem = smem_bytes<TPT, NT>();
-	static const int occ = resident_ctas(f3d_dvort_kernel<TPT, NT>, NT, smem);
+	static const int occ = resident_ctas(dvort_kernel<TPT, NT, PK>(), NT, smem);
 	return make_plan(n_fil, n_tgt, TPT * NT, kTile, 3, num_sms * occ, smem, max_split);
 }
 
@@ -451,13 +589,13 @@ cudaError_t launch_vel(const F3DVelProblem& p, const LaunchEnv& env) {
 	}
 	return cudaGetLastError();
 }
-template <int TPT, int NT>
+template <int TPT, int NT, bool PK>
 cudaError_t launch_dvort(const F3DDvortProblem& p, const LaunchEnv& env) {
-	const Plan pl = plan_dvort<TPT, NT>(p.n_fil, p.n_tgt, env.num_sms,
+	const Plan pl = plan_dvort<TPT, NT, PK>(p.n_fil, p.n_tgt, env.num_sms,
 		env.cap_to_ws ? split_cap_for(env.ws_bytes, 3, p.n_tgt) : 64);
 	if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
 	double* partial = static_cast<double*>(env.ws);
-	f3d_dvort_kernel<TPT, NT><<<dim3(pl.n_tblocks, pl.n_split), NT, pl.smem, env.stream>>>(
+	dvort_kernel<TPT, NT, PK>()<<<dim3(pl.n_tblocks, pl.n_split), NT, pl.smem, env.stream>>>(
 		p, partial, pl.src_per_split, env.err);
 	count_launch();
 	if (pl.n_split > 1) {
@@ -509,12 +647,13 @@ cudaError_t f3d_vel(const F3DVelProblem& p, const LaunchEnv& env) {
 }
 size_t f3d_dvort_ws_bytes(int n_fil, int n_tgt, int num_sms) {
 	if (n_tgt <= 0) return 0;
-	return n_tgt < kSmallTargets ? plan_dvort<1, 128>(n_fil, n_tgt, num_sms).ws_bytes
-	                             : plan_dvort<2, 128>(n_fil, n_tgt, num_sms).ws_bytes;
+	return n_tgt < kSmallTargets ? plan_dvort<1, 128, false>(n_fil, n_tgt, num_sms).ws_bytes
+	                             : plan_dvort<2, 128, true>(n_fil, n_tgt, num_sms).ws_bytes;
 }
 cudaError_t f3d_dvort(const F3DDvortProblem& p, const LaunchEnv& env) {
 	if (p.n_tgt <= 0) return cudaSuccess;
-	return p.n_tgt < kSmallTargets ? launch_dvort<1, 128>(p, env) : launch_dvort<2, 128>(p, env);
+	return p.n_tgt < kSmallTargets ? launch_dvort<1, 128, false>(p, env)
+	                               : launch_dvort<2, 128, true>(p, env);
 }
 cudaError_t f3d_inf_mtrx(const F3DInfProblem& p, const LaunchEnv& env) {
 	if (p.n_mes <= 0 || p.n_fil <= 0) return cudaSuccess;

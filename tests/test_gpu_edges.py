@@ -184,3 +184,17 @@ def test_packed_p2d_f3d_ragged_sizes(gpu, n):
     assert np.all(np.isfinite(got))
     sel = np.r_[0:128, n - 64:n]
     close(got[sel], oracle.f3d_vel(f, pts[sel]))
+
+
+@pytest.mark.parametrize("n", [8192, 12001])
+def test_packed_f3d_dvort(gpu, n):
+    """The packed F3D stretching kernel (8,192 particles and up) against the
+    oracle, with particles at filament ends (terms the reference drops)."""
+    f = workloads.wake_sheet(2000, seed=12)
+    p = workloads.uniform_cube(n, seed=13)
+    p["coord"][:30] = f["start"][:30]
+    p["coord"][30:60] = f["end"][30:60]
+    got = gpu.f3d_dvort(f, p)
+    assert np.all(np.isfinite(got))
+    sel = np.r_[0:128, n - 64:n]
+    close(got[sel], oracle.f3d_dvort(f, p[sel]))
