@@ -422,6 +422,14 @@ def extras(cv, lib, args, torch, sh, peak):
     ms = timed_dev(f, torch, 5)
     res["p2d_patch200k_winckelmans_vel"] = {"ginter_s": len(q) ** 2 / ms / 1e6,
                                             "fp32_frac": 15 * len(q) ** 2 / (ms * 1e-3) / 1e12 / peak}
+    ov = torch.empty((len(q),), dtype=torch.float32, device="cuda")
+    for rname, r, fl in (("winckelmans", 1, 16), ("gaussian", 3, 10)):
+        f = lambda: lib.cvtx_gb300_dev_P2D_M2M_visc(rq.data_ptr(), len(q), rq.data_ptr(), len(q),
+                                                    ov.data_ptr(), r, SIGMA, 1e-3, sh)
+        ms = timed_dev(f, torch, 5)
+        res[f"p2d_patch200k_{rname}_visc"] = {
+            "ginter_s": len(q) ** 2 / ms / 1e6,
+            "fp32_frac": fl * len(q) ** 2 / (ms * 1e-3) / 1e12 / peak}
     nf = 100_000
     fil = workloads.wake_sheet(nf)
     pts = workloads.sheet_targets(nf)

@@ -139,6 +139,27 @@ CVTX_EXPORT int cvtx_gb300_dev_P2D_M2M_vel(const void* src, int n_src, const voi
 	return c.done(p2d_vel(reg, p, c.env()), "cvtx_gb300_dev_P2D_M2M_vel");
 }
 
+CVTX_EXPORT int cvtx_gb300_dev_P2D_M2M_visc(const void* src, int n_src, const void* tgt,
+	int n_tgt, float* out, int reg, float sigma, float nu, void* stream)
+{
+	if (n_tgt <= 0) return 0;
+	if (n_src < 0 || !tgt || !out || bad_reg(reg)) return -1;
+	DevCall c(stream);
+	if (reg == 0 || reg == 2) {
+		if (!c.ctx) return -3;
+		const cudaError_t e = cudaMemsetAsync(out, 0, sizeof(float) * size_t(n_tgt), c.stream);
+		return e == cudaSuccess ? 0 : -2;
+	}
+	int st = c.prepare(p2d_visc_ws_bytes(reg, n_src, n_tgt, c.ctx ? c.ctx->num_sms : 1),
+		"cvtx_gb300_dev_P2D_M2M_visc");
+	if (st) return st;
+	P2DViscProblem p;
+	p.src = static_cast<const float4*>(src); p.n_src = n_src;
+	p.tgt = static_cast<const float4*>(tgt); p.n_tgt = n_tgt;
+	p.out = out; p.sigma = sigma; p.nu = nu;
+	return c.done(p2d_visc(reg, p, c.env()), "cvtx_gb300_dev_P2D_M2M_visc");
+}
+
 CVTX_EXPORT int cvtx_gb300_dev_F3D_M2M_vel(const void* fil, int n_fil, const void* tgt,
 	int tgt_stride, int n_tgt, float* out, void* stream)
 {

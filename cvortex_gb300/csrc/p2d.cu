@@ -265,6 +265,87 @@ p2d_visc_kernel(const P2DViscProblem p, const RegConsts rc, double scale,
 	}
 }
 
+// Packed viscous exchange (two targets per f32x2 lane pair).
+template <Reg R, int TPT, int NT>
+__global__ void __launch_bounds__(NT)
+p2d_visc2_kernel(const P2DViscProblem p, const RegConsts rc, double scale,
+	double* __restrict__ partial, int src_per_split, unsigned* err)
+{
+	static_assert(TPT % 2 == 0, "packed kernel: even TPT");
+	constexpr int H = TPT / 2;
+	extern __shared__ __align__(16) unsigned char smem[];
+	float* hi = reinterpret_cast<float*>(smem + Stream1::kSmemBytes);
+	float* lo = hi + TPT * NT;
+	const int tid = threadIdx.x;
+	const int tbase = blockIdx.x * (TPT * NT);
+	const int s_begin = blockIdx.y * src_per_split;
+	int n_s = p.n_src - s_begin;
+	n_s = n_s < src_per_split ? n_s : src_per_split;
+	n_s = n_s > 0 ? n_s : 0;
+	float2 ntx[H], nty[H], ntg[H], ta[H];
+#pragma unroll
+	for (int h = 0; h < H; ++h) {
+		float4 q[2];
+#pragma unroll
+		for (int e = 0; e < 2; ++e) {
+			int t = tbase + (2 * h + e) * NT + tid;
+			t = t < p.n_tgt ? t : p.n_tgt - 1;
+			q[e] = p.tgt[t];
+		}
+		ntx[h] = make_float2(-q[0].x, -q[1].x); nty[h] = make_float2(-q[0].y, -q[1].y);
+		ntg[h] = make_float2(-q[0].z, -q[1].z); ta[h] = make_float2(q[0].w, q[1].w);
+	}
+#pragma unroll
+	for (int i = 0; i < TPT; ++i) { hi[i * NT + tid] = 0.f; lo[i * NT + tid] = 0.f; }
+	auto tile_fn = [&](const float4* __restrict__ st, int cnt) {
+		float2 acc[H];
+#pragma unroll
+		for (int h = 0; h < H; ++h) acc[h] = make_float2(0.f, 0.f);
+		auto body = [&](int j) {
+			const float4 s = st[j];
+			const float2 sx = bc2(s.x), sy = bc2(s.y), sg = bc2(s.z), sa = bc2(s.w);
+#pragma unroll
+			for (int h = 0; h < H; ++h) {
+				const float2 dx = __fadd2_rn(sx, ntx[h]);
+				const float2 dy = __fadd2_rn(sy, nty[h]);
+				const float2 r2 = __ffma2_rn(dy, dy, __fmul2_rn(dx, dx));
+				float2 e = RegEta2D2<R>::eta2(r2, rc);
+				e.x = r2.x > 0.f ? e.x : 0.f;
+				e.y = r2.y > 0.f ? e.y : 0.f;
+				// Gamma_s A_t - Gamma_t A_s
+				const float2 w = __ffma2_rn(sg, ta[h], __fmul2_rn(ntg[h], sa));
+				acc[h] = __ffma2_rn(e, w, acc[h]);
+			}
+		};
+		if (cnt == kTile) {
+#pragma unroll 4
+			for (int j = 0; j < kTile; ++j) body(j);
+		} else {
+#pragma unroll 1
+			for (int j = 0; j < cnt; ++j) body(j);
+		}
+#pragma unroll
+		for (int h = 0; h < H; ++h)
+#pragma unroll
+			for (int e = 0; e < 2; ++e) {
+				const int i = (2 * h + e) * NT + tid;
+				float hv = hi[i], lv = lo[i];
+				fold_twosum(hv, lv, e == 0 ? acc[h].x : acc[h].y);
+				hi[i] = hv; lo[i] = lv;
+			}
+	};
+	if (!Stream1::run(smem, p.src, s_begin, n_s, err, tile_fn)) return;
+#pragma unroll
+	for (int k = 0; k < TPT; ++k) {
+		const int t = tbase + k * NT + tid;
+		if (t >= p.n_tgt) continue;
+		const int i = k * NT + tid;
+		const double sum = double(hi[i]) + double(lo[i]);
+		if (gridDim.y == 1) p.out[t] = float(scale * sum);
+		else partial[size_t(blockIdx.y) * p.n_tgt + t] = sum;
+	}
+}
+
 template <int NC>
 __global__ void finalize_scaled(float* __restrict__ out, int n_tgt,
 	const double* __restrict__ partial, int n_split, double scale)
@@ -327,22 +408,28 @@ cudaError_t launch_vel(const P2DVelProblem& p, const LaunchEnv& env) {
 	return cudaGetLastError();
 }
 
-template <Reg R, int TPT, int NT>
+template <Reg R, int TPT, int NT, bool PK>
+auto visc_kernel() {
+	if constexpr (PK) return p2d_visc2_kernel<R, TPT, NT>;
+	else return p2d_visc_kernel<R, TPT, NT>;
+}
+
+template <Reg R, int TPT, int NT, bool PK>
 Plan plan_visc(int n_src, int n_tgt, int num_sms, int max_split = 64) {
 	constexpr size_t smem = smem_bytes<TPT, NT, 1>();
-	static const int occ = resident_ctas(p2d_visc_kernel<R, TPT, NT>, NT, smem);
+	static const int occ = resident_ctas(visc_kernel<R, TPT, NT, PK>(), NT, smem);
 	return make_plan(n_src, n_tgt, TPT * NT, kTile, 1, num_sms * occ, smem, max_split);
 }
 
-template <Reg R, int TPT, int NT>
+template <Reg R, int TPT, int NT, bool PK>
 cudaError_t launch_visc(const P2DViscProblem& p, const LaunchEnv& env) {
-	const Plan pl = plan_visc<R, TPT, NT>(p.n_src, p.n_tgt, env.num_sms,
+	const Plan pl = plan_visc<R, TPT, NT, PK>(p.n_src, p.n_tgt, env.num_sms,
 		env.cap_to_ws ? split_cap_for(env.ws_bytes, 1, p.n_tgt) : 64);
 	if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
 	const RegConsts rc = make_reg_consts_host(p.sigma);
 	const double scale = 2.0 * double(p.nu) / (double(p.sigma) * double(p.sigma));
 	double* partial = static_cast<double*>(env.ws);
-	p2d_visc_kernel<R, TPT, NT><<<dim3(pl.n_tblocks, pl.n_split), NT, pl.smem, env.stream>>>(
+	visc_kernel<R, TPT, NT, PK>()<<<dim3(pl.n_tblocks, pl.n_split), NT, pl.smem, env.stream>>>(
 		p, rc, scale, partial, pl.src_per_split, env.err);
 	count_launch();
 	if (pl.n_split > 1) {
@@ -398,12 +485,13 @@ cudaError_t vel_r(const P2DVelProblem& p, const LaunchEnv& env) {
 }
 template <Reg R>
 size_t ws_visc_r(int n_src, int n_tgt, int num_sms) {
-	return n_tgt < kSmallTargets ? plan_visc<R, 1, 128>(n_src, n_tgt, num_sms).ws_bytes
-	                             : plan_visc<R, 4, 128>(n_src, n_tgt, num_sms).ws_bytes;
+	return n_tgt < kSmallTargets ? plan_visc<R, 1, 128, false>(n_src, n_tgt, num_sms).ws_bytes
+	                             : plan_visc<R, 4, 128, true>(n_src, n_tgt, num_sms).ws_bytes;
 }
 template <Reg R>
 cudaError_t visc_r(const P2DViscProblem& p, const LaunchEnv& env) {
-	return p.n_tgt < kSmallTargets ? launch_visc<R, 1, 128>(p, env) : launch_visc<R, 4, 128>(p, env);
+	return p.n_tgt < kSmallTargets ? launch_visc<R, 1, 128, false>(p, env)
+	                               : launch_visc<R, 4, 128, true>(p, env);
 }
 
 }  // namespace

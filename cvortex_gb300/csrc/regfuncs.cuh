@@ -368,6 +368,28 @@ template <> struct RegEta2<Reg::Gaussian> {
 	}
 };
 
+// 2D viscous weights, packed (RegP2D<R>::eta two at a time; exp through ex2).
+template <Reg R> struct RegEta2D2;
+template <> struct RegEta2D2<Reg::Winckelmans> {
+	// 24 exp(4/a^3) / a^4, a = x2 + 1
+	__device__ __forceinline__ static float2 eta2(float2 r2, const RegConsts& c) {
+		const float2 a = __ffma2_rn(r2, bc2(c.inv_s2), bc2(1.f));
+		const float2 ra = make_float2(rcp_approx(a.x), rcp_approx(a.y));
+		const float2 ra1 = __fmul2_rn(ra, __ffma2_rn(make_float2(-a.x, -a.y), ra, bc2(2.f)));
+		const float2 ra2 = __fmul2_rn(ra1, ra1);
+		const float2 ra4 = __fmul2_rn(ra2, ra2);
+		const float2 x = __fmul2_rn(__fmul2_rn(ra2, ra1), bc2(4.f * 1.4426950408889634f));
+		const float2 e = make_float2(ex2_approx(x.x), ex2_approx(x.y));
+		return __fmul2_rn(__fmul2_rn(bc2(24.f), e), ra4);
+	}
+};
+template <> struct RegEta2D2<Reg::Gaussian> {
+	__device__ __forceinline__ static float2 eta2(float2 r2, const RegConsts& c) {
+		const float2 a = __fmul2_rn(r2, bc2(c.exp2_half));
+		return make_float2(ex2_approx(a.x), ex2_approx(a.y));
+	}
+};
+
 // ---- 2D, packed (two targets per f32x2 lane pair) ----------------------------
 // 1/x from rcp refined by one Newton step, t (2 - x t): within an ulp.
 __device__ __forceinline__ float2 rcp2(float2 x) {

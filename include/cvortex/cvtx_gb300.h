@@ -93,6 +93,10 @@ CVTX_EXPORT int cvtx_gb300_dev_P3D_M2M_visc(const void* src, int n_src,
 CVTX_EXPORT int cvtx_gb300_dev_P2D_M2M_vel(const void* src, int n_src,
 	const void* tgt, int n_tgt, float* out, int reg,
 	float regularisation_radius, void* stream);
+/* P2D viscous exchange (zeros for singular / planetary, which have no eta). */
+CVTX_EXPORT int cvtx_gb300_dev_P2D_M2M_visc(const void* src, int n_src,
+	const void* tgt, int n_tgt, float* out, int reg,
+	float regularisation_radius, float kinematic_visc, void* stream);
 CVTX_EXPORT int cvtx_gb300_dev_F3D_M2M_vel(const void* fil, int n_fil,
 	const void* tgt, int tgt_stride, int n_tgt, float* out, void* stream);
 /* Stretching of P3D particles (records, tgt_stride >= 2) by filaments. */

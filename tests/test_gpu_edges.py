@@ -176,6 +176,9 @@ def test_packed_p2d_f3d_ragged_sizes(gpu, n):
     for reg in ("singular", "winckelmans", "gaussian", "planetary"):
         got = gpu.p2d_vel(q, q["coord"], reg, 0.05)
         close(got[idx], oracle.p2d_vel(q, q["coord"][idx], reg, 0.05))
+    for reg in ("winckelmans", "gaussian"):
+        got = gpu.p2d_visc(q, q, reg, 0.05, 1e-3, same=True)
+        close(got[idx], oracle.p2d_visc(q, q[idx], reg, 0.05, 1e-3))
     f = workloads.wake_sheet(3000, seed=10)
     pts = workloads.sheet_targets(n, seed=11)
     pts[:40] = f["start"][:40]
