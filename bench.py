@@ -382,9 +382,18 @@ def timed_dev(fn, torch, reps):
     return a.elapsed_time(b) / reps
 
 
+def measured_hbm_gbs():
+    """HBM copy bandwidth measured on this machine (generated file), or None."""
+    try:
+        return float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
+    except (OSError, ValueError, KeyError):
+        return None
+
+
 def extras(cv, lib, args, torch, sh, peak):
     """Per-op rates on the scale-up workloads and the 1M-particle target."""
     from cvortex_gb300 import workloads
+    hbm_peak = measured_hbm_gbs()
     res = {}
     n = args.n
     p = workloads.vortex_ring(n)
@@ -446,6 +455,20 @@ def extras(cv, lib, args, torch, sh, peak):
     ms = timed_dev(f, torch, 5)
     res["f3d_sheet100k_vel"] = {"ginter_s": nf * nf / ms / 1e6,
                                 "fp32_frac": 51 * nf * nf / (ms * 1e-3) / 1e12 / peak}
+    # influence matrix: write-bound (4 B per entry); 25,000 points x 20,000 filaments
+    nm, ni = 25_000, 20_000
+    dirs = np.zeros((nm, 4), np.float32)
+    dirs[:, 2] = 1.0
+    dd = torch.from_numpy(dirs).cuda()
+    om = torch.empty((nm, ni), dtype=torch.float32, device="cuda")
+    f = lambda: lib.cvtx_gb300_dev_F3D_inf_mtrx(rfd.data_ptr(), ni, tfd.data_ptr(), dd.data_ptr(),
+                                                nm, om.data_ptr(), sh)
+    ms = timed_dev(f, torch, 5)
+    gbs = 4.0 * nm * ni / (ms * 1e-3) / 1e9
+    res["f3d_inf_mtrx_25kx20k"] = {"ms": ms, "write_gbs": gbs,
+                                   "hbm_frac": gbs / hbm_peak if hbm_peak else None,
+                                   "hbm_peak_gbs": hbm_peak}
+    del om
     cube = workloads.uniform_cube(nf, seed=12)
     rc = torch.from_numpy(p3d_records(cube).reshape(nf, 8)).cuda()
     f = lambda: lib.cvtx_gb300_dev_F3D_M2M_dvort(rfd.data_ptr(), nf, rc.data_ptr(), 2, nf,

@@ -160,6 +160,7 @@ _EXT_SIGS = {
     "cvtx_gb300_dev_P3D_M2M_visc": (_i, [_vp, _i, _vp, _i, _i, _vp, _i, _f, _f, _vp]),
     "cvtx_gb300_dev_P2D_M2M_vel": (_i, [_vp, _i, _vp, _i, _vp, _i, _f, _vp]),
     "cvtx_gb300_dev_P2D_M2M_visc": (_i, [_vp, _i, _vp, _i, _vp, _i, _f, _f, _vp]),
+    "cvtx_gb300_dev_F3D_inf_mtrx": (_i, [_vp, _i, _vp, _vp, _i, _vp, _vp]),
     "cvtx_gb300_dev_F3D_M2M_vel": (_i, [_vp, _i, _vp, _i, _i, _vp, _vp]),
     "cvtx_gb300_dev_F3D_M2M_dvort": (_i, [_vp, _i, _vp, _i, _i, _vp, _vp]),
     "cvtx_gb300_dev_P3D_M2M_noalloc": (_i, [_vp, _i, _vp, _i, _i, _vp, _vp, _i, _f, _vp]),

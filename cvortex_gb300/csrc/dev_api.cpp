@@ -192,6 +192,21 @@ CVTX_EXPORT int cvtx_gb300_dev_F3D_M2M_dvort(const void* fil, int n_fil, const v
 	return c.done(f3d_dvort(p, c.env()), "cvtx_gb300_dev_F3D_M2M_dvort");
 }
 
+CVTX_EXPORT int cvtx_gb300_dev_F3D_inf_mtrx(const void* fil, int n_fil, const void* mes,
+	const void* dir, int n_mes, float* out, void* stream)
+{
+	if (n_mes <= 0 || n_fil <= 0) return 0;
+	if (!fil || !mes || !dir || !out) return -1;
+	DevCall c(stream);
+	if (!c.ctx) return -3;
+	F3DInfProblem p;
+	p.fil = static_cast<const float4*>(fil); p.n_fil = n_fil;
+	p.mes = static_cast<const float4*>(mes); p.n_mes = n_mes;
+	p.dir = static_cast<const float4*>(dir);
+	p.out = out;
+	return c.done(f3d_inf_mtrx(p, c.env()), "cvtx_gb300_dev_F3D_inf_mtrx");
+}
+
 CVTX_EXPORT int cvtx_gb300_dev_pack_P3D(const cvtx_P3D* aos, int n, void* rec, void* stream) {
 	if (n < 0 || (n > 0 && (!aos || !rec))) return -1;
 	return pack_p3d(aos, n, static_cast<float4*>(rec), static_cast<cudaStream_t>(stream)) ==

@@ -93,6 +93,10 @@ CVTX_EXPORT int cvtx_gb300_dev_P3D_M2M_visc(const void* src, int n_src,
 CVTX_EXPORT int cvtx_gb300_dev_P2D_M2M_vel(const void* src, int n_src,
 	const void* tgt, int n_tgt, float* out, int reg,
 	float regularisation_radius, void* stream);
+/* Filament influence matrix: out[i * n_fil + j] = vel_j(mes_i) . dir_i
+ * (mes, dir: point records). */
+CVTX_EXPORT int cvtx_gb300_dev_F3D_inf_mtrx(const void* fil, int n_fil,
+	const void* mes, const void* dir, int n_mes, float* out, void* stream);
 /* P2D viscous exchange (zeros for singular / planetary, which have no eta). */
 CVTX_EXPORT int cvtx_gb300_dev_P2D_M2M_visc(const void* src, int n_src,
 	const void* tgt, int n_tgt, float* out, int reg,

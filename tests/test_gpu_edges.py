@@ -201,3 +201,24 @@ def test_packed_f3d_dvort(gpu, n):
     assert np.all(np.isfinite(got))
     sel = np.r_[0:128, n - 64:n]
     close(got[sel], oracle.f3d_dvort(f, p[sel]))
+
+
+def test_dev_inf_mtrx_matches_abi(gpu):
+    import torch
+    f = workloads.wake_sheet(333, seed=14)
+    pts = workloads.sheet_targets(257, seed=15)
+    dirs = np.random.Generator(np.random.PCG64(16)).normal(size=(257, 3)).astype(np.float32)
+    ref = gpu.f3d_inf_mtrx(f, pts, dirs)
+    rf = np.zeros((len(f), 8), np.float32)
+    rf[:, 0:3], rf[:, 3], rf[:, 4:7] = f["start"], f["strength"], f["end"]
+    mp = np.zeros((257, 4), np.float32)
+    mp[:, :3] = pts
+    dp = np.zeros((257, 4), np.float32)
+    dp[:, :3] = dirs
+    a, m, d = (torch.from_numpy(x).cuda() for x in (rf, mp, dp))
+    out = torch.empty((257, len(f)), dtype=torch.float32, device="cuda")
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert gpu.lib.cvtx_gb300_dev_F3D_inf_mtrx(a.data_ptr(), len(f), m.data_ptr(), d.data_ptr(),
+                                               257, out.data_ptr(), stream) == 0
+    assert gpu.lib.cvtx_gb300_dev_status(stream) == 0
+    np.testing.assert_array_equal(out.cpu().numpy(), ref)
