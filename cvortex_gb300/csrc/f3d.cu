@@ -544,6 +544,69 @@ __global__ void f3d_inf_kernel(const F3DInfProblem p)
 	}
 }
 
+// Tiled influence matrix: a CTA covers kInfRows points x kInfFils filaments;
+// the filament tile sits in shared memory, and each thread evaluates
+// kInfPairs pairs of points (f32x2) against four consecutive filaments held
+// in registers, storing float4 runs, so a warp writes 512 contiguous bytes of
+// each of its rows.
+constexpr int kInfFils = 128;                 // 32 threads x 4 filaments
+constexpr int kInfPairs = 4;                  // point pairs per thread
+constexpr int kInfRows = 8 * 2 * kInfPairs;   // 8 threads x 2 points x kInfPairs
+constexpr int kInfThreads = 256;
+
+__global__ void __launch_bounds__(kInfThreads) f3d_inf2_kernel(const F3DInfProblem p)
+{
+	__shared__ float4 fs[2 * kInfFils];
+	const int tx = threadIdx.x & 31;          // filament quad
+	const int ty = threadIdx.x >> 5;          // point-pair lane
+	const int j_base = blockIdx.y * kInfFils;
+	for (int k = threadIdx.x; k < 2 * kInfFils; k += kInfThreads) {
+		const int j = j_base + (k >> 1);
+		fs[k] = j < p.n_fil ? p.fil[2 * size_t(j) + (k & 1)] : make_float4(0.f, 0.f, 0.f, 0.f);
+	}
+	__syncthreads();
+	const int j0 = j_base + 4 * tx;
+	if (j0 >= p.n_fil) return;
+	float4 fa[4], fb[4];
+#pragma unroll
+	for (int q = 0; q < 4; ++q) { fa[q] = fs[2 * (4 * tx + q)]; fb[q] = fs[2 * (4 * tx + q) + 1]; }
+	const bool vec = (p.n_fil & 3) == 0 && j0 + 3 < p.n_fil &&
+		(reinterpret_cast<uintptr_t>(p.out) & 15u) == 0;
+#pragma unroll 1
+	for (int k = 0; k < kInfPairs; ++k) {
+		const long long i0 = (long long)blockIdx.x * kInfRows + 2 * (ty + 8 * k);
+		if (i0 >= p.n_mes) break;
+		const int ia = int(i0);
+		const int ib = int(i0 + 1 < p.n_mes ? i0 + 1 : i0);
+		const float4 ma = p.mes[ia], mb = p.mes[ib];
+		const float4 da = p.dir[ia], db = p.dir[ib];
+		const float2 mx = make_float2(ma.x, mb.x), my = make_float2(ma.y, mb.y);
+		const float2 mz = make_float2(ma.z, mb.z);
+		const float2 dx = make_float2(da.x, db.x), dy = make_float2(da.y, db.y);
+		const float2 dz = make_float2(da.z, db.z);
+		float2 r[4];
+#pragma unroll
+		for (int q = 0; q < 4; ++q) {
+			float2 vx, vy, vz;
+			f3d_vel_pair2(mx, my, mz, fa[q], fb[q], vx, vy, vz);
+			r[q] = __ffma2_rn(vz, dz, __ffma2_rn(vy, dy, __fmul2_rn(vx, dx)));
+		}
+#pragma unroll
+		for (int e = 0; e < 2; ++e) {
+			if (e == 1 && i0 + 1 >= p.n_mes) break;
+			float* row = p.out + size_t(i0 + e) * p.n_fil;
+			const float v[4] = {e ? r[0].y : r[0].x, e ? r[1].y : r[1].x,
+				e ? r[2].y : r[2].x, e ? r[3].y : r[3].x};
+			if (vec) {
+				*reinterpret_cast<float4*>(row + j0) = make_float4(v[0], v[1], v[2], v[3]);
+			} else {
+#pragma unroll
+				for (int q = 0; q < 4; ++q) if (j0 + q < p.n_fil) row[j0 + q] = v[q];
+			}
+		}
+	}
+}
+
 template <int TPT, int NT>
 constexpr size_t smem_bytes() {
 	return Stream2::kSmemBytes + size_t(2) * 3 * TPT * NT * sizeof(float);
@@ -657,10 +720,18 @@ cudaError_t f3d_dvort(const F3DDvortProblem& p, const LaunchEnv& env) {
 }
 cudaError_t f3d_inf_mtrx(const F3DInfProblem& p, const LaunchEnv& env) {
 	if (p.n_mes <= 0 || p.n_fil <= 0) return cudaSuccess;
-	const long long items = (long long)((p.n_fil + 3) / 4) * p.n_mes;
-	const long long want = (items + 255) / 256;
-	const int blocks = int(want < (long long)env.num_sms * 32 ? want : (long long)env.num_sms * 32);
-	f3d_inf_kernel<<<blocks, 256, 0, env.stream>>>(p);
+	const long long row_tiles = (p.n_mes + kInfRows - 1) / kInfRows;
+	const long long fil_tiles = (p.n_fil + kInfFils - 1) / kInfFils;
+	if (fil_tiles <= 65535 && row_tiles <= 0x7fffffffLL) {
+		f3d_inf2_kernel<<<dim3(unsigned(row_tiles), unsigned(fil_tiles)), kInfThreads, 0,
+			env.stream>>>(p);
+	} else {
+		// more than 8.4M filaments: the grid-stride form
+		const long long items = (long long)((p.n_fil + 3) / 4) * p.n_mes;
+		const long long want = (items + 255) / 256;
+		const int blocks = int(want < (long long)env.num_sms * 32 ? want : (long long)env.num_sms * 32);
+		f3d_inf_kernel<<<blocks, 256, 0, env.stream>>>(p);
+	}
 	count_launch();
 	return cudaGetLastError();
 }
