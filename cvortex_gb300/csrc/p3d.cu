@@ -245,20 +245,21 @@ p3d_induce_kernel(const P3DInduceProblem p, const InduceConsts kc,
 
 // Packed variant of p3d_induce_kernel (two targets per f32x2 lane pair; see
 // induce2_block in p3d_induce.cuh). CTA (x, y) = (target block, source split).
-template <Reg R, bool VEL, bool DV, int TPT, int NT, int UNROLL>
-__global__ void __launch_bounds__(NT)
+template <Reg R, bool VEL, bool DV, int TPT, int NT, int UNROLL, int TILE, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
 p3d_induce2_kernel(const P3DInduceProblem p, const InduceConsts kc,
 	double* __restrict__ partial, int src_per_split, unsigned* err)
 {
 	constexpr int NC = InduceNC<VEL, DV>::value;
 	extern __shared__ __align__(16) unsigned char smem[];
-	if (!P3DStream::init(smem, err)) return;
+	if (!P3DStreamT<TILE>::init(smem, err)) return;
 	unsigned tcount = 0;
 	const int s_begin = blockIdx.y * src_per_split;
 	int n_s = p.n_src - s_begin;
 	n_s = n_s < src_per_split ? n_s : src_per_split;
 	n_s = n_s > 0 ? n_s : 0;
-	induce2_block<R, VEL, DV, TPT, NT, UNROLL>(p, kc, blockIdx.x * (TPT * NT), s_begin, n_s, smem, err,
+	induce2_block<R, VEL, DV, TPT, NT, UNROLL, TILE>(p, kc, blockIdx.x * (TPT * NT), s_begin, n_s,
+		smem, err,
 		tcount, [&](int t, const double* acc, float ax, float ay, float az) {
 			if (gridDim.y == 1) {
 				write_induce<VEL, DV>(p, kc, t, acc, ax, ay, az);
@@ -624,16 +625,19 @@ constexpr CfgSpec kCfg[] = {
 	{4, 128, true},  {2, 128, true},
 };
 // Configurations 7-9 repeat shapes with another source-loop unroll factor
-// (7: 1, 8 and 9: 4; all others 2).
+// (7: 1, 8 and 9: 4; all others 2). (Forcing five resident CTAs per SM with
+// 96-source tiles spilled registers and ran 20-30 % slower on a GB300.)
 constexpr int kNumCfg = int(sizeof(kCfg) / sizeof(kCfg[0]));
 
-template <Reg R, bool VEL, bool DV, int TPT, int NT, bool PK, int UNROLL = 2>
+template <Reg R, bool VEL, bool DV, int TPT, int NT, bool PK, int UNROLL = 2,
+	int TILE = kTile, int MINB = 1>
 struct InduceVariant {
 	static constexpr int NC = (VEL ? 3 : 0) + (DV ? 6 : 0);
-	static constexpr size_t kSmem = smem_bytes<TPT, NT, NC>();
+	static constexpr size_t kSmem = PK ? induce_smem_bytes<TPT, NT, NC, TILE>()
+	                                   : smem_bytes<TPT, NT, NC>();
 	using Fn = void (*)(const P3DInduceProblem, const InduceConsts, double*, int, unsigned*);
 	static Fn fn() {
-		if constexpr (PK) return p3d_induce2_kernel<R, VEL, DV, TPT, NT, UNROLL>;
+		if constexpr (PK) return p3d_induce2_kernel<R, VEL, DV, TPT, NT, UNROLL, TILE, MINB>;
 		else return p3d_induce_kernel<R, VEL, DV, TPT, NT>;
 	}
 	static int occupancy() {
@@ -641,7 +645,8 @@ struct InduceVariant {
 		return occ;
 	}
 	static Plan plan(int n_src, int n_tgt, int num_sms, int max_split) {
-		return make_plan(n_src, n_tgt, TPT * NT, kTile, NC, num_sms * occupancy(), kSmem, max_split);
+		return make_plan(n_src, n_tgt, TPT * NT, PK ? TILE : kTile, NC, num_sms * occupancy(), kSmem,
+			max_split);
 	}
 	static cudaError_t launch(const Plan& pl, const P3DInduceProblem& p, const LaunchEnv& env) {
 		if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;

@@ -22,7 +22,8 @@
 namespace cvtx {
 
 constexpr int kP3DTile = 256;
-using P3DStream = TileStream<2, kP3DTile, 2>;
+template <int TILE> using P3DStreamT = TileStream<2, TILE, 2>;
+using P3DStream = P3DStreamT<kP3DTile>;
 
 template <Reg R> struct FiniteAtZero { static constexpr bool value = true; };
 template <> struct FiniteAtZero<Reg::Singular> { static constexpr bool value = false; };
@@ -39,9 +40,9 @@ struct InduceConsts {
 InduceConsts make_induce_consts(int reg, float sigma);
 
 // Shared memory of one CTA: tile stages + barriers + (hi, lo) per target and sum.
-template <int TPT, int NT, int NC>
+template <int TPT, int NT, int NC, int TILE = kP3DTile>
 constexpr size_t induce_smem_bytes() {
-	return P3DStream::kSmemBytes + size_t(2) * NC * TPT * NT * sizeof(float);
+	return P3DStreamT<TILE>::kSmemBytes + size_t(2) * NC * TPT * NT * sizeof(float);
 }
 
 template <bool VEL, bool DV>
@@ -76,7 +77,8 @@ __device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y
 // P3DStream::init; `tcount` carries the stage phase across calls). For every
 // valid target calls sink(t, sums[NC], alpha_t). Returns false if the tile
 // pipeline timed out (results were not produced).
-template <Reg R, bool VEL, bool DV, int TPT, int NT, int UNROLL = 2, class Sink>
+template <Reg R, bool VEL, bool DV, int TPT, int NT, int UNROLL = 2, int TILE = kP3DTile,
+	class Sink>
 __device__ __forceinline__ bool induce2_block(const P3DInduceProblem& p, const InduceConsts& kc,
 	int tbase, int s_begin, int n_s, unsigned char* smem, unsigned* err, unsigned& tcount,
 	Sink&& sink)
@@ -86,7 +88,8 @@ __device__ __forceinline__ bool induce2_block(const P3DInduceProblem& p, const I
 	constexpr int NC = InduceNC<VEL, DV>::value;
 	constexpr int NR = (VEL ? (DV ? 6 : 3) : 0) + (DV ? 6 : 0);
 	constexpr bool kFinite = FiniteAtZero<R>::value;
-	float* hi = reinterpret_cast<float*>(smem + P3DStream::kSmemBytes);
+	using Stream = P3DStreamT<TILE>;
+	float* hi = reinterpret_cast<float*>(smem + Stream::kSmemBytes);
 	float* lo = hi + NC * TPT * NT;
 	const int tid = threadIdx.x;
 	const RegConsts rc = kc.rc;
@@ -177,9 +180,9 @@ __device__ __forceinline__ bool induce2_block(const P3DInduceProblem& p, const I
 				acc[o + 5][h] = __ffma2_rn(kk, dz, acc[o + 5][h]);
 			}
 		};
-		if (cnt == kP3DTile) {
+		if (cnt == TILE) {
 #pragma unroll (UNROLL)
-			for (int j = 0; j < kP3DTile; ++j) body(j);
+			for (int j = 0; j < TILE; ++j) body(j);
 		} else {
 #pragma unroll 1
 			for (int j = 0; j < cnt; ++j) body(j);
@@ -210,7 +213,7 @@ __device__ __forceinline__ bool induce2_block(const P3DInduceProblem& p, const I
 		}
 	};
 
-	if (!P3DStream::run_continue(smem, p.src, s_begin, n_s, err, tcount, tile_fn)) return false;
+	if (!Stream::run_continue(smem, p.src, s_begin, n_s, err, tcount, tile_fn)) return false;
 
 #pragma unroll
 	for (int h = 0; h < H; ++h) {
