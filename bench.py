@@ -45,8 +45,9 @@ os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 METRIC = "P3D M2M vel+dvort Ginteractions/s"
 UNIT = "Ginteractions/s"
-# Canonical flops per interaction (add/sub/mul 1, FMA 2; special functions 0):
-# Winckelmans vel 30, dvort 46, fused 61.
+# Canonical flops per interaction (add/sub/mul 1, FMA 2; special functions,
+# compares and selects 0; per-call host constants excluded), by op and
+# regularisation id (0 singular, 1 Winckelmans, 2 planetary, 3 Gaussian).
 FLOPS = {("vel", 1): 30, ("dvort", 1): 46, ("veldvort", 1): 61,
          ("vel", 0): 25, ("dvort", 0): 39, ("veldvort", 0): 49,
          ("vel", 2): 25, ("dvort", 2): 39, ("veldvort", 2): 49,

@@ -1,6 +1,5 @@
 """GPU parity: the CUDA path, called through the C ABI, against the oracle
-and the golden fixtures. Bar (the benchmark spec): relative L2 error <= 1e-5 per
-output array. Every result's error against the FP64 exact oracle is checked
+and the golden fixtures. Bar: relative L2 error <= 1e-5 per output array. Every result's error against the FP64 exact oracle is checked
 too.
 
 Gaussian regularisation: below rho_c the kernels use the exact series where
