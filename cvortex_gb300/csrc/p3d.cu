@@ -723,7 +723,7 @@ int env_cfg() {
 constexpr signed char kMidCfg[4][4] = {
 	{2, 3, 5, 3}, {2, 3, 0, 2}, {2, 3, 0, 2}, {2, 6, 5, 3}};
 constexpr signed char kLargeCfg[4][4] = {
-	{2, 3, 5, 3}, {2, 8, 6, 2}, {2, 4, 2, 2}, {2, 8, 5, 9}};
+	{2, 3, 5, 3}, {2, 6, 6, 2}, {2, 4, 2, 2}, {2, 6, 4, 9}};
 
 int choose_cfg(int reg, unsigned ops, int n_tgt) {
 	const int forced = env_cfg();

@@ -123,13 +123,14 @@ __device__ __forceinline__ bool induce2_block(const P3DInduceProblem& p, const I
 		auto body = [&](int j) {
 			const float4 sp = st[2 * j];
 			const float4 sv = st[2 * j + 1];
-			const float2 nsx = bc2(-sp.x), nsy = bc2(-sp.y), nsz = bc2(-sp.z);
+			const float2 sx = bc2(sp.x), sy = bc2(sp.y), sz = bc2(sp.z);
 			const float2 wx = bc2(sv.x), wy = bc2(sv.y), wz = bc2(sv.z);
 #pragma unroll
 			for (int h = 0; h < H; ++h) {
-				const float2 dx = __fadd2_rn(tx[h], nsx);
-				const float2 dy = __fadd2_rn(ty[h], nsy);
-				const float2 dz = __fadd2_rn(tz[h], nsz);
+				// d = t - s as s * (-1) + t: one rounding, no per-source negation
+				const float2 dx = __ffma2_rn(sx, bc2(-1.f), tx[h]);
+				const float2 dy = __ffma2_rn(sy, bc2(-1.f), ty[h]);
+				const float2 dz = __ffma2_rn(sz, bc2(-1.f), tz[h]);
 				const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
 				if (!DV) {
 					// c = d x alpha_s
