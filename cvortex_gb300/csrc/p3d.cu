@@ -625,8 +625,9 @@ constexpr CfgSpec kCfg[] = {
 	{4, 128, true},  {2, 128, true},
 };
 // Configurations 7-9 repeat shapes with another source-loop unroll factor
-// (7: 1, 8 and 9: 4; all others 2). (Forcing five resident CTAs per SM with
-// 96-source tiles spilled registers and ran 20-30 % slower on a GB300.)
+// (7: 1, 8 and 9: 4; all others 2). (Also timed on a GB300 and left out:
+// five resident CTAs per SM with 96-source tiles, which spilled registers and
+// ran 20-30 % slower, and 6 x 128 / 8 x 64 blocking, within 2 % of these.)
 constexpr int kNumCfg = int(sizeof(kCfg) / sizeof(kCfg[0]));
 
 template <Reg R, bool VEL, bool DV, int TPT, int NT, bool PK, int UNROLL = 2,
