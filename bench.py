@@ -315,7 +315,6 @@ def run_ours(args):
     if rank == 0 and not args.quick:
         out["e2e"] = e2e_abi(cv, p, args)
         out["serving"] = serve_extra(cv, lib, count=args.serve_requests)
-        out["precision"] = precision_extra(lib, torch, sh)
         out["extras"] = extras(cv, lib, args, torch, sh, peak.value)
     if rank == 0 and world == 1:
         out["cpu_baseline"] = cpu_baseline(p, args.reg)
@@ -598,62 +597,6 @@ def batch_extra(cv, lib, torch, sh, count=512):
             "tuned_shape": [tpt.value, nt.value],
             "tuned_chunk": chunk.value, "items": items.value, "graph": bool(graph.value),
             "tune_s": tune_s}
-
-
-def precision_extra(lib, torch, sh, n=1_000_000, sigma=0.01, n_random=6144, n_twin=1024,
-                    n_ref=2048):
-    """Gaussian vel + dvort at N = 1M (uniform cube, sigma 0.01, 1% of the
-    particles are twins at separation < 1e-3 sigma): the GPU path over all
-    targets, checked on a seeded sample against the FP64 oracle (exact erf,
-    series below rho = 0.5) over all sources. The sample holds n_random
-    random targets plus n_twin twins and their originals (about 8,000); the
-    reference formulation is evaluated on a random n_ref of them. Reported per
-    output: relative L2 and max relative error (per target vector, over
-    targets whose FP64 value exceeds 1e-6 of the sample's RMS) of the GPU
-    and of the reference CPU formulation (oracle restatement, FP32 pairs with
-    the reference's erf) against FP64."""
-    import oracle
-    from cvortex_gb300 import workloads
-    from oracle import exact
-    p = workloads.cube_with_twins(n, sigma)
-    rec = torch.from_numpy(p3d_records(p).reshape(n, 8)).cuda()
-    vel = torch.empty((n, 3), dtype=torch.float32, device="cuda")
-    dv = torch.empty((n, 3), dtype=torch.float32, device="cuda")
-    t0 = time.perf_counter()
-    rc = lib.cvtx_gb300_dev_P3D_M2M(rec.data_ptr(), n, rec.data_ptr(), 2, n, vel.data_ptr(),
-                                    dv.data_ptr(), REG["gaussian"], sigma, sh)
-    torch.cuda.synchronize()
-    gpu_s = time.perf_counter() - t0
-    if rc != 0 or lib.cvtx_gb300_dev_status(sh) != 0:
-        raise RuntimeError("precision run failed")
-    rng = np.random.Generator(np.random.PCG64(11))
-    k = int(n * 0.01)
-    twins = rng.choice(k, n_twin, replace=False)
-    idx = np.unique(np.concatenate([rng.choice(n, n_random, replace=False), n - k + twins, twins]))
-    sub = p[idx].copy()
-    v_gpu = vel.cpu().numpy()[idx]
-    d_gpu = dv.cpu().numpy()[idx]
-    t0 = time.perf_counter()
-    v64, d64 = oracle.exact_p3d_vel_dvort(p, sub["coord"], sub["vorticity"], "gaussian", sigma)
-    fp64_s = time.perf_counter() - t0
-    # the reference formulation on a random n_ref of the sample targets (CPU time)
-    rsel = np.sort(rng.choice(len(idx), min(n_ref, len(idx)), replace=False))
-    rsub = sub[rsel].copy()
-    v_ref = oracle.p3d_vel(p, rsub["coord"], "gaussian", sigma)
-    d_ref = oracle.p3d_dvort(p, rsub, "gaussian", sigma)
-
-    def errs(a, b):
-        rms = float(np.sqrt(np.mean(np.sum(np.asarray(b) ** 2, axis=1))))
-        return {"rel_l2": exact.rel_l2(a, b), "max_rel": exact.max_rel(a, b, floor=1e-6 * rms)}
-
-    return {"workload": f"uniform cube N={n}, 1% twins at < 1e-3 sigma, gaussian, sigma={sigma}",
-            "sample_targets": int(len(idx)), "gpu_all_targets_s": gpu_s, "fp64_oracle_s": fp64_s,
-            "reference_sample_targets": int(len(rsub)),
-            "vel": {"gpu_vs_fp64": errs(v_gpu, v64),
-                    "reference_vs_fp64": errs(v_ref, v64[rsel])},
-            "dvort": {"gpu_vs_fp64": errs(d_gpu, d64),
-                      "reference_vs_fp64": errs(d_ref, d64[rsel])},
-            "rho_c": float(lib.cvtx_gb300_gaussian_rho_c())}
 
 
 SERVE_RATES = (100, 300, 1000, 3000, 5000)
