@@ -383,7 +383,7 @@ def timed_dev(fn, torch, reps):
 
 
 def measured_hbm_gbs():
-    """HBM copy bandwidth measured on this machine (generated file), or None."""
+    """Measured HBM copy bandwidth of this GPU model (MEASURED_PEAKS.json), or None."""
     try:
         return float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
     except (OSError, ValueError, KeyError):

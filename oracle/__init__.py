@@ -4,8 +4,8 @@ Three checkers for the GB300 library, none of which the product imports:
 
 * ``lib()``: ``cvtx_oracle.c``, a plain-C restatement of the reference
   cvortex CPU (OpenMP) path for the M2M interactions, built here by ``build()``
-  into ``oracle/lib/libcvtx_oracle.so``. It runs anywhere gcc runs (including
-  the Arm GPU host), so tests, the smoke check and the CPU-baseline leg of the
+  into ``oracle/lib/libcvtx_oracle.so``. It runs anywhere gcc runs (x86-64 or
+  aarch64), so tests, the smoke check and the CPU-baseline leg of the
   benchmark can use it where the reference sources are absent.
 * ``ref_lib()``: the reference library itself, compiled from the reference
   sources by ``oracle/build_ref.sh`` into ``oracle/_ref/libcvtx_ref.so`` when
@@ -13,7 +13,11 @@ Three checkers for the GB300 library, none of which the product imports:
   and generates the golden fixtures under ``tests/golden``.
 * ``oracle.exact``: the same formulas in float64 with the exact error
   function, i.e. the "error vs FP64" reference (independent of the reference
-  implementation and of FP32 rounding).
+  implementation and of FP32 rounding); ``exact_p3d_vel_dvort`` is the same
+  in compiled C for large samples.
+* ``oracle.redist``: a numpy restatement of the reference's particle
+  redistribution (parity unpinned: the reference's own build does not
+  return from those functions with GCC; see that module).
 """
 from __future__ import annotations
 
