@@ -39,6 +39,7 @@
 #include <cstring>
 #include <deque>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -62,6 +63,7 @@ constexpr size_t kSlotWsBytes = size_t(64) << 20;        // split partials per s
 constexpr size_t kStagingBytes = size_t(1) << 30;        // pinned staging arena
 constexpr size_t kDefaultMaxHbm = size_t(64) << 30;
 constexpr int kMaxLevels = 8;                              // stream priority levels used
+constexpr size_t kKeepFinished = size_t(1) << 20;          // finished records kept
 inline size_t up(size_t b) { return (b + kAlign - 1) & ~(kAlign - 1); }
 
 // First-fit range allocator over [0, cap) with coalescing of free ranges.
@@ -257,7 +259,9 @@ class Server {
 	bool stop_ = false;
 	std::thread thread_;
 	Arena dev_, host_;
-	std::unordered_map<unsigned long long, Request> reqs_;
+	// shared so that a waiter keeps its record alive when it is forgotten
+	std::unordered_map<unsigned long long, std::shared_ptr<Request>> reqs_;
+	std::deque<unsigned long long> finished_;   // oldest first
 	std::deque<unsigned long long> queue_;
 	std::vector<int> free_slots_;
 	std::deque<int> done_slots_;
@@ -390,7 +394,7 @@ unsigned long long Server::submit(const cvtx_gb300_request* r) {
 		q.t_submit = now_s();
 		if (submitted_ == 0) first_submit_ = q.t_submit;
 		++submitted_;
-		reqs_.emplace(id, q);
+		reqs_.emplace(id, std::make_shared<Request>(q));
 		queue_.push_back(id);
 	}
 	cv_.notify_all();
@@ -410,6 +414,12 @@ void Server::complete_locked(Request& q, int status) {
 		++rejected_;
 	} else {
 		++failed_;
+	}
+	// keep a bounded number of finished records for wait / request_info
+	finished_.push_back(q.id);
+	if (finished_.size() > kKeepFinished) {
+		reqs_.erase(finished_.front());
+		finished_.pop_front();
 	}
 	done_cv_.notify_all();
 }
@@ -431,7 +441,7 @@ void Server::loop() {
 
 void Server::admit(std::unique_lock<std::mutex>& lk) {
 	while (!queue_.empty() && !free_slots_.empty()) {
-		Request& q = reqs_.at(queue_.front());
+		Request& q = *reqs_.at(queue_.front());
 		if (q.L.total > dev_.cap() || q.host_bytes > host_.cap()) {
 			queue_.pop_front();
 			complete_locked(q, CVTX_GB300_ST_REJECTED);
@@ -555,7 +565,7 @@ cudaError_t Server::launch(Request& q, Slot& sl) {
 
 void Server::finish(int s, std::unique_lock<std::mutex>& lk) {
 	Slot& sl = slots_[size_t(s)];
-	Request& q = reqs_.at(sl.req);
+	Request& q = *reqs_.at(sl.req);
 	int status = CVTX_GB300_ST_DONE;
 	if (!dry_) {
 		if (sl.launch_error != cudaSuccess) {
@@ -590,7 +600,7 @@ int Server::wait(unsigned long long id, double timeout_ms) {
 	std::unique_lock<std::mutex> lk(mu_);
 	auto it = reqs_.find(id);
 	if (it == reqs_.end()) return CVTX_GB300_ST_UNKNOWN;
-	Request* q = &it->second;    // element pointers survive rehashing
+	const std::shared_ptr<Request> q = it->second;
 	auto pred = [&] { return q->status <= CVTX_GB300_ST_DONE; };
 	if (timeout_ms < 0) done_cv_.wait(lk, pred);
 	else done_cv_.wait_for(lk, std::chrono::duration<double, std::milli>(timeout_ms), pred);
@@ -609,7 +619,7 @@ int Server::info(unsigned long long id, double* lat, double* qd) {
 	std::lock_guard<std::mutex> g(mu_);
 	auto it = reqs_.find(id);
 	if (it == reqs_.end()) return CVTX_GB300_ST_UNKNOWN;
-	const Request& q = it->second;
+	const Request& q = *it->second;
 	if (lat) *lat = q.status == CVTX_GB300_ST_DONE ? 1e3 * (q.t_done - q.t_submit) : -1.0;
 	if (qd) *qd = q.t_admit > 0 ? 1e3 * (q.t_admit - q.t_submit) : -1.0;
 	return q.status;
@@ -660,8 +670,9 @@ void Server::reset_stats() {
 	dev_.reset_peak();
 	launches0_ = launch_count();
 	// forget finished requests
+	finished_.clear();
 	for (auto it = reqs_.begin(); it != reqs_.end();) {
-		if (it->second.status <= CVTX_GB300_ST_DONE) it = reqs_.erase(it);
+		if (it->second->status <= CVTX_GB300_ST_DONE) it = reqs_.erase(it);
 		else ++it;
 	}
 }

@@ -244,7 +244,8 @@ CVTX_EXPORT int cvtx_gb300_server_request_info(cvtx_gb300_server* srv,
 CVTX_EXPORT int cvtx_gb300_server_stats_get(cvtx_gb300_server* srv,
 	cvtx_gb300_server_stats* out);
 /* Restart the statistics and forget finished requests (their ids become
- * unknown); call it while no thread waits on a request. */
+ * unknown). Without it a finished request stays queryable until 1,048,576
+ * newer ones have finished. */
 CVTX_EXPORT void cvtx_gb300_server_reset_stats(cvtx_gb300_server* srv);
 /* Host-side fault injection: the next `count` arena allocations fail as if
  * the device were out of memory. */
