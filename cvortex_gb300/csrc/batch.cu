@@ -44,7 +44,7 @@ p3d_batch_kernel(const BatchProblem* __restrict__ probs, int n_probs,
 {
 	constexpr int NC = InduceNC<VEL, DV>::value;
 	extern __shared__ __align__(16) unsigned char smem[];
-	__shared__ BatchProblem sp;
+	__shared__ __align__(16) BatchProblem sp;
 	__shared__ int s_item;
 	__shared__ int s_last;
 	if (__syncthreads_or(blockDim.x != NT)) {
