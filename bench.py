@@ -495,9 +495,7 @@ def extras(cv, lib, args, torch, sh, peak):
 def redistribute_extra(cv, lib, n=200_000, gd=0.01):
     """cvtx_P3D_redistribute_on_grid (M4' stencil, 125 grid points per
     particle) of a 200,000-particle vortex ring: the GPU path against this
-    library's host path (all host cores); both give identical particles.
-    (The reference's own implementation does not terminate when built with
-    GCC, so it has no time here.)"""
+    library's host path (all host cores); both give identical particles."""
     from cvortex_gb300 import abi, workloads
     p = workloads.vortex_ring(n)
     ptrs = abi.ptr_array(p)

@@ -8,10 +8,9 @@
 // of this library's (redist.cu), else on the host. The algorithm and its
 // order of operations are described in redist.h.
 //
-// The reference's own GCC build cannot serve as a check here: its octree
-// insertion relies on UIntKey96::matching_leading_bits, which is unimplemented
-// for GCC (src/UIntKey96.h:222-247, "assert(false); TO DO") and does not
-// terminate with NDEBUG.
+// The output order is the depth-first order of the reference's octree /
+// quadtree without building a tree: that order is ascending Morton order of
+// the grid keys, so one sort of the keys gives it.
 #include <algorithm>
 #include <cmath>
 #include <cstring>

@@ -16,8 +16,8 @@ Three checkers for the GB300 library, none of which the product imports:
   implementation and of FP32 rounding); ``exact_p3d_vel_dvort`` is the same
   in compiled C for large samples.
 * ``oracle.redist``: a numpy restatement of the reference's particle
-  redistribution (parity unpinned: the reference's own build does not
-  return from those functions with GCC; see that module).
+  redistribution, pinned to the reference library's outputs (golden
+  fixture ``tests/golden/redist.npz``; see that module).
 """
 from __future__ import annotations
 

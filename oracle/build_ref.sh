@@ -13,6 +13,15 @@
 #                 print a warning and return zeros (src/VortFunc.cpp:52-62)
 #                 instead of aborting on assert(0).
 #
+# The grid-key files (octree / quadtree and the two key classes) are built
+# through the reference's MSVC branch: the GCC branch of
+# matching_leading_bits (src/UIntKey96.h:243-250, src/UIntKey64.h:220-225)
+# is an unfinished stub with which the redistribution functions never
+# return. ref_compat/intrin.h supplies the one MSVC intrinsic that branch
+# calls (_BitScanReverse). No other file of the reference tests __GNUC__ or
+# _MSC_VER except accelerators.cpp (a compiler name string), which keeps the
+# default flags.
+#
 # Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
 set -euo pipefail
 here="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
@@ -29,12 +38,19 @@ flags=(-std=c++17 -O3 -DNDEBUG -fPIC -fopenmp -fpermissive -w
        -DCVTX_USING_OPENMP "-DCVTX_EXPORT=" -DCVORTEX_VERSION_MAJOR=0
        -DCVORTEX_VERSION_MINOR=3 -DCVORTEX_VERSION_PATCH=8
        -I "$repo/include" -I "$ref/include/cvortex")
+key_flags=(-U__GNUC__ -D_MSC_VER=1929 -I "$here/ref_compat")
 objs=()
 pids=()
 for src in "$ref"/src/*.cpp; do
-  obj="$out/obj/$(basename "${src%.cpp}").o"
+  name="$(basename "${src%.cpp}")"
+  obj="$out/obj/$name.o"
   objs+=("$obj")
-  "$CXX" "${flags[@]}" -c "$src" -o "$obj" &
+  case "$name" in
+    GridParticleOcttree|GridParticleQuadtree|UIntKey96|UIntKey64)
+      "$CXX" "${flags[@]}" "${key_flags[@]}" -c "$src" -o "$obj" & ;;
+    *)
+      "$CXX" "${flags[@]}" -c "$src" -o "$obj" & ;;
+  esac
   pids+=($!)
 done
 for p in "${pids[@]}"; do wait "$p"; done

@@ -5,12 +5,12 @@ src/redistribution_helper_funcs.cpp:34-112, src/array_methods.cpp:150-194,
 redistribution functions src/RedistFunc.cpp:35-96, grid keys
 src/UIntKey96.cpp:49-141, octree order src/GridParticleOcttree.cpp:139-190).
 
-Parity unpinned: the reference's own build with GCC does not terminate in
-these functions (its octree insertion calls UIntKey96::matching_leading_bits,
-which is a "TO DO" stub under GCC, src/UIntKey96.h:222-247), so there are no
-reference outputs to pin this restatement to. It follows the reference
-source step by step instead; grid-point sums are taken in FP64 in particle
-order (the reference sums in FP32 per OpenMP thread).
+Pinned against the reference library itself (built by oracle/build_ref.sh
+through the reference's complete MSVC branch of matching_leading_bits, whose
+GCC branch is a stub, src/UIntKey96.h:240-265) on the golden fixture
+tests/golden/redist.npz: same counts, coordinates and order bit for bit;
+strengths to 2^-21 of the largest, because grid-point sums are taken here in
+FP64 in particle order and the reference sums in FP32 per OpenMP thread.
 
 Used only by tests/ as the checker.
 """

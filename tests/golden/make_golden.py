@@ -16,6 +16,9 @@ reference's OpenMP path) and stores inputs and outputs as compressed .npz:
                      LCG of test/testmain.c:87-92) with its outputs
 * kat.npz          -- g, zeta, eta (3D and 2D) of every regularisation on a
                      grid of rho, from the reference's function pointers
+* redist.npz       -- cvtx_P3D_redistribute_on_grid / cvtx_P2D_redistribute_on_grid
+                     for the five redistribution functions with and without
+                     removal of weak particles and with an output limit
 
 Run from the repository root: python tests/golden/make_golden.py
 """
@@ -127,6 +130,42 @@ def kat_case(ref):
     np.savez_compressed(OUT / "kat.npz", **d)
 
 
+REDIST_FUNCS = ("lambda0", "lambda1", "lambda2", "lambda3", "m4p")
+# (negligible_vort, max_output_particles): keep all, remove weak ones,
+# and an output limit that triggers the strength-threshold search
+REDIST_P3D = ((0.0, 10**6), (1e-2, 10**6), (0.1, 150))
+REDIST_P2D = ((0.0, 10**6), (1e-2, 10**6), (0.05, 100))
+
+
+def redist_case(ref):
+    sys.path.insert(0, str(ROOT / "tests"))
+    from redist_util import p2d, p3d
+    cube = workloads.uniform_cube(120, seed=21)
+    ring = workloads.vortex_ring(100, seed=22)
+    patch = workloads.gaussian_patch_2d(150, seed=23)
+    one = abi.make_p3d([[0.013, 0.021, -0.007]], [[1.0, 0.5, -0.25]], [1.0])
+    d = {"cube": cube, "ring": ring, "patch": patch, "one": one}
+
+    def put(key, n, out):
+        d[f"{key}_n"], d[f"{key}_coord"], d[f"{key}_vort"] = np.int64(n), out["coord"], out["vorticity"]
+
+    for f in REDIST_FUNCS:
+        for i, (neg, mo) in enumerate(REDIST_P3D):
+            put(f"cube_{f}_{i}", *p3d(ref.lib, cube, f, 0.35, neg, mo))
+        for i, (neg, mo) in enumerate(REDIST_P2D):
+            put(f"patch_{f}_{i}", *p2d(ref.lib, patch, f, 0.1, neg, mo))
+        put(f"one_{f}", *p3d(ref.lib, one, f, 0.1, 0.0, 1000))
+    put("ring_m4p", *p3d(ref.lib, ring, "m4p", 0.15, 1e-3, 10**6))
+    # edges: NULL output array (count only), empty input, and an output
+    # limit whose threshold search removes every particle
+    d["cube_m4p_null_n"] = np.int64(p3d(ref.lib, cube, "m4p", 0.35, 1e-2, 0, null_output=True)[0])
+    d["empty_n"] = np.int64(p3d(ref.lib, cube[:0], "m4p", 0.35, 0.0, 10)[0])
+    dense = workloads.gaussian_patch_2d(250, seed=23)
+    d["dense"] = dense
+    put("dense_lambda3", *p2d(ref.lib, dense, "lambda3", 0.05, 0.05, 100))
+    np.savez_compressed(OUT / "redist.npz", **d)
+
+
 def main():
     ref = reference()
     cube = workloads.uniform_cube(700, seed=11)
@@ -138,6 +177,7 @@ def main():
     f3d_case(ref)
     reftest_case(ref)
     kat_case(ref)
+    redist_case(ref)
     for f in sorted(OUT.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

@@ -1,11 +1,13 @@
 """Particle redistribution on the GPU: the same grid points, order and
-strengths as the host path and the oracle, bit for bit."""
+strengths as the host path and the oracle, bit for bit, and the reference
+library's own outputs (golden fixture) to the FP32 summation tolerance."""
 import numpy as np
 import pytest
 
 from cvortex_gb300 import workloads
 from oracle import redist as R
 from redist_util import p2d, p3d
+from test_redist import GOLD, GOLD_CASES, assert_matches_gold
 
 pytestmark = pytest.mark.gpu
 
@@ -23,6 +25,16 @@ def test_p3d_gpu_matches_oracle(gpu, fname, neg, max_out):
     assert n == cnt
     assert np.array_equal(out["coord"], coord)
     assert np.array_equal(out["vorticity"], vort)
+
+
+@pytest.mark.parametrize("case", GOLD_CASES, ids=[c[0] for c in GOLD_CASES])
+def test_gpu_matches_reference_golden(gpu, case):
+    key, dims, inp, fname, gd, neg, mo = case
+    call = p3d if dims == 3 else p2d
+    launches = gpu.launches()
+    n, out = call(gpu.lib, GOLD[inp], fname, gd, neg, mo)
+    assert gpu.launches() > launches, "redistribution did not run on the GPU"
+    assert_matches_gold(key, n, out["coord"], out["vorticity"])
 
 
 @pytest.mark.parametrize("fname", FUNCS)
