@@ -52,7 +52,12 @@ FLOPS = {("vel", 1): 30, ("dvort", 1): 46, ("veldvort", 1): 61,
          ("vel", 0): 25, ("dvort", 0): 39, ("veldvort", 0): 49,
          ("vel", 2): 25, ("dvort", 2): 39, ("veldvort", 2): 49,
          ("vel", 3): 46, ("dvort", 3): 62, ("veldvort", 3): 77}
+# vorticity field (5 sigma box cut-off), FP32 operations per pair:
+# winckelmans 22, planetary 15, gaussian 17
+VORT_FLOPS = {1: 22, 2: 15, 3: 17}
 REG = {"singular": 0, "winckelmans": 1, "planetary": 2, "gaussian": 3}
+OPS = {"veldvort": "fused vel+dvort", "vel": "vel", "dvort": "dvort",
+       "vort": "vorticity field (5 sigma box cut-off)"}
 SIGMA = 0.05
 CPU_SAMPLE_TARGETS = 2048
 
@@ -66,6 +71,9 @@ def parse():
     ap.add_argument("--n", type=int, default=100_000, help="particles in the ring")
     ap.add_argument("--reg", default="winckelmans", choices=list(REG))
     ap.add_argument("--quick", action="store_true", help="skip the extra measurements")
+    ap.add_argument("--op", default="veldvort", choices=list(OPS),
+                    help="the kernel timed as the step; the benchmark is veldvort, the others "
+                         "exist to profile one kernel with the same command")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--serve-requests", type=int, default=64,
                     help="requests per arrival rate in the served-stream measurement")
@@ -246,11 +254,22 @@ def run_ours(args):
     stream = torch.cuda.current_stream()
     sh = C.c_void_p(stream.cuda_stream)
 
+    op = args.op
+    if op == "vort" and reg not in VORT_FLOPS:
+        raise SystemExit("--op vort: the singular vorticity field is zero (no kernel)")
+    flops_per = VORT_FLOPS[reg] if op == "vort" else FLOPS[(op, reg)]
+    v_out = vel.data_ptr() if op in ("veldvort", "vel") else None
+    d_out = dv.data_ptr() if op in ("veldvort", "dvort") else None
+
     def step():
-        rc = lib.cvtx_gb300_dev_P3D_M2M(rec.data_ptr(), n, rec.data_ptr(), 2, n, vel.data_ptr(),
-                                        dv.data_ptr(), reg, SIGMA, sh)
+        if op == "vort":
+            rc = lib.cvtx_gb300_dev_P3D_M2M_vort(rec.data_ptr(), n, rec.data_ptr(), 2, n,
+                                                 vel.data_ptr(), reg, SIGMA, sh)
+        else:
+            rc = lib.cvtx_gb300_dev_P3D_M2M(rec.data_ptr(), n, rec.data_ptr(), 2, n, v_out, d_out,
+                                            reg, SIGMA, sh)
         if rc != 0:
-            raise RuntimeError(f"dev_P3D_M2M failed ({rc}): {cv.last_error()}")
+            raise RuntimeError(f"{op} step failed ({rc}): {cv.last_error()}")
 
     p_scalar, p_packed = C.c_double(0.0), C.c_double(0.0)
     if lib.cvtx_gb300_probe_fp32_detail(5, C.byref(p_scalar), C.byref(p_packed)) != 0:
@@ -288,35 +307,35 @@ def run_ours(args):
     t_max = max_over_ranks(total_ms, device="cuda")
     pairs = float(n) * n
     value = world * args.steps * pairs / (t_max * 1e-3) / 1e9
-    flops = FLOPS[("veldvort", reg)] * pairs
+    flops = flops_per * pairs
     achieved = flops / (kernel_ms * 1e-3) / 1e12
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": f"P3D vortex ring N={n}, {args.reg}, sigma={SIGMA}, "
-                               "fused vel+dvort, targets = sources",
+                               f"{OPS[op]}, targets = sources",
                    "interactions_per_step": pairs, "l2": "flushed between steps (256 MB write)",
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
                      "frac": achieved / peak.value if peak.value else None,
-                     "traffic": profiled_traffic(n, args.reg),
+                     "traffic": profiled_traffic(n, args.reg) if op == "veldvort" else None,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
                                        "launch (profiles/p3d_induce2_ring100k_launches.md); "
                                        "algorithmic bytes 5.6 MB, the rest FP64 split partials",
                      "peak_source": "measured FP32 FMA probe, max of scalar FFMA "
                                     f"{p_scalar.value:.2f} and packed f32x2 FFMA "
                                     f"{p_packed.value:.2f} TFLOP/s",
-                     "flops_per_interaction": FLOPS[("veldvort", reg)],
+                     "flops_per_interaction": flops_per,
                      "launch_ms": kernel_ms},
         "gpu_launches": launches,
         "clocks": clk,
     }
-    if rank == 0 and not args.quick:
+    if rank == 0 and not args.quick and op == "veldvort":
         out["e2e"] = e2e_abi(cv, p, args)
         out["serving"] = serve_extra(cv, lib, count=args.serve_requests)
         out["extras"] = extras(cv, lib, args, torch, sh, peak.value)
-    if rank == 0 and world == 1:
+    if rank == 0 and world == 1 and op == "veldvort":
         out["cpu_baseline"] = cpu_baseline(p, args.reg)
     if rank == 0:
         print(json.dumps(out), flush=True)
@@ -416,6 +435,12 @@ def extras(cv, lib, args, torch, sh, peak):
             ms = timed_dev(f, torch, 5)
             row["visc"] = {"ginter_s": n * n / ms / 1e6,
                            "fp32_frac": (22 if r == 1 else 17) * n * n / (ms * 1e-3) / 1e12 / peak}
+        if r in VORT_FLOPS:
+            f = lambda: lib.cvtx_gb300_dev_P3D_M2M_vort(rec.data_ptr(), n, rec.data_ptr(), 2, n,
+                                                        o1.data_ptr(), r, SIGMA, sh)
+            ms = timed_dev(f, torch, 5)
+            row["vort"] = {"ginter_s": n * n / ms / 1e6,
+                           "fp32_frac": VORT_FLOPS[r] * n * n / (ms * 1e-3) / 1e12 / peak}
         res[f"ring{n}_{rname}"] = row
     q = workloads.gaussian_patch_2d(200_000)
     rq = torch.from_numpy(np.ascontiguousarray(

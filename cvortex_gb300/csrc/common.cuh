@@ -110,6 +110,12 @@ __device__ __forceinline__ float ex2_approx(float x) {
 	asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
 	return y;
 }
+// max(a, b, c), NaN if any input is NaN (three-input form, sm_100 and up).
+__device__ __forceinline__ float max3_nan(float a, float b, float c) {
+	float y;
+	asm("max.NaN.f32 %0, %1, %2, %3;" : "=f"(y) : "f"(a), "f"(b), "f"(c));
+	return y;
+}
 __device__ __forceinline__ float rcp_approx(float x) {
 	float y;
 	asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));

@@ -560,7 +560,9 @@ p3d_vort_kernel(const P3DVortProblem p, const RegConsts rc, float cutoff,
 				const float dx = sp.x - tx[k];
 				const float dy = sp.y - ty[k];
 				const float dz = sp.z - tz[k];
-				const bool in = fabsf(dx) < cutoff && fabsf(dy) < cutoff && fabsf(dz) < cutoff;
+				// the box test as one three-input max: NaN in any component
+				// gives NaN, which fails it, as each separate test would
+				const bool in = max3_nan(fabsf(dx), fabsf(dy), fabsf(dz)) < cutoff;
 				const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
 				float z = ZetaP3D<R>::z(r2, rc);
 				z = in ? z : 0.f;
@@ -585,6 +587,123 @@ p3d_vort_kernel(const P3DVortProblem p, const RegConsts rc, float cutoff,
 				fold_twosum(h, l, acc[c][k]);
 				hi[i] = h; lo[i] = l;
 			}
+	};
+	if (!Stream2::run(smem, p.src, s_begin, n_s, err, tile_fn)) return;
+#pragma unroll
+	for (int k = 0; k < TPT; ++k) {
+		const int t = tbase + k * NT + tid;
+		if (t >= p.n_tgt) continue;
+#pragma unroll
+		for (int c = 0; c < NC; ++c) {
+			const int i = (c * TPT + k) * NT + tid;
+			const double s = double(hi[i]) + double(lo[i]);
+			if (gridDim.y == 1) p.out[3 * size_t(t) + c] = float(scale * s);
+			else partial[(size_t(blockIdx.y) * NC + c) * p.n_tgt + t] = s;
+		}
+	}
+}
+
+// Packed form (two targets per f32x2 lane pair). zeta's constant factor
+// (7.5 Winckelmans, 3 planetary, sqrt(2/pi) Gaussian) is left to the FP64
+// output scale, so each pair evaluates only the shape of zeta.
+template <Reg R> struct ZetaShape2;
+template <> struct ZetaShape2<Reg::Winckelmans> {
+	static constexpr double kFactor = 7.5;
+	__device__ __forceinline__ static float2 z(float2 r2, const RegConsts& c) {
+		const float2 q = __ffma2_rn(r2, bc2(c.inv_s2), bc2(1.f));
+		const float2 s = make_float2(rsqrt_approx(q.x), rsqrt_approx(q.y));
+		const float2 s2 = __fmul2_rn(s, s);
+		return __fmul2_rn(__fmul2_rn(s2, s2), __fmul2_rn(s2, s));   // (1 + rho^2)^-3.5
+	} };
+template <> struct ZetaShape2<Reg::Planetary> {
+	static constexpr double kFactor = 3.0;
+	__device__ __forceinline__ static float2 z(float2 r2, const RegConsts& c) {
+		return make_float2(r2.x < c.s2 ? 1.f : 0.f, r2.y < c.s2 ? 1.f : 0.f);
+	} };
+template <> struct ZetaShape2<Reg::Gaussian> {
+	static constexpr double kFactor = 0.7978845608028654;   // sqrt(2/pi)
+	__device__ __forceinline__ static float2 z(float2 r2, const RegConsts& c) {
+		const float2 a = __fmul2_rn(r2, bc2(c.exp2_half));
+		return make_float2(ex2_approx(a.x), ex2_approx(a.y));       // exp(-rho^2/2)
+	} };
+
+template <Reg R, int TPT, int NT>
+__global__ void __launch_bounds__(NT)
+p3d_vort2_kernel(const P3DVortProblem p, const RegConsts rc, float cutoff,
+	double scale, double* __restrict__ partial, int src_per_split, unsigned* err)
+{
+	static_assert(TPT % 2 == 0, "packed kernel: even TPT");
+	constexpr int NC = 3, H = TPT / 2;
+	extern __shared__ __align__(16) unsigned char smem[];
+	float* hi = reinterpret_cast<float*>(smem + Stream2::kSmemBytes);
+	float* lo = hi + NC * TPT * NT;
+	const int tid = threadIdx.x;
+	const int tbase = blockIdx.x * (TPT * NT);
+	const int s_begin = blockIdx.y * src_per_split;
+	int n_s = p.n_src - s_begin;
+	n_s = n_s < src_per_split ? n_s : src_per_split;
+	n_s = n_s > 0 ? n_s : 0;
+	float2 ntx[H], nty[H], ntz[H];   // negated target coordinates
+#pragma unroll
+	for (int h = 0; h < H; ++h) {
+		float4 q[2];
+#pragma unroll
+		for (int e = 0; e < 2; ++e) {
+			int t = tbase + (2 * h + e) * NT + tid;
+			t = t < p.n_tgt ? t : p.n_tgt - 1;
+			q[e] = p.tgt[size_t(t) * p.tstride];
+		}
+		ntx[h] = make_float2(-q[0].x, -q[1].x);
+		nty[h] = make_float2(-q[0].y, -q[1].y);
+		ntz[h] = make_float2(-q[0].z, -q[1].z);
+	}
+#pragma unroll
+	for (int i = 0; i < NC * TPT; ++i) { hi[i * NT + tid] = 0.f; lo[i * NT + tid] = 0.f; }
+	auto tile_fn = [&](const float4* __restrict__ st, int cnt) {
+		float2 acc[NC][H];
+#pragma unroll
+		for (int c = 0; c < NC; ++c)
+#pragma unroll
+			for (int h = 0; h < H; ++h) acc[c][h] = make_float2(0.f, 0.f);
+		auto body = [&](int j) {
+			const float4 sp = st[2 * j];
+			const float4 sv = st[2 * j + 1];
+			const float2 sx = bc2(sp.x), sy = bc2(sp.y), sz = bc2(sp.z);
+#pragma unroll
+			for (int h = 0; h < H; ++h) {
+				// source - target, rounded once as in the scalar form
+				const float2 dx = __fadd2_rn(sx, ntx[h]);
+				const float2 dy = __fadd2_rn(sy, nty[h]);
+				const float2 dz = __fadd2_rn(sz, ntz[h]);
+				const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+				float2 z = ZetaShape2<R>::z(r2, rc);
+				const bool in0 = max3_nan(fabsf(dx.x), fabsf(dy.x), fabsf(dz.x)) < cutoff;
+				const bool in1 = max3_nan(fabsf(dx.y), fabsf(dy.y), fabsf(dz.y)) < cutoff;
+				z.x = in0 ? z.x : 0.f;
+				z.y = in1 ? z.y : 0.f;
+				acc[0][h] = __ffma2_rn(z, bc2(sv.x), acc[0][h]);
+				acc[1][h] = __ffma2_rn(z, bc2(sv.y), acc[1][h]);
+				acc[2][h] = __ffma2_rn(z, bc2(sv.z), acc[2][h]);
+			}
+		};
+		if (cnt == kTile) {
+#pragma unroll 2
+			for (int j = 0; j < kTile; ++j) body(j);
+		} else {
+#pragma unroll 1
+			for (int j = 0; j < cnt; ++j) body(j);
+		}
+#pragma unroll
+		for (int c = 0; c < NC; ++c)
+#pragma unroll
+			for (int h = 0; h < H; ++h)
+#pragma unroll
+				for (int e = 0; e < 2; ++e) {
+					const int i = (c * TPT + 2 * h + e) * NT + tid;
+					float hv = hi[i], lv = lo[i];
+					fold_twosum(hv, lv, e == 0 ? acc[c][h].x : acc[c][h].y);
+					hi[i] = hv; lo[i] = lv;
+				}
 	};
 	if (!Stream2::run(smem, p.src, s_begin, n_s, err, tile_fn)) return;
 #pragma unroll
@@ -795,24 +914,38 @@ cudaError_t launch_visc(const P3DViscProblem& p, const LaunchEnv& env) {
 	return cudaGetLastError();
 }
 
-template <Reg R, int TPT, int NT>
-Plan plan_vort(int n_src, int n_tgt, int num_sms) {
-	constexpr size_t smem = smem_bytes<TPT, NT, 3>();
-	static const int occ = resident_ctas(p3d_vort_kernel<R, TPT, NT>, NT, smem);
-	return make_plan(n_src, n_tgt, TPT * NT, kTile, 3, num_sms * occ, smem);
+template <Reg R_, int TPT_, bool PK_> struct vort_tag {
+	static constexpr Reg R = R_;
+	static constexpr int TPT = TPT_;
+	static constexpr bool PK = PK_;
+};
+
+template <Reg R, int TPT, int NT, bool PK>
+auto vort_kernel() {
+	if constexpr (PK) return p3d_vort2_kernel<R, TPT, NT>;
+	else return p3d_vort_kernel<R, TPT, NT>;
 }
 
-template <Reg R, int TPT, int NT>
+template <Reg R, int TPT, int NT, bool PK>
+Plan plan_vort(int n_src, int n_tgt, int num_sms, int max_split = 64) {
+	constexpr size_t smem = smem_bytes<TPT, NT, 3>();
+	static const int occ = resident_ctas(vort_kernel<R, TPT, NT, PK>(), NT, smem);
+	return make_plan(n_src, n_tgt, TPT * NT, kTile, 3, num_sms * occ, smem, max_split);
+}
+
+template <Reg R, int TPT, int NT, bool PK>
 cudaError_t launch_vort(const P3DVortProblem& p, const LaunchEnv& env) {
-	const Plan pl = plan_vort<R, TPT, NT>(p.n_src, p.n_tgt, env.num_sms);
+	const Plan pl = plan_vort<R, TPT, NT, PK>(p.n_src, p.n_tgt, env.num_sms,
+		env.cap_to_ws ? split_cap_for(env.ws_bytes, 3, p.n_tgt) : 64);
 	if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
 	const RegConsts rc = make_reg_consts(p.sigma);
 	const double s = p.sigma;
-	const double scale = 1.0 / (4.0 * 3.14159265358979323846 * s * s * s);
+	double scale = 1.0 / (4.0 * 3.14159265358979323846 * s * s * s);
+	if constexpr (PK) scale *= ZetaShape2<R>::kFactor;
 	const float cutoff = 5.f * p.sigma;
 	double* partial = static_cast<double*>(env.ws);
 	dim3 grid(pl.n_tblocks, pl.n_split);
-	p3d_vort_kernel<R, TPT, NT><<<grid, NT, pl.smem, env.stream>>>(
+	vort_kernel<R, TPT, NT, PK>()<<<grid, NT, pl.smem, env.stream>>>(
 		p, rc, cutoff, scale, partial, pl.src_per_split, env.err);
 	count_launch();
 	if (pl.n_split > 1) {
@@ -888,25 +1021,64 @@ cudaError_t p3d_visc(int reg, const P3DViscProblem& p, const LaunchEnv& env) {
 	return cudaErrorInvalidValue;
 }
 
-size_t p3d_vort_ws_bytes(int reg, int n_src, int n_tgt, int num_sms) {
-	if (n_tgt <= 0) return 0;
-	switch (reg) {
-	case 0: return plan_vort<Reg::Singular, 4, 128>(n_src, n_tgt, num_sms).ws_bytes;
-	case 1: return plan_vort<Reg::Winckelmans, 4, 128>(n_src, n_tgt, num_sms).ws_bytes;
-	case 2: return plan_vort<Reg::Planetary, 4, 128>(n_src, n_tgt, num_sms).ws_bytes;
-	default: return plan_vort<Reg::Gaussian, 4, 128>(n_src, n_tgt, num_sms).ws_bytes;
+// Vorticity-field configurations (targets per thread, 128 threads per CTA):
+// 0 scalar (4), 1 packed (4), 2 packed (8), 3 packed (2). Default from GB300
+// timings (vortex ring, 20,000 / 100,000 / 400,000 targets): 0 below
+// kSmallTargets targets, 3 up to 65,535, else 2; CVTX_GB300_VORT_CFG forces
+// one.
+// The singular regularisation's zeta is identically zero (reference
+// src/VortFunc.cpp:68-70), so its field is zero without evaluating any pair.
+int vort_cfg(int n_tgt) {
+	static const int forced = [] {
+		const char* e = std::getenv("CVTX_GB300_VORT_CFG");
+		if (!e || !*e) return -1;
+		const int c = std::atoi(e);
+		return (c >= 0 && c <= 3) ? c : -1;
+	}();
+	if (forced >= 0) return forced;
+	return n_tgt < kSmallTargets ? 0 : n_tgt < 65536 ? 3 : 2;
+}
+
+template <Reg R, typename F>
+cudaError_t with_vort_tpt(int cfg, F&& f) {
+	switch (cfg) {
+	case 0: return f(vort_tag<R, 4, false>{});
+	case 2: return f(vort_tag<R, 8, true>{});
+	case 3: return f(vort_tag<R, 2, true>{});
+	default: return f(vort_tag<R, 4, true>{});
 	}
+}
+
+template <typename F>
+cudaError_t with_vort_cfg(int reg, int n_tgt, F&& f) {
+	const int cfg = vort_cfg(n_tgt);
+	switch (reg) {
+	case 1: return with_vort_tpt<Reg::Winckelmans>(cfg, f);
+	case 2: return with_vort_tpt<Reg::Planetary>(cfg, f);
+	case 3: return with_vort_tpt<Reg::Gaussian>(cfg, f);
+	default: return cudaErrorInvalidValue;
+	}
+}
+
+size_t p3d_vort_ws_bytes(int reg, int n_src, int n_tgt, int num_sms) {
+	if (n_tgt <= 0 || reg == int(Reg::Singular)) return 0;
+	size_t ws = 0;
+	with_vort_cfg(reg, n_tgt, [&](auto tag) {
+		using T = decltype(tag);
+		ws = plan_vort<T::R, T::TPT, 128, T::PK>(n_src, n_tgt, num_sms).ws_bytes;
+		return cudaSuccess;
+	});
+	return ws;
 }
 
 cudaError_t p3d_vort(int reg, const P3DVortProblem& p, const LaunchEnv& env) {
 	if (p.n_tgt <= 0) return cudaSuccess;
-	switch (reg) {
-	case 0: return launch_vort<Reg::Singular, 4, 128>(p, env);
-	case 1: return launch_vort<Reg::Winckelmans, 4, 128>(p, env);
-	case 2: return launch_vort<Reg::Planetary, 4, 128>(p, env);
-	case 3: return launch_vort<Reg::Gaussian, 4, 128>(p, env);
-	default: return cudaErrorInvalidValue;
-	}
+	if (reg == int(Reg::Singular))
+		return cudaMemsetAsync(p.out, 0, sizeof(float) * 3 * size_t(p.n_tgt), env.stream);
+	return with_vort_cfg(reg, p.n_tgt, [&](auto tag) {
+		using T = decltype(tag);
+		return launch_vort<T::R, T::TPT, 128, T::PK>(p, env);
+	});
 }
 
 }  // namespace cvtx

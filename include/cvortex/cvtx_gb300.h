@@ -90,6 +90,12 @@ CVTX_EXPORT int cvtx_gb300_dev_P3D_M2M(const void* src, int n_src,
 CVTX_EXPORT int cvtx_gb300_dev_P3D_M2M_visc(const void* src, int n_src,
 	const void* tgt, int tgt_stride, int n_tgt, float* out, int reg,
 	float regularisation_radius, float kinematic_visc, void* stream);
+/* Vorticity field at points (tgt: records with tgt_stride float4 per point;
+ * the first float4 holds the position), with the reference CPU path's
+ * 5 sigma box cut-off. Zeros for singular (zeta = 0). */
+CVTX_EXPORT int cvtx_gb300_dev_P3D_M2M_vort(const void* src, int n_src,
+	const void* tgt, int tgt_stride, int n_tgt, float* out, int reg,
+	float regularisation_radius, void* stream);
 CVTX_EXPORT int cvtx_gb300_dev_P2D_M2M_vel(const void* src, int n_src,
 	const void* tgt, int n_tgt, float* out, int reg,
 	float regularisation_radius, void* stream);

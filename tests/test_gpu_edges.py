@@ -166,6 +166,28 @@ def test_dev_f3d_dvort_matches_oracle(gpu):
     close(out.cpu().numpy(), oracle.f3d_dvort(f, p))
 
 
+def test_dev_p3d_vort_matches_abi(gpu):
+    """The device-pointer vorticity field (point records, stride 1) equals the
+    ABI call bit for bit."""
+    import torch
+    p = workloads.vortex_ring(5000, seed=17)
+    mes = workloads.vortex_ring(9000, seed=18)["coord"].copy()
+    rp = np.zeros((len(p), 8), np.float32)
+    rp[:, 0:3], rp[:, 3], rp[:, 4:7] = p["coord"], p["volume"], p["vorticity"]
+    rm = np.zeros((len(mes), 4), np.float32)
+    rm[:, 0:3] = mes
+    a, b = torch.from_numpy(rp).cuda(), torch.from_numpy(rm).cuda()
+    out = torch.empty((len(mes), 3), dtype=torch.float32, device="cuda")
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for reg, code in (("winckelmans", 1), ("gaussian", 3), ("singular", 0)):
+        out.fill_(7.0)
+        assert gpu.lib.cvtx_gb300_dev_P3D_M2M_vort(a.data_ptr(), len(p), b.data_ptr(), 1,
+                                                   len(mes), out.data_ptr(), code, 0.05,
+                                                   stream) == 0
+        assert gpu.lib.cvtx_gb300_dev_status(stream) == 0
+        assert np.array_equal(out.cpu().numpy(), gpu.p3d_vort(p, mes, reg, 0.05))
+
+
 @pytest.mark.parametrize("n", [8192, 8193, 20001])
 def test_packed_p2d_f3d_ragged_sizes(gpu, n):
     """The packed P2D / F3D velocity kernels (8,192 targets and up) on sizes
@@ -201,6 +223,29 @@ def test_packed_f3d_dvort(gpu, n):
     assert np.all(np.isfinite(got))
     sel = np.r_[0:128, n - 64:n]
     close(got[sel], oracle.f3d_dvort(f, p[sel]))
+
+
+@pytest.mark.parametrize("n", [8192, 8193, 12_345, 70_001])
+def test_packed_p3d_vort_ragged_sizes(gpu, n):
+    """The packed vorticity-field kernels (two targets per thread from 8,192
+    targets, eight from 65,536) against the oracle on ragged sizes, with
+    targets exactly on the 5 sigma box edge and on sources; one source split,
+    and many splits (few sources)."""
+    s = 0.05
+    p = workloads.vortex_ring(3000, seed=15)
+    mes = workloads.vortex_ring(n, seed=16)["coord"].copy()
+    mes[:32] = p["coord"][:32]
+    mes[32:64] = p["coord"][32:64] + np.float32(5 * s) * np.array([1, 0, 0], np.float32)
+    idx = np.r_[0:128, n - 64:n]
+    for reg in ("winckelmans", "planetary", "gaussian"):
+        before = gpu.launches()
+        got = gpu.p3d_vort(p, mes, reg, s)
+        assert gpu.launches() > before
+        close(got[idx], oracle.p3d_vort(p, mes[idx], reg, s))
+        few = p[:40]
+        close(gpu.p3d_vort(few, mes, reg, s)[idx], oracle.p3d_vort(few, mes[idx], reg, s))
+    sing = gpu.p3d_vort(p, mes, "singular", s)
+    assert not np.any(sing)
 
 
 def test_dev_inf_mtrx_matches_abi(gpu):
