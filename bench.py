@@ -57,7 +57,11 @@ FLOPS = {("vel", 1): 30, ("dvort", 1): 46, ("veldvort", 1): 61,
 VORT_FLOPS = {1: 22, 2: 15, 3: 17}
 REG = {"singular": 0, "winckelmans": 1, "planetary": 2, "gaussian": 3}
 OPS = {"veldvort": "fused vel+dvort", "vel": "vel", "dvort": "dvort",
-       "vort": "vorticity field (5 sigma box cut-off)"}
+       "vort": "vorticity field (5 sigma box cut-off)",
+       "inf": "F3D influence matrix, 25,000 points x 20,000 filaments (2 GB)"}
+# influence matrix: F3D vel (51) + the dot with the direction (5) per entry
+INF_FLOPS = 56
+INF_SHAPE = (25_000, 20_000)
 SIGMA = 0.05
 CPU_SAMPLE_TARGETS = 2048
 
@@ -257,12 +261,29 @@ def run_ours(args):
     op = args.op
     if op == "vort" and reg not in VORT_FLOPS:
         raise SystemExit("--op vort: the singular vorticity field is zero (no kernel)")
-    flops_per = VORT_FLOPS[reg] if op == "vort" else FLOPS[(op, reg)]
+    flops_per = (VORT_FLOPS[reg] if op == "vort" else INF_FLOPS if op == "inf"
+                 else FLOPS[(op, reg)])
     v_out = vel.data_ptr() if op in ("veldvort", "vel") else None
     d_out = dv.data_ptr() if op in ("veldvort", "dvort") else None
+    pairs = float(n) * n
+    if op == "inf":
+        nm, ni = INF_SHAPE
+        pairs = float(nm) * ni
+        fil = workloads.wake_sheet(ni)
+        rf = np.zeros((ni, 8), np.float32)
+        rf[:, 0:3], rf[:, 3], rf[:, 4:7] = fil["start"], fil["strength"], fil["end"]
+        tf = np.zeros((nm, 4), np.float32)
+        tf[:, 0:3] = workloads.sheet_targets(nm)
+        dirs = np.zeros((nm, 4), np.float32)
+        dirs[:, 2] = 1.0
+        rfd, tfd, dd = (torch.from_numpy(x).cuda() for x in (rf, tf, dirs))
+        om = torch.empty((nm, ni), dtype=torch.float32, device="cuda")
 
     def step():
-        if op == "vort":
+        if op == "inf":
+            rc = lib.cvtx_gb300_dev_F3D_inf_mtrx(rfd.data_ptr(), ni, tfd.data_ptr(), dd.data_ptr(),
+                                                 nm, om.data_ptr(), sh)
+        elif op == "vort":
             rc = lib.cvtx_gb300_dev_P3D_M2M_vort(rec.data_ptr(), n, rec.data_ptr(), 2, n,
                                                  vel.data_ptr(), reg, SIGMA, sh)
         else:
@@ -305,7 +326,6 @@ def run_ours(args):
     kernel_ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
     from cvortex_gb300.multi import max_over_ranks
     t_max = max_over_ranks(total_ms, device="cuda")
-    pairs = float(n) * n
     value = world * args.steps * pairs / (t_max * 1e-3) / 1e9
     flops = flops_per * pairs
     achieved = flops / (kernel_ms * 1e-3) / 1e12
@@ -313,8 +333,8 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": f"P3D vortex ring N={n}, {args.reg}, sigma={SIGMA}, "
-                               f"{OPS[op]}, targets = sources",
+        "config": {"workload": OPS[op] if op == "inf" else
+                   f"P3D vortex ring N={n}, {args.reg}, sigma={SIGMA}, {OPS[op]}, targets = sources",
                    "interactions_per_step": pairs, "l2": "flushed between steps (256 MB write)",
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
@@ -481,7 +501,7 @@ def extras(cv, lib, args, torch, sh, peak):
     res["f3d_sheet100k_vel"] = {"ginter_s": nf * nf / ms / 1e6,
                                 "fp32_frac": 51 * nf * nf / (ms * 1e-3) / 1e12 / peak}
     # influence matrix: write-bound (4 B per entry); 25,000 points x 20,000 filaments
-    nm, ni = 25_000, 20_000
+    nm, ni = INF_SHAPE
     dirs = np.zeros((nm, 4), np.float32)
     dirs[:, 2] = 1.0
     dd = torch.from_numpy(dirs).cuda()
@@ -492,7 +512,8 @@ def extras(cv, lib, args, torch, sh, peak):
     gbs = 4.0 * nm * ni / (ms * 1e-3) / 1e9
     res["f3d_inf_mtrx_25kx20k"] = {"ms": ms, "write_gbs": gbs,
                                    "hbm_frac": gbs / hbm_peak if hbm_peak else None,
-                                   "hbm_peak_gbs": hbm_peak}
+                                   "hbm_peak_gbs": hbm_peak,
+                                   "fp32_frac": INF_FLOPS * nm * ni / (ms * 1e-3) / 1e12 / peak}
     del om
     cube = workloads.uniform_cube(nf, seed=12)
     rc = torch.from_numpy(p3d_records(cube).reshape(nf, 8)).cuda()

@@ -544,18 +544,59 @@ __global__ void f3d_inf_kernel(const F3DInfProblem p)
 	}
 }
 
-// Tiled influence matrix: a CTA covers kInfRows points x kInfFils filaments;
-// the filament tile sits in shared memory, and each thread evaluates
-// kInfPairs pairs of points (f32x2) against four consecutive filaments held
-// in registers, storing float4 runs, so a warp writes 512 contiguous bytes of
-// each of its rows.
+// Tiled influence matrix: a CTA covers 16 PAIRS points x kInfFils filaments;
+// the filament tile sits in shared memory, and each thread evaluates PAIRS
+// pairs of points (f32x2) against four consecutive filaments held in
+// registers, storing float4 runs, so a warp writes 512 contiguous bytes of
+// each of its rows. All lanes of a warp share their points (broadcast loads).
 constexpr int kInfFils = 128;                 // 32 threads x 4 filaments
-constexpr int kInfPairs = 4;                  // point pairs per thread
-constexpr int kInfRows = 8 * 2 * kInfPairs;   // 8 threads x 2 points x kInfPairs
 constexpr int kInfThreads = 256;
+template <int PAIRS> constexpr int inf_rows() { return 8 * 2 * PAIRS; }
 
+// One influence entry per lane: dir . (velocity of filament a -> b at m), the
+// terms of f3d_vel_pair2 with the direction dotted in before the guard, so
+// one test and one select drop a non-finite term (the reference tests t1 and
+// t2 separately, src/F3D.cpp:51-52; the single test on t1 t2 differs only
+// where two finite factors overflow, when the reference's entry is not finite
+// either). ga = gamma / (4 pi). Differences are formed as fma(x, -1, y): one
+// rounding, as y - x.
+// One filament's operands, each held twice (one per point of a lane pair).
+struct InfFil2 { float2 ax, ay, az, bx, by, bz, ga; };
+
+__device__ __forceinline__ float2 f3d_inf_pair2(float2 mx, float2 my, float2 mz,
+	float2 ex, float2 ey, float2 ez, const InfFil2& f2)
+{
+	const float2 m1 = bc2(-1.f);
+	const float2 r1x = __ffma2_rn(f2.ax, m1, mx), r1y = __ffma2_rn(f2.ay, m1, my);
+	const float2 r1z = __ffma2_rn(f2.az, m1, mz);
+	const float2 r2x = __ffma2_rn(f2.bx, m1, mx), r2y = __ffma2_rn(f2.by, m1, my);
+	const float2 r2z = __ffma2_rn(f2.bz, m1, mz);
+	const float2 r0x = __ffma2_rn(r2x, m1, r1x), r0y = __ffma2_rn(r2y, m1, r1y);
+	const float2 r0z = __ffma2_rn(r2z, m1, r1z);
+	const float2 cx = __ffma2_rn(r1y, r2z, neg2f(__fmul2_rn(r1z, r2y)));
+	const float2 cy = __ffma2_rn(r1z, r2x, neg2f(__fmul2_rn(r1x, r2z)));
+	const float2 cz = __ffma2_rn(r1x, r2y, neg2f(__fmul2_rn(r1y, r2x)));
+	const float2 cc = __ffma2_rn(cz, cz, __ffma2_rn(cy, cy, __fmul2_rn(cx, cx)));
+	const float2 q1 = __ffma2_rn(r1z, r1z, __ffma2_rn(r1y, r1y, __fmul2_rn(r1x, r1x)));
+	const float2 q2 = __ffma2_rn(r2z, r2z, __ffma2_rn(r2y, r2y, __fmul2_rn(r2x, r2x)));
+	const float2 l1 = make_float2(rsqrt_approx(q1.x), rsqrt_approx(q1.y));
+	const float2 l2 = make_float2(rsqrt_approx(q2.x), rsqrt_approx(q2.y));
+	const float2 t21 = __fmul2_rn(__ffma2_rn(r1z, r0z, __ffma2_rn(r1y, r0y, __fmul2_rn(r1x, r0x))), l1);
+	const float2 t22 = __fmul2_rn(__ffma2_rn(r2z, r0z, __ffma2_rn(r2y, r0y, __fmul2_rn(r2x, r0x))), l2);
+	const float2 t2 = __ffma2_rn(t22, m1, t21);
+	const float2 f = __fmul2_rn(__fmul2_rn(f2.ga, rcp2(cc)), t2);
+	const float2 cd = __ffma2_rn(cz, ez, __ffma2_rn(cy, ey, __fmul2_rn(cx, ex)));
+	float2 r = __fmul2_rn(f, cd);
+	// |t1 t2| <= FLT_MAX; NaN fails
+	r.x = fabsf(f.x) <= kBig ? r.x : 0.f;
+	r.y = fabsf(f.y) <= kBig ? r.y : 0.f;
+	return r;
+}
+
+template <int PAIRS, int UNROLL>
 __global__ void __launch_bounds__(kInfThreads) f3d_inf2_kernel(const F3DInfProblem p)
 {
+	constexpr int kInfRows = inf_rows<PAIRS>();
 	__shared__ float4 fs[2 * kInfFils];
 	const int tx = threadIdx.x & 31;          // filament quad
 	const int ty = threadIdx.x >> 5;          // point-pair lane
@@ -567,36 +608,50 @@ __global__ void __launch_bounds__(kInfThreads) f3d_inf2_kernel(const F3DInfProbl
 	__syncthreads();
 	const int j0 = j_base + 4 * tx;
 	if (j0 >= p.n_fil) return;
-	float4 fa[4], fb[4];
+	InfFil2 fil[4];
 #pragma unroll
-	for (int q = 0; q < 4; ++q) { fa[q] = fs[2 * (4 * tx + q)]; fb[q] = fs[2 * (4 * tx + q) + 1]; }
+	for (int q = 0; q < 4; ++q) {
+		const float4 a = fs[2 * (4 * tx + q)], b = fs[2 * (4 * tx + q) + 1];
+		fil[q].ax = bc2(a.x); fil[q].ay = bc2(a.y); fil[q].az = bc2(a.z);
+		fil[q].bx = bc2(b.x); fil[q].by = bc2(b.y); fil[q].bz = bc2(b.z);
+		fil[q].ga = bc2(a.w * kInv4PiF);
+	}
 	const bool vec = (p.n_fil & 3) == 0 && j0 + 3 < p.n_fil &&
 		(reinterpret_cast<uintptr_t>(p.out) & 15u) == 0;
-#pragma unroll 1
-	for (int k = 0; k < kInfPairs; ++k) {
-		const long long i0 = (long long)blockIdx.x * kInfRows + 2 * (ty + 8 * k);
-		if (i0 >= p.n_mes) break;
-		const int ia = int(i0);
-		const int ib = int(i0 + 1 < p.n_mes ? i0 + 1 : i0);
-		const float4 ma = p.mes[ia], mb = p.mes[ib];
-		const float4 da = p.dir[ia], db = p.dir[ib];
+	// rows i0, i0 + 1 of iteration k: i0 = base + 2 (ty + 8 k); the next
+	// pair's points and directions are loaded while this pair is evaluated
+	const long long base = (long long)blockIdx.x * kInfRows;
+	long long i0 = base + 2 * ty;
+	if (i0 >= p.n_mes) return;
+	auto load = [&](long long i, float4& ma, float4& mb, float4& da, float4& db) {
+		const int ia = int(i);
+		const int ib = int(i + 1 < p.n_mes ? i + 1 : i);
+		ma = p.mes[ia]; mb = p.mes[ib];
+		da = p.dir[ia]; db = p.dir[ib];
+	};
+	float4 ma, mb, da, db;
+	load(i0, ma, mb, da, db);
+#pragma unroll (UNROLL)
+	for (int k = 0; k < PAIRS; ++k) {
+		const long long in = i0 + 16;
+		const bool more = k + 1 < PAIRS && in < p.n_mes;
+		float4 na = ma, nb = mb, nda = da, ndb = db;
+		if (more) load(in, na, nb, nda, ndb);
+		float v2[2][4];   // [row][filament]
 		const float2 mx = make_float2(ma.x, mb.x), my = make_float2(ma.y, mb.y);
 		const float2 mz = make_float2(ma.z, mb.z);
-		const float2 dx = make_float2(da.x, db.x), dy = make_float2(da.y, db.y);
-		const float2 dz = make_float2(da.z, db.z);
-		float2 r[4];
+		const float2 ex = make_float2(da.x, db.x), ey = make_float2(da.y, db.y);
+		const float2 ez = make_float2(da.z, db.z);
 #pragma unroll
 		for (int q = 0; q < 4; ++q) {
-			float2 vx, vy, vz;
-			f3d_vel_pair2(mx, my, mz, fa[q], fb[q], vx, vy, vz);
-			r[q] = __ffma2_rn(vz, dz, __ffma2_rn(vy, dy, __fmul2_rn(vx, dx)));
+			const float2 r = f3d_inf_pair2(mx, my, mz, ex, ey, ez, fil[q]);
+			v2[0][q] = r.x; v2[1][q] = r.y;
 		}
 #pragma unroll
 		for (int e = 0; e < 2; ++e) {
 			if (e == 1 && i0 + 1 >= p.n_mes) break;
 			float* row = p.out + size_t(i0 + e) * p.n_fil;
-			const float v[4] = {e ? r[0].y : r[0].x, e ? r[1].y : r[1].x,
-				e ? r[2].y : r[2].x, e ? r[3].y : r[3].x};
+			const float* v = v2[e];
 			if (vec) {
 				*reinterpret_cast<float4*>(row + j0) = make_float4(v[0], v[1], v[2], v[3]);
 			} else {
@@ -604,6 +659,9 @@ __global__ void __launch_bounds__(kInfThreads) f3d_inf2_kernel(const F3DInfProbl
 				for (int q = 0; q < 4; ++q) if (j0 + q < p.n_fil) row[j0 + q] = v[q];
 			}
 		}
+		if (!more) break;
+		i0 = in;
+		ma = na; mb = nb; da = nda; db = ndb;
 	}
 }
 
@@ -718,13 +776,68 @@ cudaError_t f3d_dvort(const F3DDvortProblem& p, const LaunchEnv& env) {
 	return p.n_tgt < kSmallTargets ? launch_dvort<1, 128, false>(p, env)
 	                               : launch_dvort<2, 128, true>(p, env);
 }
+namespace {
+
+// Influence-matrix configurations (point pairs per thread, unroll):
+// 0 (4, 1), 1 (16, 1), 2 (16, 2), 3 (64, 1), 4 (64, 2), 5 (32, 2).
+// CVTX_GB300_INF_CFG forces one. Default: of 0, 1 and 3, the one with the
+// least (time per entry) / (fill of the last wave of CTAs); the time per
+// entry of each, relative to 1, is from GB300 timings (25,000 x 20,000:
+// 1.019 / 0.794 / 0.756 ms), where longer-lived CTAs amortise the filament
+// tile load.
+template <int PAIRS, int UNROLL>
+int inf_resident_ctas() {
+	static const int occ = resident_ctas(f3d_inf2_kernel<PAIRS, UNROLL>, kInfThreads, 0);
+	return occ;
+}
+
+int inf_cfg(const F3DInfProblem& p, int num_sms) {
+	static const int forced = [] {
+		const char* e = std::getenv("CVTX_GB300_INF_CFG");
+		if (!e || !*e) return -1;
+		const int c = std::atoi(e);
+		return (c >= 0 && c <= 5) ? c : -1;
+	}();
+	if (forced >= 0) return forced;
+	const double fil_tiles = double((p.n_fil + kInfFils - 1) / kInfFils);
+	const int cfgs[3] = {0, 1, 3};
+	const int rows[3] = {inf_rows<4>(), inf_rows<16>(), inf_rows<64>()};
+	const int occ[3] = {inf_resident_ctas<4, 1>(), inf_resident_ctas<16, 1>(),
+		inf_resident_ctas<64, 1>()};
+	const double per_entry[3] = {1.284, 1.0, 0.953};
+	int best = 1;
+	double best_cost = 1e300;
+	for (int c = 0; c < 3; ++c) {
+		const double ctas = std::ceil(double(p.n_mes) / rows[c]) * fil_tiles;
+		const double wave = double(num_sms) * (occ[c] > 0 ? occ[c] : 1);
+		const double fill = ctas / (std::ceil(ctas / wave) * wave);
+		const double cost = per_entry[c] / fill;
+		if (cost < best_cost) { best_cost = cost; best = cfgs[c]; }
+	}
+	return best;
+}
+
+template <int PAIRS, int UNROLL>
+void launch_inf2(const F3DInfProblem& p, long long fil_tiles, cudaStream_t stream) {
+	const long long row_tiles = (p.n_mes + inf_rows<PAIRS>() - 1) / inf_rows<PAIRS>();
+	f3d_inf2_kernel<PAIRS, UNROLL><<<dim3(unsigned(row_tiles), unsigned(fil_tiles)),
+		kInfThreads, 0, stream>>>(p);
+}
+
+}  // namespace
+
 cudaError_t f3d_inf_mtrx(const F3DInfProblem& p, const LaunchEnv& env) {
 	if (p.n_mes <= 0 || p.n_fil <= 0) return cudaSuccess;
-	const long long row_tiles = (p.n_mes + kInfRows - 1) / kInfRows;
 	const long long fil_tiles = (p.n_fil + kInfFils - 1) / kInfFils;
-	if (fil_tiles <= 65535 && row_tiles <= 0x7fffffffLL) {
-		f3d_inf2_kernel<<<dim3(unsigned(row_tiles), unsigned(fil_tiles)), kInfThreads, 0,
-			env.stream>>>(p);
+	if (fil_tiles <= 65535) {
+		switch (inf_cfg(p, env.num_sms)) {
+		case 1: launch_inf2<16, 1>(p, fil_tiles, env.stream); break;
+		case 2: launch_inf2<16, 2>(p, fil_tiles, env.stream); break;
+		case 3: launch_inf2<64, 1>(p, fil_tiles, env.stream); break;
+		case 4: launch_inf2<64, 2>(p, fil_tiles, env.stream); break;
+		case 5: launch_inf2<32, 2>(p, fil_tiles, env.stream); break;
+		default: launch_inf2<4, 1>(p, fil_tiles, env.stream); break;
+		}
 	} else {
 		// more than 8.4M filaments: the grid-stride form
 		const long long items = (long long)((p.n_fil + 3) / 4) * p.n_mes;
