@@ -535,6 +535,16 @@ def extras(cv, lib, args, torch, sh, peak):
     res["cube1M_winckelmans_veldvort"] = {
         "ginter_s": m * m / ms / 1e6, "ms": ms,
         "fp32_frac": 61 * m * m / (ms * 1e-3) / 1e12 / peak}
+    # the precision configuration's input: Gaussian, sigma 0.01, 1 % twins
+    # closer than 1e-3 sigma (its errors against FP64 come from the tests)
+    tw = workloads.cube_with_twins(m, 0.01)
+    rb.copy_(torch.from_numpy(p3d_records(tw).reshape(m, 8)))
+    f = lambda: lib.cvtx_gb300_dev_P3D_M2M(rb.data_ptr(), m, rb.data_ptr(), 2, m, b1.data_ptr(),
+                                           b2.data_ptr(), 3, 0.01, sh)
+    ms = timed_dev(f, torch, 2)
+    res["twins1M_gaussian_veldvort"] = {
+        "ginter_s": m * m / ms / 1e6, "ms": ms,
+        "fp32_frac": FLOPS[("veldvort", 3)] * m * m / (ms * 1e-3) / 1e12 / peak}
     return res
 
 
