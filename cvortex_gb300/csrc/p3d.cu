@@ -96,6 +96,70 @@ namespace {
 // when the cross products are.
 // Shared state per target (compensated across tiles): u (3, VEL), A' and B
 // (6, DV).
+//
+// One source-target pair in scalar FP32 into the register partials of one
+// target (layout above). d = t - s; sv = source vorticity; a = alpha_t.
+template <Reg R, bool VEL, bool DV, int NR>
+__device__ __forceinline__ void induce_pair(float dx, float dy, float dz, const float4 sv,
+	float ax, float ay, float az, const InduceConsts& kc, float (&acc)[NR])
+{
+	constexpr bool kFinite = FiniteAtZero<R>::value;
+	const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+	if (DV) {
+		const float ex = sv.x - ax;
+		const float ey = sv.y - ay;
+		const float ez = sv.z - az;
+		// c' = d x da
+		const float cx = fmaf(dy, ez, -dz * ey);
+		const float cy = fmaf(dz, ex, -dx * ez);
+		const float cz = fmaf(dx, ey, -dy * ex);
+		float G, K;
+		RegP3D<R>::gk(r2, kc.rc, G, K);
+		const bool nz = r2 > 0.f;
+		G = nz ? G : 0.f;
+		if (!kFinite) K = nz ? K : 0.f;
+		constexpr int o = VEL ? 6 : 0;
+		if (VEL) {
+			acc[0] = fmaf(G, cx, acc[0]);
+			acc[1] = fmaf(G, cy, acc[1]);
+			acc[2] = fmaf(G, cz, acc[2]);
+			acc[3] = fmaf(G, dx, acc[3]);
+			acc[4] = fmaf(G, dy, acc[4]);
+			acc[5] = fmaf(G, dz, acc[5]);
+		}
+		acc[o + 0] = fmaf(G, ex, acc[o + 0]);
+		acc[o + 1] = fmaf(G, ey, acc[o + 1]);
+		acc[o + 2] = fmaf(G, ez, acc[o + 2]);
+		const float pd = fmaf(az, cz, fmaf(ay, cy, ax * cx));
+		const float kk = K * pd;
+		acc[o + 3] = fmaf(kk, dx, acc[o + 3]);
+		acc[o + 4] = fmaf(kk, dy, acc[o + 4]);
+		acc[o + 5] = fmaf(kk, dz, acc[o + 5]);
+	} else {
+		// c = d x alpha_s
+		const float cx = fmaf(dy, sv.z, -dz * sv.y);
+		const float cy = fmaf(dz, sv.x, -dx * sv.z);
+		const float cz = fmaf(dx, sv.y, -dy * sv.x);
+		float G = RegP3D<R>::g(r2, kc.rc);
+		if (!kFinite) G = r2 > 0.f ? G : 0.f;
+		acc[0] = fmaf(G, cx, acc[0]);
+		acc[1] = fmaf(G, cy, acc[1]);
+		acc[2] = fmaf(G, cz, acc[2]);
+	}
+}
+
+// Fused vel + dvort: the velocity partial u' + W x alpha_t into slots 0..2.
+template <bool VEL, bool DV, int NR>
+__device__ __forceinline__ void induce_combine(float ax, float ay, float az, float (&acc)[NR])
+{
+	if (VEL && DV) {
+		const float wx = acc[3], wy = acc[4], wz = acc[5];
+		acc[0] += fmaf(wy, az, -wz * ay);
+		acc[1] += fmaf(wz, ax, -wx * az);
+		acc[2] += fmaf(wx, ay, -wy * ax);
+	}
+}
+
 template <Reg R, bool VEL, bool DV, int TPT, int NT>
 __global__ void __launch_bounds__(NT)
 p3d_induce_kernel(const P3DInduceProblem p, const InduceConsts kc,
@@ -103,7 +167,6 @@ p3d_induce_kernel(const P3DInduceProblem p, const InduceConsts kc,
 {
 	constexpr int NC = (VEL ? 3 : 0) + (DV ? 6 : 0);     // compensated sums
 	constexpr int NR = (VEL ? (DV ? 6 : 3) : 0) + (DV ? 6 : 0);  // register partials
-	constexpr bool kFinite = FiniteAtZero<R>::value;
 	extern __shared__ __align__(16) unsigned char smem[];
 	float* hi = reinterpret_cast<float*>(smem + Stream2::kSmemBytes);
 	float* lo = hi + NC * TPT * NT;
@@ -133,63 +196,19 @@ p3d_induce_kernel(const P3DInduceProblem p, const InduceConsts kc,
 	for (int i = 0; i < NC * TPT; ++i) { hi[i * NT + tid] = 0.f; lo[i * NT + tid] = 0.f; }
 
 	auto tile_fn = [&](const float4* __restrict__ st, int cnt) {
-		float acc[NR][TPT];
+		float acc[TPT][NR];
 #pragma unroll
-		for (int c = 0; c < NR; ++c)
+		for (int k = 0; k < TPT; ++k)
 #pragma unroll
-			for (int k = 0; k < TPT; ++k) acc[c][k] = 0.f;
+			for (int c = 0; c < NR; ++c) acc[k][c] = 0.f;
 
 		auto body = [&](int j) {
 			const float4 sp = st[2 * j];
 			const float4 sv = st[2 * j + 1];
 #pragma unroll
-			for (int k = 0; k < TPT; ++k) {
-				const float dx = tx[k] - sp.x;
-				const float dy = ty[k] - sp.y;
-				const float dz = tz[k] - sp.z;
-				const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-				if (DV) {
-					const float ex = sv.x - ax[k];
-					const float ey = sv.y - ay[k];
-					const float ez = sv.z - az[k];
-					// c' = d x da
-					const float cx = fmaf(dy, ez, -dz * ey);
-					const float cy = fmaf(dz, ex, -dx * ez);
-					const float cz = fmaf(dx, ey, -dy * ex);
-					float G, K;
-					RegP3D<R>::gk(r2, kc.rc, G, K);
-					const bool nz = r2 > 0.f;
-					G = nz ? G : 0.f;
-					if (!kFinite) K = nz ? K : 0.f;
-					constexpr int o = VEL ? 6 : 0;
-					if (VEL) {
-						acc[0][k] = fmaf(G, cx, acc[0][k]);
-						acc[1][k] = fmaf(G, cy, acc[1][k]);
-						acc[2][k] = fmaf(G, cz, acc[2][k]);
-						acc[3][k] = fmaf(G, dx, acc[3][k]);
-						acc[4][k] = fmaf(G, dy, acc[4][k]);
-						acc[5][k] = fmaf(G, dz, acc[5][k]);
-					}
-					acc[o + 0][k] = fmaf(G, ex, acc[o + 0][k]);
-					acc[o + 1][k] = fmaf(G, ey, acc[o + 1][k]);
-					acc[o + 2][k] = fmaf(G, ez, acc[o + 2][k]);
-					const float pd = fmaf(az[k], cz, fmaf(ay[k], cy, ax[k] * cx));
-					const float kk = K * pd;
-					acc[o + 3][k] = fmaf(kk, dx, acc[o + 3][k]);
-					acc[o + 4][k] = fmaf(kk, dy, acc[o + 4][k]);
-					acc[o + 5][k] = fmaf(kk, dz, acc[o + 5][k]);
-				} else {
-					// c = d x alpha_s
-					const float cx = fmaf(dy, sv.z, -dz * sv.y);
-					const float cy = fmaf(dz, sv.x, -dx * sv.z);
-					const float cz = fmaf(dx, sv.y, -dy * sv.x);
-					float G = RegP3D<R>::g(r2, kc.rc);
-					if (!kFinite) G = r2 > 0.f ? G : 0.f;
-					acc[0][k] = fmaf(G, cx, acc[0][k]);
-					acc[1][k] = fmaf(G, cy, acc[1][k]);
-					acc[2][k] = fmaf(G, cz, acc[2][k]);
-				}
-			}
+			for (int k = 0; k < TPT; ++k)
+				induce_pair<R, VEL, DV>(tx[k] - sp.x, ty[k] - sp.y, tz[k] - sp.z, sv,
+					ax[k], ay[k], az[k], kc, acc[k]);
 		};
 		if (cnt == kTile) {
 #pragma unroll 2
@@ -198,16 +217,8 @@ p3d_induce_kernel(const P3DInduceProblem p, const InduceConsts kc,
 #pragma unroll 1
 			for (int j = 0; j < cnt; ++j) body(j);
 		}
-		if (VEL && DV) {
-			// tile velocity u' + W x alpha_t into slots 0..2
 #pragma unroll
-			for (int k = 0; k < TPT; ++k) {
-				const float wx = acc[3][k], wy = acc[4][k], wz = acc[5][k];
-				acc[0][k] += fmaf(wy, az[k], -wz * ay[k]);
-				acc[1][k] += fmaf(wz, ax[k], -wx * az[k]);
-				acc[2][k] += fmaf(wx, ay[k], -wy * ax[k]);
-			}
-		}
+		for (int k = 0; k < TPT; ++k) induce_combine<VEL, DV>(ax[k], ay[k], az[k], acc[k]);
 #pragma unroll
 		for (int c = 0; c < NC; ++c) {
 			const int src_c = (VEL && DV && c >= 3) ? c + 3 : c;
@@ -215,7 +226,7 @@ p3d_induce_kernel(const P3DInduceProblem p, const InduceConsts kc,
 			for (int k = 0; k < TPT; ++k) {
 				const int i = (c * TPT + k) * NT + tid;
 				float h = hi[i], l = lo[i];
-				fold_twosum(h, l, acc[src_c][k]);
+				fold_twosum(h, l, acc[k][src_c]);
 				hi[i] = h; lo[i] = l;
 			}
 		}
@@ -290,6 +301,123 @@ __global__ void p3d_induce_finalize(const P3DInduceProblem p, const InduceConsts
 		ax = tv.x; ay = tv.y; az = tv.z;
 	}
 	write_induce<VEL, DV>(p, kc, t, s, ax, ay, az);
+}
+
+// Few targets, many sources (the reference's small-target / M2S case,
+// src/nbody.cl:258-292 with host-side partial sums): CTA (x, y) takes targets
+// [TT y, TT y + TT) and the source chunk [chunk_len x, chunk_len (x + 1)).
+// Each thread strides over the chunk (coalesced 32-byte records) with the
+// TT targets in registers and FP32 partials; the CTA then reduces every
+// partial in FP64, by warp shuffles and then across warps in a fixed order,
+// into one FP64 partial per chunk, stored target-major
+// (partial[(t NC + c) n_chunks + chunk]), that p3d_induce_finalize_wide
+// reduces with a whole CTA per target. Every thread does useful work
+// whatever the target count.
+constexpr int kFewThreads = 256;
+constexpr int kFewMinChunk = 8 * kFewThreads;    // sources per CTA, at least
+
+template <Reg R, bool VEL, bool DV, int TT>
+__global__ void __launch_bounds__(kFewThreads)
+p3d_induce_few_kernel(const P3DInduceProblem p, const InduceConsts kc,
+	double* __restrict__ partial, int chunk_len)
+{
+	constexpr int NC = InduceNC<VEL, DV>::value;
+	constexpr int NR = (VEL ? (DV ? 6 : 3) : 0) + (DV ? 6 : 0);
+	constexpr int kWarps = kFewThreads / 32;
+	__shared__ double red[kWarps][TT * NC];
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const int t0 = blockIdx.y * TT;
+	float tx[TT], ty[TT], tz[TT], ax[TT], ay[TT], az[TT];
+#pragma unroll
+	for (int k = 0; k < TT; ++k) {
+		const int t = t0 + k < p.n_tgt ? t0 + k : p.n_tgt - 1;
+		const float4 tp = p.tgt[size_t(t) * p.tstride];
+		tx[k] = tp.x; ty[k] = tp.y; tz[k] = tp.z;
+		if (DV) {
+			const float4 tv = p.tgt[size_t(t) * p.tstride + 1];
+			ax[k] = tv.x; ay[k] = tv.y; az[k] = tv.z;
+		} else {
+			ax[k] = ay[k] = az[k] = 0.f;
+		}
+	}
+	float acc[TT][NR];
+#pragma unroll
+	for (int k = 0; k < TT; ++k)
+#pragma unroll
+		for (int c = 0; c < NR; ++c) acc[k][c] = 0.f;
+	const long long s0 = (long long)blockIdx.x * chunk_len;
+	long long s1 = s0 + chunk_len;
+	s1 = s1 < p.n_src ? s1 : p.n_src;
+	for (long long s = s0 + tid; s < s1; s += kFewThreads) {
+		const float4 sp = p.src[2 * s];
+		const float4 sv = p.src[2 * s + 1];
+#pragma unroll
+		for (int k = 0; k < TT; ++k)
+			induce_pair<R, VEL, DV>(tx[k] - sp.x, ty[k] - sp.y, tz[k] - sp.z, sv,
+				ax[k], ay[k], az[k], kc, acc[k]);
+	}
+#pragma unroll
+	for (int k = 0; k < TT; ++k) {
+		induce_combine<VEL, DV>(ax[k], ay[k], az[k], acc[k]);
+#pragma unroll
+		for (int c = 0; c < NC; ++c) {
+			const int src_c = (VEL && DV && c >= 3) ? c + 3 : c;
+			double v = double(acc[k][src_c]);
+#pragma unroll
+			for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+			if (lane == 0) red[warp][k * NC + c] = v;
+		}
+	}
+	__syncthreads();
+	for (int i = tid; i < TT * NC; i += kFewThreads) {
+		const int k = i / NC, c = i - k * NC;
+		if (t0 + k >= p.n_tgt) continue;
+		double v = 0.0;
+#pragma unroll
+		for (int w = 0; w < kWarps; ++w) v += red[w][i];
+		partial[(size_t(t0 + k) * NC + c) * gridDim.x + blockIdx.x] = v;
+	}
+}
+
+// Combine target-major chunk partials: CTA t, threads over chunks in a fixed
+// assignment, then a fixed shuffle / cross-warp tree; deterministic.
+template <bool VEL, bool DV>
+__global__ void __launch_bounds__(kFewThreads)
+p3d_induce_finalize_wide(const P3DInduceProblem p, const InduceConsts kc,
+	const double* __restrict__ partial, int n_chunks)
+{
+	constexpr int NC = InduceNC<VEL, DV>::value;
+	constexpr int kWarps = kFewThreads / 32;
+	__shared__ double red[kWarps][NC];
+	const int t = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	double s[NC];
+#pragma unroll
+	for (int c = 0; c < NC; ++c) s[c] = 0.0;
+	for (int k = tid; k < n_chunks; k += kFewThreads)
+#pragma unroll
+		for (int c = 0; c < NC; ++c) s[c] += partial[(size_t(t) * NC + c) * n_chunks + k];
+#pragma unroll
+	for (int c = 0; c < NC; ++c) {
+		double v = s[c];
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+		if (lane == 0) red[warp][c] = v;
+	}
+	__syncthreads();
+	if (tid != 0) return;
+	double tot[NC];
+#pragma unroll
+	for (int c = 0; c < NC; ++c) {
+		tot[c] = 0.0;
+#pragma unroll
+		for (int w = 0; w < kWarps; ++w) tot[c] += red[w][c];
+	}
+	float ax = 0.f, ay = 0.f, az = 0.f;
+	if (DV) {
+		const float4 tv = p.tgt[size_t(t) * p.tstride + 1];
+		ax = tv.x; ay = tv.y; az = tv.z;
+	}
+	write_induce<VEL, DV>(p, kc, t, tot, ax, ay, az);
 }
 
 // ---------------------------------------------------------------------------
@@ -731,17 +859,19 @@ constexpr size_t smem_bytes() {
 // ---- induce launch configurations ------------------------------------------
 // A configuration is (targets per thread, threads per CTA, packed f32x2 or
 // scalar arithmetic). The table below is what the autotuner chooses from;
-// without a tuned entry, fewer than kSmallTargets targets use configuration 0
-// (one target per thread, so the source dimension can be split across more
-// CTAs) and larger problems the measured per-(regularisation, ops) choice of
-// kMidCfg / kLargeCfg below.
+// without a tuned entry, up to few_max_targets() targets use configuration 10
+// (p3d_induce_few_kernel: sources spread over the threads), fewer than
+// kSmallTargets configuration 0 (one target per thread, so the source
+// dimension can be split across more CTAs) and larger problems the measured
+// per-(regularisation, ops) choice of kMidCfg / kLargeCfg below.
 constexpr int kSmallTargets = 8192;
+constexpr int kFewCfg = 10;
 
 struct CfgSpec { int tpt, nt; bool packed; };
 constexpr CfgSpec kCfg[] = {
 	{1, 128, false}, {4, 128, false}, {4, 128, true}, {2, 128, true},
 	{4, 64, true},   {2, 256, true},  {6, 64, true},  {4, 128, true},
-	{4, 128, true},  {2, 128, true},
+	{4, 128, true},  {2, 128, true},  {4, 256, false},   // 10: few targets (TT = 4 or 8)
 };
 // Configurations 7-9 repeat shapes with another source-loop unroll factor
 // (7: 1, 8 and 9: 4; all others 2). (Also timed on a GB300 and left out:
@@ -764,9 +894,10 @@ struct InduceVariant {
 		static const int occ = resident_ctas(fn(), NT, kSmem);
 		return occ;
 	}
+	// max_split < 0: this kernel's own cap (64 splits)
 	static Plan plan(int n_src, int n_tgt, int num_sms, int max_split) {
 		return make_plan(n_src, n_tgt, TPT * NT, PK ? TILE : kTile, NC, num_sms * occupancy(), kSmem,
-			max_split);
+			max_split < 0 ? 64 : max_split);
 	}
 	static cudaError_t launch(const Plan& pl, const P3DInduceProblem& p, const LaunchEnv& env) {
 		if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
@@ -784,6 +915,54 @@ struct InduceVariant {
 	}
 };
 
+// The few-target form as a configuration: Plan.n_tblocks = target groups of
+// TT, n_split = source chunks (at least kFewMinChunk sources each, about two
+// waves of CTAs, at most max_split or 4,096), src_per_split = chunk length.
+template <Reg R, bool VEL, bool DV>
+struct FewVariant {
+	static constexpr int NC = InduceNC<VEL, DV>::value;
+	static constexpr int kTT = (VEL && !DV) ? 8 : 4;
+	static int tt(int n_tgt) { return n_tgt == 1 ? 1 : kTT; }   // targets per CTA
+	static int occupancy() {
+		static const int occ = resident_ctas(p3d_induce_few_kernel<R, VEL, DV, kTT>, kFewThreads, 0);
+		return occ;
+	}
+	static Plan plan(int n_src, int n_tgt, int num_sms, int max_split) {
+		Plan pl;
+		const int TT = tt(n_tgt);
+		pl.n_tblocks = std::max(1, (n_tgt + TT - 1) / TT);
+		const long long want = 2LL * num_sms * occupancy();
+		long long chunks = (want + pl.n_tblocks - 1) / pl.n_tblocks;
+		chunks = std::min<long long>(chunks, std::max(1, n_src / kFewMinChunk));
+		chunks = std::min<long long>(chunks, max_split < 0 ? 4096 : max_split);
+		chunks = std::max<long long>(chunks, 1);
+		int len = int((n_src + chunks - 1) / chunks);
+		len = std::max(32, (len + 31) / 32 * 32);
+		pl.src_per_split = len;
+		pl.n_split = std::max(1, (n_src + len - 1) / len);
+		pl.smem = 0;
+		pl.ws_bytes = size_t(pl.n_split) * NC * size_t(n_tgt) * sizeof(double);
+		return pl;
+	}
+	static cudaError_t launch(const Plan& pl, const P3DInduceProblem& p, const LaunchEnv& env) {
+		if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
+		const InduceConsts kc = make_induce_consts(int(R), p.sigma);
+		double* partial = static_cast<double*>(env.ws);
+		const dim3 grid(pl.n_split, pl.n_tblocks);
+		if (tt(p.n_tgt) == 1)
+			p3d_induce_few_kernel<R, VEL, DV, 1><<<grid, kFewThreads, 0, env.stream>>>(
+				p, kc, partial, pl.src_per_split);
+		else
+			p3d_induce_few_kernel<R, VEL, DV, kTT><<<grid, kFewThreads, 0, env.stream>>>(
+				p, kc, partial, pl.src_per_split);
+		count_launch();
+		p3d_induce_finalize_wide<VEL, DV><<<p.n_tgt, kFewThreads, 0, env.stream>>>(
+			p, kc, partial, pl.n_split);
+		count_launch();
+		return cudaGetLastError();
+	}
+};
+
 template <Reg R, bool VEL, bool DV, class F>
 auto with_cfg(int ci, F&& f) {
 	switch (ci) {
@@ -796,7 +975,8 @@ auto with_cfg(int ci, F&& f) {
 	case 6: return f(InduceVariant<R, VEL, DV, 6, 64, true>{});
 	case 7: return f(InduceVariant<R, VEL, DV, 4, 128, true, 1>{});
 	case 8: return f(InduceVariant<R, VEL, DV, 4, 128, true, 4>{});
-	default: return f(InduceVariant<R, VEL, DV, 2, 128, true, 4>{});
+	case 9: return f(InduceVariant<R, VEL, DV, 2, 128, true, 4>{});
+	default: return f(FewVariant<R, VEL, DV>{});
 	}
 }
 
@@ -845,11 +1025,26 @@ constexpr signed char kMidCfg[4][4] = {
 constexpr signed char kLargeCfg[4][4] = {
 	{2, 3, 5, 3}, {2, 6, 6, 2}, {2, 4, 2, 2}, {2, 6, 4, 9}};
 
-int choose_cfg(int reg, unsigned ops, int n_tgt) {
+// Largest target count for the few-target form, from GB300 timings against
+// configuration 0 (vortex ring, vel and vel+dvort, 1 to 2,048 targets): it
+// is faster up to 256 targets at 100,000 sources and up to 2,048 at
+// 1,000,000, where the split form's 64-split cap leaves SMs idle.
+// CVTX_GB300_FEW_MAX overrides it.
+int few_max_targets(int n_src) {
+	static const int forced = [] {
+		const char* e = std::getenv("CVTX_GB300_FEW_MAX");
+		return (e && *e) ? std::atoi(e) : -1;
+	}();
+	if (forced >= 0) return forced;
+	return n_src >= 262144 ? 2048 : 256;
+}
+
+int choose_cfg(int reg, unsigned ops, int n_tgt, int n_src) {
 	const int forced = env_cfg();
 	if (forced >= 0) return forced;
 	const int t = g_tuned[reg & 3][ops & 3][size_bucket(n_tgt)].load(std::memory_order_relaxed);
 	if (t >= 0 && t < kNumCfg) return t;
+	if (n_tgt <= few_max_targets(n_src)) return kFewCfg;
 	if (n_tgt < kSmallTargets) return 0;
 	return n_tgt < 32768 ? kMidCfg[reg & 3][ops & 3] : kLargeCfg[reg & 3][ops & 3];
 }
@@ -859,7 +1054,7 @@ size_t induce_ws(int reg, unsigned ops, int n_src, int n_tgt, int num_sms, int c
 		constexpr Reg R = decltype(rt)::value;
 		constexpr bool VEL = decltype(vt)::value, DV = decltype(dt)::value;
 		return with_cfg<R, VEL, DV>(cfg, [&](auto var) {
-			return decltype(var)::plan(n_src, n_tgt, num_sms, 64).ws_bytes;
+			return decltype(var)::plan(n_src, n_tgt, num_sms, -1).ws_bytes;
 		});
 	});
 }
@@ -873,7 +1068,7 @@ cudaError_t induce_launch(int reg, unsigned ops, const P3DInduceProblem& p, cons
 			using V = decltype(var);
 			// capped: the FP64 split partials must fit env.ws_bytes
 			const int max_split = (bounded || env.cap_to_ws)
-				? split_cap_for(env.ws_bytes, V::NC, p.n_tgt) : 64;
+				? split_cap_for(env.ws_bytes, V::NC, p.n_tgt) : -1;
 			return V::launch(V::plan(p.n_src, p.n_tgt, env.num_sms, max_split), p, env);
 		});
 	});
@@ -960,20 +1155,20 @@ cudaError_t launch_vort(const P3DVortProblem& p, const LaunchEnv& env) {
 
 size_t p3d_induce_ws_bytes(int reg, unsigned ops, int n_src, int n_tgt, int num_sms) {
 	if (n_tgt <= 0) return 0;
-	return induce_ws(reg, ops, n_src, n_tgt, num_sms, choose_cfg(reg, ops, n_tgt));
+	return induce_ws(reg, ops, n_src, n_tgt, num_sms, choose_cfg(reg, ops, n_tgt, n_src));
 }
 
 cudaError_t p3d_induce(int reg, unsigned ops, const P3DInduceProblem& p, const LaunchEnv& env) {
 	if (p.n_tgt <= 0) return cudaSuccess;
 	if (reg < 0 || reg > 3 || ops < 1 || ops > 3) return cudaErrorInvalidValue;
-	return induce_launch(reg, ops, p, env, choose_cfg(reg, ops, p.n_tgt), false);
+	return induce_launch(reg, ops, p, env, choose_cfg(reg, ops, p.n_tgt, p.n_src), false);
 }
 
 cudaError_t p3d_induce_bounded(int reg, unsigned ops, const P3DInduceProblem& p,
 	const LaunchEnv& env) {
 	if (p.n_tgt <= 0) return cudaSuccess;
 	if (reg < 0 || reg > 3 || ops < 1 || ops > 3) return cudaErrorInvalidValue;
-	return induce_launch(reg, ops, p, env, choose_cfg(reg, ops, p.n_tgt), true);
+	return induce_launch(reg, ops, p, env, choose_cfg(reg, ops, p.n_tgt, p.n_src), true);
 }
 
 int p3d_induce_num_configs() { return kNumCfg; }
@@ -992,7 +1187,7 @@ bool p3d_induce_set_tuned(int reg, unsigned ops, int bucket, int cfg) {
 }
 
 int p3d_induce_current_config(int reg, unsigned ops, int n_tgt) {
-	return choose_cfg(reg & 3, ops & 3, n_tgt);
+	return choose_cfg(reg & 3, ops & 3, n_tgt, 0);
 }
 
 size_t p3d_visc_ws_bytes(int reg, int n_src, int n_tgt, int num_sms) {

@@ -66,8 +66,12 @@ CVTX_EXPORT int cvtx_gb300_probe_fp32_mix(int packed, int scalar, int repeats,
 /* Launch configurations of the P3D velocity / stretching kernels (targets
  * per thread, threads per CTA, packed two-wide FP32 arithmetic or scalar) and
  * the table that selects one per (reg, ops, target-count bucket); ops: 1 vel,
- * 2 dvort, 3 both; cfg -1 restores the built-in choice. The autotuner in
- * cvortex_gb300/autotune.py fills the table. */
+ * 2 dvort, 3 both; cfg -1 restores the built-in choice. The last
+ * configuration is the few-target form (sources spread over the threads of
+ * a CTA, reduced in FP64), which the built-in choice takes up to 256 targets,
+ * or 2,048 from 262,144 sources; cvtx_gb300_p3d_current_config reports the
+ * choice for fewer sources. The autotuner in cvortex_gb300/autotune.py fills
+ * the table. */
 CVTX_EXPORT int cvtx_gb300_p3d_num_configs(void);
 CVTX_EXPORT int cvtx_gb300_p3d_config_info(int cfg, int* tpt, int* nt, int* packed);
 CVTX_EXPORT int cvtx_gb300_size_bucket(int n_targets);

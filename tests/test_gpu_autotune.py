@@ -36,7 +36,7 @@ def test_tune_installs_and_keeps_parity(gpu, tmp_path):
         lib.cvtx_gb300_p3d_set_tuned(1, 3, b, -1)
 
 
-@pytest.mark.parametrize("cfg", range(10))
+@pytest.mark.parametrize("cfg", range(11))
 def test_every_configuration_matches_oracle(gpu, cfg):
     lib = gpu.lib
     n = 9000

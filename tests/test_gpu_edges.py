@@ -68,6 +68,21 @@ def test_few_targets_many_sources(gpu, reg):
     check(gpu.p3d_dvort(p, q, reg, 0.05), oracle.p3d_dvort(p, q, reg, 0.05), reg, y, x, 0.05, ed)
 
 
+@pytest.mark.parametrize("reg", REGS)
+@pytest.mark.parametrize("n_tgt", [1, 5, 9, 100, 512])
+def test_few_targets_every_op(gpu, reg, n_tgt):
+    """The few-target kernel (sources spread over the threads, FP64
+    shuffle reduction, fixed-order chunk sums): ragged target groups, a
+    source count that does not fill its last chunk, targets on sources."""
+    p = workloads.vortex_ring(200_003, seed=51)
+    q = workloads.vortex_ring(n_tgt, seed=52)
+    q["coord"][: min(2, n_tgt)] = p["coord"][:min(2, n_tgt)]
+    x, y = p["coord"], q["coord"]
+    ev, ed = oracle.exact_p3d_vel_dvort(p, y, q["vorticity"], reg, 0.05)
+    check(gpu.p3d_vel(p, y, reg, 0.05), oracle.p3d_vel(p, y, reg, 0.05), reg, y, x, 0.05, ev)
+    check(gpu.p3d_dvort(p, q, reg, 0.05), oracle.p3d_dvort(p, q, reg, 0.05), reg, y, x, 0.05, ed)
+
+
 def test_many_targets_few_sources(gpu):
     p = workloads.uniform_cube(3, seed=45)
     mes = workloads.uniform_cube(40_000, seed=46)["coord"]
