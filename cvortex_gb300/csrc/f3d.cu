@@ -14,6 +14,7 @@
 #include "plan.cuh"
 #include "regfuncs.cuh"
 #include "tile_stream.cuh"
+#include "few.cuh"
 
 namespace cvtx {
 namespace {
@@ -728,18 +729,53 @@ cudaError_t launch_dvort(const F3DDvortProblem& p, const LaunchEnv& env) {
 
 }  // namespace
 
+// The F3D velocity pair as an operation of the few-target form (few.cuh):
+// the same per-pair arithmetic as f3d_vel_kernel (f3d_vel_pair).
+struct F3DVelOp {
+	using Problem = F3DVelProblem;
+	struct Consts { int unused; };
+	static constexpr int NC = 3, NR = 3;
+	struct Tgt { float x, y, z; };
+	struct Src { float4 a, b; };
+	__device__ static int n_src(const Problem& p) { return p.n_fil; }
+	__device__ static int n_tgt(const Problem& p) { return p.n_tgt; }
+	__device__ static Tgt target(const Problem& p, int t) {
+		const float4 q = p.tgt[size_t(t) * p.tstride];
+		return Tgt{q.x, q.y, q.z};
+	}
+	__device__ static Src source(const Problem& p, long long s) {
+		return Src{p.fil[2 * s], p.fil[2 * s + 1]};
+	}
+	__device__ static void pair(const Consts&, const Tgt& t, const Src& s, float (&acc)[NR]) {
+		float vx, vy, vz;
+		f3d_vel_pair(t.x, t.y, t.z, s.a, s.b, vx, vy, vz);
+		acc[0] += vx; acc[1] += vy; acc[2] += vz;
+	}
+	__device__ static void combine(const Tgt&, float (&)[NR]) {}
+	__device__ static int slot(int c) { return c; }
+	__device__ static void write(const Problem& p, const Consts&, int t, const double* s) {
+		p.out[3 * size_t(t)] = float(s[0]);
+		p.out[3 * size_t(t) + 1] = float(s[1]);
+		p.out[3 * size_t(t) + 2] = float(s[2]);
+	}
+};
+using F3DFew = FewForm<F3DVelOp, 4>;
+constexpr int kF3DFewCfg = 5;   // the few-target form
+
 // Velocity launch configurations: 0 scalar (1 target/thread, 128 threads),
-// 1 scalar (4, 128), 2 packed (4, 128), 3 packed (2, 128), 4 packed (2, 256).
-// Default from GB300 timings (wake sheet, 20,000 and 100,000 points): 0 below
-// kSmallTargets targets, else 4; CVTX_GB300_F3D_CFG forces one.
-int f3d_vel_cfg(int n_tgt) {
+// 1 scalar (4, 128), 2 packed (4, 128), 3 packed (2, 128), 4 packed (2, 256),
+// 5 the few-target form. Default from GB300 timings (wake sheet, 20,000 and
+// 100,000 points): 5 up to few_max_targets_vel2() targets, 0 below
+// kSmallTargets, else 4; CVTX_GB300_F3D_CFG forces one.
+int f3d_vel_cfg(int n_tgt, int n_fil) {
 	static const int forced = [] {
 		const char* e = std::getenv("CVTX_GB300_F3D_CFG");
 		if (!e || !*e) return -1;
 		const int c = std::atoi(e);
-		return (c >= 0 && c <= 4) ? c : -1;
+		return (c >= 0 && c <= kF3DFewCfg) ? c : -1;
 	}();
 	if (forced >= 0) return forced;
+	if (n_tgt <= few_max_targets_vel2(n_fil)) return kF3DFewCfg;
 	return n_tgt < kSmallTargets ? 0 : 4;
 }
 template <class F>
@@ -755,14 +791,21 @@ auto with_vel_cfg(int cfg, F&& f) {
 
 size_t f3d_vel_ws_bytes(int n_fil, int n_tgt, int num_sms) {
 	if (n_tgt <= 0) return 0;
-	return with_vel_cfg(f3d_vel_cfg(n_tgt), [&](auto t, auto n, auto pk) {
+	if (f3d_vel_cfg(n_tgt, n_fil) == kF3DFewCfg)
+		return F3DFew::plan(n_fil, n_tgt, num_sms, -1).ws_bytes;
+	return with_vel_cfg(f3d_vel_cfg(n_tgt, n_fil), [&](auto t, auto n, auto pk) {
 		return plan_vel<decltype(t)::value, decltype(n)::value, decltype(pk)::value>(
 			n_fil, n_tgt, num_sms).ws_bytes;
 	});
 }
 cudaError_t f3d_vel(const F3DVelProblem& p, const LaunchEnv& env) {
 	if (p.n_tgt <= 0) return cudaSuccess;
-	return with_vel_cfg(f3d_vel_cfg(p.n_tgt), [&](auto t, auto n, auto pk) {
+	if (f3d_vel_cfg(p.n_tgt, p.n_fil) == kF3DFewCfg) {
+		const Plan pl = F3DFew::plan(p.n_fil, p.n_tgt, env.num_sms,
+			env.cap_to_ws ? split_cap_for(env.ws_bytes, 3, p.n_tgt) : -1);
+		return F3DFew::launch(pl, p, F3DVelOp::Consts{0}, p.n_tgt, env);
+	}
+	return with_vel_cfg(f3d_vel_cfg(p.n_tgt, p.n_fil), [&](auto t, auto n, auto pk) {
 		return launch_vel<decltype(t)::value, decltype(n)::value, decltype(pk)::value>(p, env);
 	});
 }

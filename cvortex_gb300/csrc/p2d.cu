@@ -12,6 +12,7 @@
 #include "plan.cuh"
 #include "regfuncs.cuh"
 #include "tile_stream.cuh"
+#include "few.cuh"
 
 namespace cvtx {
 RegConsts make_reg_consts_host(float sigma);
@@ -442,21 +443,57 @@ cudaError_t launch_visc(const P2DViscProblem& p, const LaunchEnv& env) {
 
 // Velocity launch configurations: 0 scalar (1 target/thread, 128 threads),
 // 1 scalar (4, 128), 2 packed (4, 128), 3 packed (2, 128), 4 packed (8, 128),
-// 5 packed (4, 256). Default from GB300 timings (Gaussian patch, 20,000 and
-// 200,000 targets): 0 below kSmallTargets targets, 3 up to 65,535, else 2;
+// 5 packed (4, 256), 6 the few-target form. Default from GB300 timings
+// (Gaussian patch, 20,000 and 200,000 targets): 6 up to
+// few_max_targets_vel2() targets, 0 below kSmallTargets, 3 up to 65,535,
+// else 2;
 // CVTX_GB300_P2D_CFG forces one.
+constexpr int kP2DFewCfg = 6;   // the few-target form (few.cuh)
 int p2d_env_cfg() {
 	static const int v = [] {
 		const char* e = std::getenv("CVTX_GB300_P2D_CFG");
 		if (!e || !*e) return -1;
 		const int c = std::atoi(e);
-		return (c >= 0 && c <= 5) ? c : -1;
+		return (c >= 0 && c <= kP2DFewCfg) ? c : -1;
 	}();
 	return v;
 }
-int vel_cfg(int n_tgt) {
+// The P2D velocity pair as an operation of the few-target form (few.cuh):
+// the same per-pair arithmetic as p2d_vel_kernel.
+template <Reg R>
+struct P2DVelOp {
+	using Problem = P2DVelProblem;
+	struct Consts { RegConsts rc; double scale; };
+	static constexpr int NC = 2, NR = 2;
+	struct Tgt { float x, y; };
+	using Src = float4;
+	__device__ static int n_src(const Problem& p) { return p.n_src; }
+	__device__ static int n_tgt(const Problem& p) { return p.n_tgt; }
+	__device__ static Tgt target(const Problem& p, int t) { const float4 q = p.tgt[t]; return Tgt{q.x, q.y}; }
+	__device__ static Src source(const Problem& p, long long s) { return p.src[s]; }
+	__device__ static void pair(const Consts& k, const Tgt& t, const Src& s, float (&acc)[NR]) {
+		const float dx = t.x - s.x;
+		const float dy = t.y - s.y;
+		const float r2 = fmaf(dy, dy, dx * dx);
+		float h = RegP2D<R>::h(r2, k.rc);
+		if (!HFinite<R>::value) h = r2 > 0.f ? h : 0.f;
+		const float hg = h * s.z;
+		acc[0] = fmaf(hg, dy, acc[0]);
+		acc[1] = fmaf(-hg, dx, acc[1]);
+	}
+	__device__ static void combine(const Tgt&, float (&)[NR]) {}
+	__device__ static int slot(int c) { return c; }
+	__device__ static void write(const Problem& p, const Consts& k, int t, const double* s) {
+		p.out[2 * size_t(t)] = float(k.scale * s[0]);
+		p.out[2 * size_t(t) + 1] = float(k.scale * s[1]);
+	}
+};
+template <Reg R> using P2DFew = FewForm<P2DVelOp<R>, 8>;
+
+int vel_cfg(int n_tgt, int n_src) {
 	const int f = p2d_env_cfg();
 	if (f >= 0) return f;
+	if (n_tgt <= few_max_targets_vel2(n_src)) return kP2DFewCfg;
 	return n_tgt < kSmallTargets ? 0 : n_tgt < 65536 ? 3 : 2;
 }
 template <Reg R, class F>
@@ -472,14 +509,22 @@ auto with_vel_cfg(int cfg, F&& f) {
 }
 template <Reg R>
 size_t ws_vel_r(int n_src, int n_tgt, int num_sms) {
-	return with_vel_cfg<R>(vel_cfg(n_tgt), [&](auto t, auto n, auto pk) {
+	if (vel_cfg(n_tgt, n_src) == kP2DFewCfg)
+		return P2DFew<R>::plan(n_src, n_tgt, num_sms, -1).ws_bytes;
+	return with_vel_cfg<R>(vel_cfg(n_tgt, n_src), [&](auto t, auto n, auto pk) {
 		return plan_vel<R, decltype(t)::value, decltype(n)::value, decltype(pk)::value>(
 			n_src, n_tgt, num_sms).ws_bytes;
 	});
 }
 template <Reg R>
 cudaError_t vel_r(const P2DVelProblem& p, const LaunchEnv& env) {
-	return with_vel_cfg<R>(vel_cfg(p.n_tgt), [&](auto t, auto n, auto pk) {
+	if (vel_cfg(p.n_tgt, p.n_src) == kP2DFewCfg) {
+		const Plan pl = P2DFew<R>::plan(p.n_src, p.n_tgt, env.num_sms,
+			env.cap_to_ws ? split_cap_for(env.ws_bytes, 2, p.n_tgt) : -1);
+		typename P2DVelOp<R>::Consts k{make_reg_consts_host(p.sigma), vel_scale(int(R), p.sigma)};
+		return P2DFew<R>::launch(pl, p, k, p.n_tgt, env);
+	}
+	return with_vel_cfg<R>(vel_cfg(p.n_tgt, p.n_src), [&](auto t, auto n, auto pk) {
 		return launch_vel<R, decltype(t)::value, decltype(n)::value, decltype(pk)::value>(p, env);
 	});
 }

@@ -23,8 +23,13 @@
 #include "plan.cuh"
 #include "regfuncs.cuh"
 #include "p3d_induce.cuh"
+#include "few.cuh"
 
 namespace cvtx {
+
+// Largest target count for the few-target form of the P3D velocity /
+// stretching kernels, by source count (defined below).
+int few_max_targets(int n_src);
 
 RegConsts make_reg_consts_host(float sigma) {
 	RegConsts c;
@@ -303,122 +308,43 @@ __global__ void p3d_induce_finalize(const P3DInduceProblem p, const InduceConsts
 	write_induce<VEL, DV>(p, kc, t, s, ax, ay, az);
 }
 
-// Few targets, many sources (the reference's small-target / M2S case,
-// src/nbody.cl:258-292 with host-side partial sums): CTA (x, y) takes targets
-// [TT y, TT y + TT) and the source chunk [chunk_len x, chunk_len (x + 1)).
-// Each thread strides over the chunk (coalesced 32-byte records) with the
-// TT targets in registers and FP32 partials; the CTA then reduces every
-// partial in FP64, by warp shuffles and then across warps in a fixed order,
-// into one FP64 partial per chunk, stored target-major
-// (partial[(t NC + c) n_chunks + chunk]), that p3d_induce_finalize_wide
-// reduces with a whole CTA per target. Every thread does useful work
-// whatever the target count.
-constexpr int kFewThreads = 256;
-constexpr int kFewMinChunk = 8 * kFewThreads;    // sources per CTA, at least
-
-template <Reg R, bool VEL, bool DV, int TT>
-__global__ void __launch_bounds__(kFewThreads)
-p3d_induce_few_kernel(const P3DInduceProblem p, const InduceConsts kc,
-	double* __restrict__ partial, int chunk_len)
-{
-	constexpr int NC = InduceNC<VEL, DV>::value;
-	constexpr int NR = (VEL ? (DV ? 6 : 3) : 0) + (DV ? 6 : 0);
-	constexpr int kWarps = kFewThreads / 32;
-	__shared__ double red[kWarps][TT * NC];
-	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-	const int t0 = blockIdx.y * TT;
-	float tx[TT], ty[TT], tz[TT], ax[TT], ay[TT], az[TT];
-#pragma unroll
-	for (int k = 0; k < TT; ++k) {
-		const int t = t0 + k < p.n_tgt ? t0 + k : p.n_tgt - 1;
+// The P3D velocity / stretching pair as an operation of the few-target form
+// (few.cuh): the same per-pair arithmetic as p3d_induce_kernel.
+template <Reg R, bool VEL, bool DV>
+struct P3DInduceOp {
+	using Problem = P3DInduceProblem;
+	using Consts = InduceConsts;
+	static constexpr int NC = InduceNC<VEL, DV>::value;
+	static constexpr int NR = (VEL ? (DV ? 6 : 3) : 0) + (DV ? 6 : 0);
+	struct Tgt { float x, y, z, ax, ay, az; };
+	struct Src { float4 pos, vort; };
+	__device__ static int n_src(const Problem& p) { return p.n_src; }
+	__device__ static int n_tgt(const Problem& p) { return p.n_tgt; }
+	__device__ static Tgt target(const Problem& p, int t) {
 		const float4 tp = p.tgt[size_t(t) * p.tstride];
-		tx[k] = tp.x; ty[k] = tp.y; tz[k] = tp.z;
+		Tgt g{tp.x, tp.y, tp.z, 0.f, 0.f, 0.f};
 		if (DV) {
 			const float4 tv = p.tgt[size_t(t) * p.tstride + 1];
-			ax[k] = tv.x; ay[k] = tv.y; az[k] = tv.z;
-		} else {
-			ax[k] = ay[k] = az[k] = 0.f;
+			g.ax = tv.x; g.ay = tv.y; g.az = tv.z;
 		}
+		return g;
 	}
-	float acc[TT][NR];
-#pragma unroll
-	for (int k = 0; k < TT; ++k)
-#pragma unroll
-		for (int c = 0; c < NR; ++c) acc[k][c] = 0.f;
-	const long long s0 = (long long)blockIdx.x * chunk_len;
-	long long s1 = s0 + chunk_len;
-	s1 = s1 < p.n_src ? s1 : p.n_src;
-	for (long long s = s0 + tid; s < s1; s += kFewThreads) {
-		const float4 sp = p.src[2 * s];
-		const float4 sv = p.src[2 * s + 1];
-#pragma unroll
-		for (int k = 0; k < TT; ++k)
-			induce_pair<R, VEL, DV>(tx[k] - sp.x, ty[k] - sp.y, tz[k] - sp.z, sv,
-				ax[k], ay[k], az[k], kc, acc[k]);
+	__device__ static Src source(const Problem& p, long long s) {
+		return Src{p.src[2 * s], p.src[2 * s + 1]};
 	}
-#pragma unroll
-	for (int k = 0; k < TT; ++k) {
-		induce_combine<VEL, DV>(ax[k], ay[k], az[k], acc[k]);
-#pragma unroll
-		for (int c = 0; c < NC; ++c) {
-			const int src_c = (VEL && DV && c >= 3) ? c + 3 : c;
-			double v = double(acc[k][src_c]);
-#pragma unroll
-			for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-			if (lane == 0) red[warp][k * NC + c] = v;
-		}
+	__device__ static void pair(const Consts& k, const Tgt& t, const Src& s, float (&acc)[NR]) {
+		induce_pair<R, VEL, DV>(t.x - s.pos.x, t.y - s.pos.y, t.z - s.pos.z, s.vort,
+			t.ax, t.ay, t.az, k, acc);
 	}
-	__syncthreads();
-	for (int i = tid; i < TT * NC; i += kFewThreads) {
-		const int k = i / NC, c = i - k * NC;
-		if (t0 + k >= p.n_tgt) continue;
-		double v = 0.0;
-#pragma unroll
-		for (int w = 0; w < kWarps; ++w) v += red[w][i];
-		partial[(size_t(t0 + k) * NC + c) * gridDim.x + blockIdx.x] = v;
+	__device__ static void combine(const Tgt& t, float (&acc)[NR]) {
+		induce_combine<VEL, DV>(t.ax, t.ay, t.az, acc);
 	}
-}
-
-// Combine target-major chunk partials: CTA t, threads over chunks in a fixed
-// assignment, then a fixed shuffle / cross-warp tree; deterministic.
-template <bool VEL, bool DV>
-__global__ void __launch_bounds__(kFewThreads)
-p3d_induce_finalize_wide(const P3DInduceProblem p, const InduceConsts kc,
-	const double* __restrict__ partial, int n_chunks)
-{
-	constexpr int NC = InduceNC<VEL, DV>::value;
-	constexpr int kWarps = kFewThreads / 32;
-	__shared__ double red[kWarps][NC];
-	const int t = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-	double s[NC];
-#pragma unroll
-	for (int c = 0; c < NC; ++c) s[c] = 0.0;
-	for (int k = tid; k < n_chunks; k += kFewThreads)
-#pragma unroll
-		for (int c = 0; c < NC; ++c) s[c] += partial[(size_t(t) * NC + c) * n_chunks + k];
-#pragma unroll
-	for (int c = 0; c < NC; ++c) {
-		double v = s[c];
-#pragma unroll
-		for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-		if (lane == 0) red[warp][c] = v;
+	__device__ static int slot(int c) { return (VEL && DV && c >= 3) ? c + 3 : c; }
+	__device__ static void write(const Problem& p, const Consts& k, int t, const double* s) {
+		const Tgt g = target(p, t);
+		write_induce<VEL, DV>(p, k, t, s, g.ax, g.ay, g.az);
 	}
-	__syncthreads();
-	if (tid != 0) return;
-	double tot[NC];
-#pragma unroll
-	for (int c = 0; c < NC; ++c) {
-		tot[c] = 0.0;
-#pragma unroll
-		for (int w = 0; w < kWarps; ++w) tot[c] += red[w][c];
-	}
-	float ax = 0.f, ay = 0.f, az = 0.f;
-	if (DV) {
-		const float4 tv = p.tgt[size_t(t) * p.tstride + 1];
-		ax = tv.x; ay = tv.y; az = tv.z;
-	}
-	write_induce<VEL, DV>(p, kc, t, tot, ax, ay, az);
-}
+};
 
 // ---------------------------------------------------------------------------
 // Viscous vorticity exchange (PSE), reference src/P3D.cpp:116-144:
@@ -915,51 +841,17 @@ struct InduceVariant {
 	}
 };
 
-// The few-target form as a configuration: Plan.n_tblocks = target groups of
-// TT, n_split = source chunks (at least kFewMinChunk sources each, about two
-// waves of CTAs, at most max_split or 4,096), src_per_split = chunk length.
+// The few-target form (few.cuh) as configuration 10: Plan.n_tblocks =
+// target groups, n_split = source chunks, src_per_split = chunk length.
 template <Reg R, bool VEL, bool DV>
 struct FewVariant {
 	static constexpr int NC = InduceNC<VEL, DV>::value;
-	static constexpr int kTT = (VEL && !DV) ? 8 : 4;
-	static int tt(int n_tgt) { return n_tgt == 1 ? 1 : kTT; }   // targets per CTA
-	static int occupancy() {
-		static const int occ = resident_ctas(p3d_induce_few_kernel<R, VEL, DV, kTT>, kFewThreads, 0);
-		return occ;
-	}
+	using Form = FewForm<P3DInduceOp<R, VEL, DV>, (VEL && !DV) ? 8 : 4>;
 	static Plan plan(int n_src, int n_tgt, int num_sms, int max_split) {
-		Plan pl;
-		const int TT = tt(n_tgt);
-		pl.n_tblocks = std::max(1, (n_tgt + TT - 1) / TT);
-		const long long want = 2LL * num_sms * occupancy();
-		long long chunks = (want + pl.n_tblocks - 1) / pl.n_tblocks;
-		chunks = std::min<long long>(chunks, std::max(1, n_src / kFewMinChunk));
-		chunks = std::min<long long>(chunks, max_split < 0 ? 4096 : max_split);
-		chunks = std::max<long long>(chunks, 1);
-		int len = int((n_src + chunks - 1) / chunks);
-		len = std::max(32, (len + 31) / 32 * 32);
-		pl.src_per_split = len;
-		pl.n_split = std::max(1, (n_src + len - 1) / len);
-		pl.smem = 0;
-		pl.ws_bytes = size_t(pl.n_split) * NC * size_t(n_tgt) * sizeof(double);
-		return pl;
+		return Form::plan(n_src, n_tgt, num_sms, max_split);
 	}
 	static cudaError_t launch(const Plan& pl, const P3DInduceProblem& p, const LaunchEnv& env) {
-		if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
-		const InduceConsts kc = make_induce_consts(int(R), p.sigma);
-		double* partial = static_cast<double*>(env.ws);
-		const dim3 grid(pl.n_split, pl.n_tblocks);
-		if (tt(p.n_tgt) == 1)
-			p3d_induce_few_kernel<R, VEL, DV, 1><<<grid, kFewThreads, 0, env.stream>>>(
-				p, kc, partial, pl.src_per_split);
-		else
-			p3d_induce_few_kernel<R, VEL, DV, kTT><<<grid, kFewThreads, 0, env.stream>>>(
-				p, kc, partial, pl.src_per_split);
-		count_launch();
-		p3d_induce_finalize_wide<VEL, DV><<<p.n_tgt, kFewThreads, 0, env.stream>>>(
-			p, kc, partial, pl.n_split);
-		count_launch();
-		return cudaGetLastError();
+		return Form::launch(pl, p, make_induce_consts(int(R), p.sigma), p.n_tgt, env);
 	}
 };
 
@@ -1024,20 +916,6 @@ constexpr signed char kMidCfg[4][4] = {
 	{2, 3, 5, 3}, {2, 3, 0, 2}, {2, 3, 0, 2}, {2, 6, 5, 3}};
 constexpr signed char kLargeCfg[4][4] = {
 	{2, 3, 5, 3}, {2, 6, 6, 2}, {2, 4, 2, 2}, {2, 6, 4, 9}};
-
-// Largest target count for the few-target form, from GB300 timings against
-// configuration 0 (vortex ring, vel and vel+dvort, 1 to 2,048 targets): it
-// is faster up to 256 targets at 100,000 sources and up to 2,048 at
-// 1,000,000, where the split form's 64-split cap leaves SMs idle.
-// CVTX_GB300_FEW_MAX overrides it.
-int few_max_targets(int n_src) {
-	static const int forced = [] {
-		const char* e = std::getenv("CVTX_GB300_FEW_MAX");
-		return (e && *e) ? std::atoi(e) : -1;
-	}();
-	if (forced >= 0) return forced;
-	return n_src >= 262144 ? 2048 : 256;
-}
 
 int choose_cfg(int reg, unsigned ops, int n_tgt, int n_src) {
 	const int forced = env_cfg();
@@ -1152,6 +1030,25 @@ cudaError_t launch_vort(const P3DVortProblem& p, const LaunchEnv& env) {
 }
 
 }  // namespace
+
+// Largest target count for the few-target form, from GB300 timings against
+// configuration 0 (vortex ring, vel and vel+dvort, 1 to 2,048 targets): it
+// is faster up to 256 targets at 100,000 sources and up to 2,048 at
+// 1,000,000, where the split form's 64-split cap leaves SMs idle.
+// CVTX_GB300_FEW_MAX overrides it.
+int few_max_override() {
+	static const int forced = [] {
+		const char* e = std::getenv("CVTX_GB300_FEW_MAX");
+		return (e && *e) ? std::atoi(e) : -1;
+	}();
+	return forced;
+}
+
+int few_max_targets(int n_src) {
+	const int forced = few_max_override();
+	if (forced >= 0) return forced;
+	return n_src >= 262144 ? 2048 : 256;
+}
 
 size_t p3d_induce_ws_bytes(int reg, unsigned ops, int n_src, int n_tgt, int num_sms) {
 	if (n_tgt <= 0) return 0;

@@ -94,7 +94,7 @@ def test_inf_configs(tmp_path):
             assert np.array_equal(r[f"inf{nf}"], runs[0][f"inf{nf}"])
 
 
-@pytest.mark.parametrize("cfg", range(6))
+@pytest.mark.parametrize("cfg", range(7))
 def test_p2d_configs(tmp_path, cfg):
     got = run_child(tmp_path, "p2d", "CVTX_GB300_P2D_CFG", cfg)
     q = workloads.gaussian_patch_2d(9001, seed=66)
@@ -104,7 +104,7 @@ def test_p2d_configs(tmp_path, cfg):
     check(got["visc_g"][SAMPLE], oracle.p2d_visc(q, q[SAMPLE], "gaussian", 0.05, 1e-3), tol=1e-5)
 
 
-@pytest.mark.parametrize("cfg", range(5))
+@pytest.mark.parametrize("cfg", range(6))
 def test_f3d_vel_configs(tmp_path, cfg):
     got = run_child(tmp_path, "f3d", "CVTX_GB300_F3D_CFG", cfg)
     f = workloads.wake_sheet(3000, seed=67)

@@ -83,6 +83,23 @@ def test_few_targets_every_op(gpu, reg, n_tgt):
     check(gpu.p3d_dvort(p, q, reg, 0.05), oracle.p3d_dvort(p, q, reg, 0.05), reg, y, x, 0.05, ed)
 
 
+@pytest.mark.parametrize("n_tgt", [1, 7, 100])
+def test_few_targets_p2d_f3d(gpu, n_tgt):
+    """The few-target form of P2D and F3D velocity: targets on sources, at
+    filament ends and on a filament (the reference drops those terms)."""
+    q = workloads.gaussian_patch_2d(300_001, seed=53)
+    m = workloads.gaussian_patch_2d(n_tgt, seed=54)["coord"].copy()
+    m[0] = q["coord"][0]
+    for reg in REGS:
+        close(gpu.p2d_vel(q, m, reg, 0.05), oracle.p2d_vel(q, m, reg, 0.05))
+    f = workloads.wake_sheet(100_003, seed=55)
+    t = workloads.sheet_targets(n_tgt, seed=56)
+    t[0] = f["start"][5]
+    if n_tgt > 2:
+        t[1] = 0.5 * (f["start"][9] + f["end"][9])
+    close(gpu.f3d_vel(f, t), oracle.f3d_vel(f, t))
+
+
 def test_many_targets_few_sources(gpu):
     p = workloads.uniform_cube(3, seed=45)
     mes = workloads.uniform_cube(40_000, seed=46)["coord"]
