@@ -159,7 +159,10 @@ def cpu_cores():
         return os.cpu_count() or 1
 
 
-def cpu_baseline(p, reg, reps=3, sample=CPU_SAMPLE_TARGETS):
+def cpu_baseline(p, reg, min_s=12.0, max_reps=40, sample=CPU_SAMPLE_TARGETS):
+    """The reference CPU formulation on all host cores: vel + dvort for
+    `sample` seeded targets against all sources, repeated until about `min_s`
+    seconds of CPU work (at least three repeats)."""
     os.environ.setdefault("OMP_NUM_THREADS", str(cpu_cores()))
     os.environ.setdefault("OMP_PROC_BIND", "spread")
     kind, ref = cpu_reference()
@@ -167,8 +170,10 @@ def cpu_baseline(p, reg, reps=3, sample=CPU_SAMPLE_TARGETS):
     sub = p[np.sort(idx)].copy()
     cpu_step(kind, ref, p, sub[:64].copy(), reg)   # warm caches / thread pool
     t0 = time.perf_counter()
-    for _ in range(reps):
+    reps = 0
+    while reps < 3 or (time.perf_counter() - t0 < min_s and reps < max_reps):
         cpu_step(kind, ref, p, sub, reg)
+        reps += 1
     dt = time.perf_counter() - t0
     pairs = reps * len(sub) * len(p)
     return {"value": pairs / dt / 1e9, "unit": UNIT, "cores": int(os.environ["OMP_NUM_THREADS"]),
