@@ -55,42 +55,47 @@ few_targets_kernel(const typename Op::Problem p, const typename Op::Consts k,
 	__shared__ double red[kWarps][TT * NC];
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 	const int n_tgt = Op::n_tgt(p);
-	const int t0 = blockIdx.y * TT;
-	typename Op::Tgt tg[TT];
+	const int n_groups = (n_tgt + TT - 1) / TT;
+	// target groups blockIdx.y, + gridDim.y, ... (grid.y is at most 65,535)
+	for (int grp = blockIdx.y; grp < n_groups; grp += gridDim.y) {
+		const int t0 = grp * TT;
+		typename Op::Tgt tg[TT];
 #pragma unroll
-	for (int q = 0; q < TT; ++q) tg[q] = Op::target(p, t0 + q < n_tgt ? t0 + q : n_tgt - 1);
-	float acc[TT][NR];
+		for (int q = 0; q < TT; ++q) tg[q] = Op::target(p, t0 + q < n_tgt ? t0 + q : n_tgt - 1);
+		float acc[TT][NR];
 #pragma unroll
-	for (int q = 0; q < TT; ++q)
+		for (int q = 0; q < TT; ++q)
 #pragma unroll
-		for (int c = 0; c < NR; ++c) acc[q][c] = 0.f;
-	const long long s0 = (long long)blockIdx.x * chunk_len;
-	long long s1 = s0 + chunk_len;
-	s1 = s1 < Op::n_src(p) ? s1 : Op::n_src(p);
-	for (long long s = s0 + tid; s < s1; s += kFewThreads) {
-		const typename Op::Src sr = Op::source(p, s);
+			for (int c = 0; c < NR; ++c) acc[q][c] = 0.f;
+		const long long s0 = (long long)blockIdx.x * chunk_len;
+		long long s1 = s0 + chunk_len;
+		s1 = s1 < Op::n_src(p) ? s1 : Op::n_src(p);
+		for (long long s = s0 + tid; s < s1; s += kFewThreads) {
+			const typename Op::Src sr = Op::source(p, s);
 #pragma unroll
-		for (int q = 0; q < TT; ++q) Op::pair(k, tg[q], sr, acc[q]);
-	}
-#pragma unroll
-	for (int q = 0; q < TT; ++q) {
-		Op::combine(tg[q], acc[q]);
-#pragma unroll
-		for (int c = 0; c < NC; ++c) {
-			double v = double(acc[q][Op::slot(c)]);
-#pragma unroll
-			for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-			if (lane == 0) red[warp][q * NC + c] = v;
+			for (int q = 0; q < TT; ++q) Op::pair(k, tg[q], sr, acc[q]);
 		}
-	}
-	__syncthreads();
-	for (int i = tid; i < TT * NC; i += kFewThreads) {
-		const int q = i / NC, c = i - q * NC;
-		if (t0 + q >= n_tgt) continue;
-		double v = 0.0;
 #pragma unroll
-		for (int w = 0; w < kWarps; ++w) v += red[w][i];
-		partial[(size_t(t0 + q) * NC + c) * gridDim.x + blockIdx.x] = v;
+		for (int q = 0; q < TT; ++q) {
+			Op::combine(tg[q], acc[q]);
+#pragma unroll
+			for (int c = 0; c < NC; ++c) {
+				double v = double(acc[q][Op::slot(c)]);
+#pragma unroll
+				for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+				if (lane == 0) red[warp][q * NC + c] = v;
+			}
+		}
+		__syncthreads();
+		for (int i = tid; i < TT * NC; i += kFewThreads) {
+			const int q = i / NC, c = i - q * NC;
+			if (t0 + q >= n_tgt) continue;
+			double v = 0.0;
+#pragma unroll
+			for (int w = 0; w < kWarps; ++w) v += red[w][i];
+			partial[(size_t(t0 + q) * NC + c) * gridDim.x + blockIdx.x] = v;
+		}
+		__syncthreads();   // red is reused by the next group
 	}
 }
 
@@ -166,7 +171,7 @@ struct FewForm {
 		const typename Op::Consts& k, int n_tgt, const LaunchEnv& env) {
 		if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
 		double* partial = static_cast<double*>(env.ws);
-		const dim3 grid(pl.n_split, pl.n_tblocks);
+		const dim3 grid(pl.n_split, std::min(pl.n_tblocks, 65535));
 		if (tt(n_tgt) == 1)
 			few_targets_kernel<Op, 1><<<grid, kFewThreads, 0, env.stream>>>(p, k, partial,
 				pl.src_per_split);

@@ -100,6 +100,23 @@ def test_few_targets_p2d_f3d(gpu, n_tgt):
     close(gpu.f3d_vel(f, t), oracle.f3d_vel(f, t))
 
 
+def test_few_target_form_beyond_grid_limit(gpu):
+    """The few-target form forced (tuning table) on 300,000 stretching
+    targets: 75,000 groups of four, more than one grid dimension holds, so
+    CTAs loop over target groups."""
+    p = workloads.vortex_ring(3000, seed=57)
+    q = workloads.uniform_cube(300_000, seed=58)
+    lib = gpu.lib
+    bucket = lib.cvtx_gb300_size_bucket(len(q))
+    lib.cvtx_gb300_p3d_set_tuned(1, 2, bucket, 10)
+    try:
+        dv = gpu.p3d_dvort(p, q, "winckelmans", 0.05)
+    finally:
+        lib.cvtx_gb300_p3d_set_tuned(1, 2, bucket, -1)
+    idx = np.r_[0:100, 150_000:150_100, 299_900:300_000]
+    close(dv[idx], oracle.p3d_dvort(p, q[idx], "winckelmans", 0.05))
+
+
 def test_many_targets_few_sources(gpu):
     p = workloads.uniform_cube(3, seed=45)
     mes = workloads.uniform_cube(40_000, seed=46)["coord"]
