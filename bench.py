@@ -39,8 +39,8 @@ import numpy as np
 
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
-# the serving measurement runs up to 64 slots x 8 priority streams; more
-# hardware queues keep unrelated streams from serialising behind each other
+# the serving measurement runs 32 slots, one hardware work queue each, so
+# that no request's kernels queue behind another request's
 os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 METRIC = "P3D M2M vel+dvort Ginteractions/s"
@@ -695,7 +695,7 @@ def serve_extra(cv, lib, count=64, steps=10, dt=1e-3, rates=SERVE_RATES):
            "mix": {"p3d_vel_dvort": int((kinds == 0).sum()), "p2d_vel": int((kinds == 1).sum()),
                    "f3d_vel": int((kinds == 2).sum())},
            "sizes": [int(sizes.min()), int(sizes.max())], "interactions": pairs, "rates": {}}
-    srv = serve.Server(lib, n_slots=64)
+    srv = serve.Server(lib, n_slots=32)
     try:
         warm = build()[:4]                        # first-use costs out of the timed runs
         for r in warm:

@@ -678,10 +678,10 @@ auto vel_kernel() {
 }
 
 template <int TPT, int NT, bool PK>
-Plan plan_vel(int n_fil, int n_tgt, int num_sms, int max_split = 64) {
+Plan plan_vel(int n_fil, int n_tgt, int num_sms, int max_split = 64, int min_split = 1) {
 	constexpr size_t smem = smem_bytes<TPT, NT>();
 	static const int occ = resident_ctas(vel_kernel<TPT, NT, PK>(), NT, smem);
-	return make_plan(n_fil, n_tgt, TPT * NT, kTile, 3, num_sms * occ, smem, max_split);
+	return make_plan(n_fil, n_tgt, TPT * NT, kTile, 3, num_sms * occ, smem, max_split, min_split);
 }
 template <int TPT, int NT, bool PK>
 auto dvort_kernel() {
@@ -699,7 +699,7 @@ Plan plan_dvort(int n_fil, int n_tgt, int num_sms, int max_split = 64) {
 template <int TPT, int NT, bool PK>
 cudaError_t launch_vel(const F3DVelProblem& p, const LaunchEnv& env) {
 	const Plan pl = plan_vel<TPT, NT, PK>(p.n_fil, p.n_tgt, env.num_sms,
-		env.cap_to_ws ? split_cap_for(env.ws_bytes, 3, p.n_tgt) : 64);
+		env.cap_to_ws ? split_cap_for(env.ws_bytes, 3, p.n_tgt) : 64, min_split_for(env, p.n_fil));
 	if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
 	double* partial = static_cast<double*>(env.ws);
 	vel_kernel<TPT, NT, PK>()<<<dim3(pl.n_tblocks, pl.n_split), NT, pl.smem, env.stream>>>(

@@ -88,7 +88,18 @@ struct LaunchEnv {
 	// When set, launchers cap the number of source splits so that the split
 	// partials fit ws_bytes (for callers with a fixed-size workspace).
 	bool cap_to_ws = false;
+	// When > 0, the P3D / P2D / F3D velocity launchers use at least
+	// ceil(n_src / cta_src_cap) source splits (within the caps above), which
+	// bounds how long one CTA holds its SM: the CUDA block scheduler does not
+	// preempt running CTAs, so this bounds how long a higher-priority launch
+	// waits for one.
+	int cta_src_cap = 0;
 };
+
+// The fewest source splits a launch takes under env.cta_src_cap.
+inline int min_split_for(const LaunchEnv& env, int n_src) {
+	return env.cta_src_cap > 0 ? (n_src + env.cta_src_cap - 1) / env.cta_src_cap : 1;
+}
 
 // Largest split count whose FP64 partials (nc sums per target) fit `ws_bytes`.
 inline int split_cap_for(size_t ws_bytes, int nc, int n_tgt) {

@@ -375,10 +375,10 @@ auto vel_kernel() {
 }
 
 template <Reg R, int TPT, int NT, bool PK>
-Plan plan_vel(int n_src, int n_tgt, int num_sms, int max_split = 64) {
+Plan plan_vel(int n_src, int n_tgt, int num_sms, int max_split = 64, int min_split = 1) {
 	constexpr size_t smem = smem_bytes<TPT, NT, 2>();
 	static const int occ = resident_ctas(vel_kernel<R, TPT, NT, PK>(), NT, smem);
-	return make_plan(n_src, n_tgt, TPT * NT, kTile, 2, num_sms * occ, smem, max_split);
+	return make_plan(n_src, n_tgt, TPT * NT, kTile, 2, num_sms * occ, smem, max_split, min_split);
 }
 
 // Reference scale 1/(2 pi) (src/P2D.cpp:118); Winckelmans and Gaussian H are
@@ -393,7 +393,7 @@ double vel_scale(int reg, float sigma) {
 template <Reg R, int TPT, int NT, bool PK>
 cudaError_t launch_vel(const P2DVelProblem& p, const LaunchEnv& env) {
 	const Plan pl = plan_vel<R, TPT, NT, PK>(p.n_src, p.n_tgt, env.num_sms,
-		env.cap_to_ws ? split_cap_for(env.ws_bytes, 2, p.n_tgt) : 64);
+		env.cap_to_ws ? split_cap_for(env.ws_bytes, 2, p.n_tgt) : 64, min_split_for(env, p.n_src));
 	if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
 	const RegConsts rc = make_reg_consts_host(p.sigma);
 	const double scale = vel_scale(int(R), p.sigma);

@@ -821,9 +821,9 @@ struct InduceVariant {
 		return occ;
 	}
 	// max_split < 0: this kernel's own cap (64 splits)
-	static Plan plan(int n_src, int n_tgt, int num_sms, int max_split) {
+	static Plan plan(int n_src, int n_tgt, int num_sms, int max_split, int min_split = 1) {
 		return make_plan(n_src, n_tgt, TPT * NT, PK ? TILE : kTile, NC, num_sms * occupancy(), kSmem,
-			max_split < 0 ? 64 : max_split);
+			max_split < 0 ? 64 : max_split, min_split);
 	}
 	static cudaError_t launch(const Plan& pl, const P3DInduceProblem& p, const LaunchEnv& env) {
 		if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
@@ -847,7 +847,7 @@ template <Reg R, bool VEL, bool DV>
 struct FewVariant {
 	static constexpr int NC = InduceNC<VEL, DV>::value;
 	using Form = FewForm<P3DInduceOp<R, VEL, DV>, (VEL && !DV) ? 8 : 4>;
-	static Plan plan(int n_src, int n_tgt, int num_sms, int max_split) {
+	static Plan plan(int n_src, int n_tgt, int num_sms, int max_split, int = 1) {
 		return Form::plan(n_src, n_tgt, num_sms, max_split);
 	}
 	static cudaError_t launch(const Plan& pl, const P3DInduceProblem& p, const LaunchEnv& env) {
@@ -947,7 +947,8 @@ cudaError_t induce_launch(int reg, unsigned ops, const P3DInduceProblem& p, cons
 			// capped: the FP64 split partials must fit env.ws_bytes
 			const int max_split = (bounded || env.cap_to_ws)
 				? split_cap_for(env.ws_bytes, V::NC, p.n_tgt) : -1;
-			return V::launch(V::plan(p.n_src, p.n_tgt, env.num_sms, max_split), p, env);
+			return V::launch(V::plan(p.n_src, p.n_tgt, env.num_sms, max_split,
+				min_split_for(env, p.n_src)), p, env);
 		});
 	});
 }

@@ -36,7 +36,7 @@ inline int resident_ctas(K kernel, int nt, size_t smem) {
 }
 
 inline Plan make_plan(int n_src, int n_tgt, int targets_per_cta, int tile, int nc,
-	int capacity, size_t smem, int max_split = 64)
+	int capacity, size_t smem, int max_split = 64, int min_split = 1)
 {
 	Plan pl;
 	pl.smem = smem;
@@ -45,9 +45,11 @@ inline Plan make_plan(int n_src, int n_tgt, int targets_per_cta, int tile, int n
 	// At least four tiles of sources per split keeps the copy pipeline busy.
 	int cap_split = n_src / (4 * tile);
 	cap_split = std::max(1, std::min(max_split, cap_split));
-	int best_s = 1;
+	// min_split: the caller's bound on sources per CTA, within the caps
+	const int lo_split = std::max(1, std::min(min_split, cap_split));
+	int best_s = lo_split;
 	double best_eff = -1.0;
-	for (int s = 1; s <= cap_split; ++s) {
+	for (int s = lo_split; s <= cap_split; ++s) {
 		const double waves = double(pl.n_tblocks) * s / double(capacity);
 		const double eff = waves / std::ceil(waves);
 		if (eff > best_eff + 0.02) { best_eff = eff; best_s = s; }

@@ -18,9 +18,13 @@
 //    others are on the GPU run beside them. A slot has one stream per CUDA
 //    stream priority level, and a request runs at a priority set by its
 //    work per step (smaller = higher), so the block scheduler serves the CTAs
-//    of small requests ahead of the waves of large ones. (More streams than
-//    hardware queues alias onto shared queues: serving processes should set
-//    CUDA_DEVICE_MAX_CONNECTIONS=32 before CUDA starts.)
+//    of small requests ahead of the waves of large ones. Running CTAs are
+//    not preempted, so served launches bound the sources per CTA
+//    (kCtaSrcCap) and a small request's kernel waits at most ~2 ms for SMs.
+//    The default 32 slots match the hardware work queues at
+//    CUDA_DEVICE_MAX_CONNECTIONS=32, which serving processes should set
+//    before CUDA starts; the streams are created so that slots do not share
+//    a queue.
 //  * Determinism. A launch's source partition and reduction order depend only
 //    on its problem size and the slot workspace size (equal for all slots),
 //    never on what else is in flight, so a result is bit-identical alone and
@@ -59,9 +63,17 @@ double now_s() {
 }
 
 constexpr size_t kAlign = 256;
-constexpr size_t kSlotWsBytes = size_t(64) << 20;        // split partials per slot
+// Split partials per slot: enough for the splits that kCtaSrcCap asks of a
+// 200,000-particle step (25 splits x 9 FP64 sums x 200,000 targets = 360 MB).
+constexpr size_t kSlotWsBytes = size_t(512) << 20;
+// Sources per CTA in served launches: about 2 ms of FMA work per CTA for
+// the fused P3D kernel, so a newly launched high-priority kernel waits at
+// most that long for SMs held by the CTAs of large requests.
+constexpr int kCtaSrcCap = 8192;
 constexpr size_t kStagingBytes = size_t(1) << 30;        // pinned staging arena
 constexpr size_t kDefaultMaxHbm = size_t(64) << 30;
+// One slot per hardware work queue at CUDA_DEVICE_MAX_CONNECTIONS=32.
+constexpr int kDefaultSlots = 32;
 constexpr int kMaxLevels = 8;                              // stream priority levels used
 constexpr size_t kKeepFinished = size_t(1) << 20;          // finished records kept
 inline size_t up(size_t b) { return (b + kAlign - 1) & ~(kAlign - 1); }
@@ -232,6 +244,7 @@ class Server {
 	void finish(int s, std::unique_lock<std::mutex>& lk);
 	void complete_locked(Request& q, int status);
 	cudaError_t launch(Request& q, Slot& sl);
+	cudaError_t warm_up();
 	bool can_admit() const {
 		return !queue_.empty() && !free_slots_.empty() && !mem_blocked_;
 	}
@@ -284,7 +297,7 @@ void CUDART_CB on_slot_done(void* p) {
 
 bool Server::open(int n_slots, size_t hbm, bool dry, std::string* why) {
 	dry_ = dry;
-	if (n_slots <= 0) n_slots = 64;
+	if (n_slots <= 0) n_slots = kDefaultSlots;
 	if (n_slots > 256) n_slots = 256;
 	slots_.resize(size_t(n_slots));
 	if (!dry_) {
@@ -312,10 +325,17 @@ bool Server::open(int n_slots, size_t hbm, bool dry, std::string* why) {
 		// numerically lower = higher priority; hi_pri <= lo_pri
 		levels_ = std::min(kMaxLevels, lo_pri - hi_pri + 1);
 		if (levels_ < 1) levels_ = 1;
+		// Streams are created level by level, slot by slot. CUDA maps streams
+		// onto its hardware work queues in creation order, so with n_slots
+		// equal to the queue count (CUDA_DEVICE_MAX_CONNECTIONS) a slot's
+		// streams of every level share one queue and no two slots share one:
+		// a request never waits in a queue behind another request's kernels.
+		for (int l = 0; e == cudaSuccess && l < levels_; ++l)
+			for (int i = 0; e == cudaSuccess && i < n_slots; ++i)
+				e = cudaStreamCreateWithPriority(&slots_[size_t(i)].st[l], cudaStreamNonBlocking,
+					hi_pri + l);
 		for (int i = 0; e == cudaSuccess && i < n_slots; ++i) {
 			Slot& s = slots_[size_t(i)];
-			for (int l = 0; e == cudaSuccess && l < levels_; ++l)
-				e = cudaStreamCreateWithPriority(&s.st[l], cudaStreamNonBlocking, hi_pri + l);
 			if (e == cudaSuccess) e = cudaMalloc(&s.ws, kSlotWsBytes);
 			if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&s.d_err), sizeof(unsigned));
 			if (e == cudaSuccess) e = cudaHostAlloc(reinterpret_cast<void**>(&s.h_err), sizeof(unsigned),
@@ -332,9 +352,68 @@ bool Server::open(int n_slots, size_t hbm, bool dry, std::string* why) {
 		slots_[size_t(i)].index = i;
 		free_slots_.push_back(n_slots - 1 - i);
 	}
+	if (!dry_) {
+		const cudaError_t e = warm_up();
+		if (e != cudaSuccess) { *why = cudaGetErrorString(e); return false; }
+	}
 	launches0_ = launch_count();
 	thread_ = std::thread([this] { loop(); });
 	return true;
+}
+
+// Every kernel a served request can launch, launched once on zeroed scratch
+// records through the same dispatch and launch environment as served
+// requests, with sizes that reach every branch of the launch choice (the
+// few-target form, configuration 0, mid-size and large packed forms) and
+// every regularisation. CUDA loads a kernel's code at its first launch by
+// default (lazy loading), and that load stalls other work on the device:
+// without this the first requests to need a new kernel wait for everything
+// in flight, about a second in a busy stream.
+cudaError_t Server::warm_up() {
+	const int p3d_n[] = {1, 8, 300, 9000, 40000};
+	const int p2d_n[] = {1, 8, 3000, 9000, 70000};
+	const int f3d_n[] = {1, 8, 3000, 9000};
+	const size_t max_n = 70000;
+	void* scratch = nullptr;
+	cudaError_t e = cudaMalloc(&scratch, max_n * (32 + 16 + 12 + 12));
+	if (e != cudaSuccess) return e;
+	float4* rec = static_cast<float4*>(scratch);                  // 2 float4 per record
+	float4* pts = rec + 2 * max_n;                                // 1 float4 per point
+	float* out1 = reinterpret_cast<float*>(pts + max_n);          // 3 floats per target
+	float* out2 = out1 + 3 * max_n;
+	Slot& sl = slots_[0];
+	cudaStream_t st = sl.st[0];
+	e = cudaMemsetAsync(scratch, 0, max_n * (32 + 16 + 12 + 12), st);
+	LaunchEnv env{sl.ws, kSlotWsBytes, sl.d_err, st, num_sms_, true, kCtaSrcCap};
+	for (int reg = 0; e == cudaSuccess && reg < 4; ++reg) {
+		for (int n : p3d_n) {
+			if (e != cudaSuccess) break;
+			P3DInduceProblem p;
+			p.src = rec; p.n_src = n; p.tgt = rec; p.tstride = 2; p.n_tgt = n;
+			p.out_vel = out1; p.out_dvort = out2; p.sigma = 0.05f;
+			e = p3d_induce(reg, kOpVel | kOpDvort, p, env);
+		}
+		for (int n : p2d_n) {
+			if (e != cudaSuccess) break;
+			P2DVelProblem p;
+			p.src = pts; p.n_src = n; p.tgt = pts; p.n_tgt = n; p.out = out1; p.sigma = 0.05f;
+			e = p2d_vel(reg, p, env);
+		}
+	}
+	for (int n : f3d_n) {
+		if (e != cudaSuccess) break;
+		F3DVelProblem p;
+		p.fil = rec; p.n_fil = n; p.tgt = pts; p.tstride = 1; p.n_tgt = n; p.out = out1;
+		e = f3d_vel(p, env);
+	}
+	if (e == cudaSuccess) e = advance_p3d(rec, 8, out1, out2, 0.f, st);
+	if (e == cudaSuccess) e = advance_p2d(pts, 8, out1, 0.f, st);
+	if (e == cudaSuccess) e = advance_points(pts, 8, out1, 0.f, st);
+	if (e == cudaSuccess) e = cudaMemsetAsync(sl.d_err, 0, sizeof(unsigned), st);
+	const cudaError_t s = cudaStreamSynchronize(st);
+	if (e == cudaSuccess) e = s;
+	cudaFree(scratch);
+	return e;
 }
 
 void Server::shutdown() {
@@ -516,7 +595,7 @@ cudaError_t Server::launch(Request& q, Slot& sl) {
 	if (e == cudaSuccess && r.kind == CVTX_GB300_REQ_F3D)
 		e = cudaMemcpyAsync(tgt, src_of(r.tgt_in, q.st_tgt, L.tgt_b), L.tgt_b,
 			cudaMemcpyHostToDevice, st);
-	LaunchEnv env{sl.ws, kSlotWsBytes, sl.d_err, st, num_sms_, true};
+	LaunchEnv env{sl.ws, kSlotWsBytes, sl.d_err, st, num_sms_, true, kCtaSrcCap};
 	for (int k = 0; e == cudaSuccess && k < r.n_steps; ++k) {
 		switch (r.kind) {
 		case CVTX_GB300_REQ_P3D: {

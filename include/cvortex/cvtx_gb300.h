@@ -227,8 +227,10 @@ typedef struct {
 	unsigned long long kernel_launches;
 } cvtx_gb300_server_stats;
 typedef struct cvtx_gb300_server cvtx_gb300_server;
-/* n_slots: concurrent requests (0 = 64). hbm_bytes: arena size (0 = half of
- * the free device memory, at most 64 GiB). flags: CVTX_GB300_SERVER_DRY_RUN
+/* n_slots: concurrent requests (0 = 32, one per hardware work queue at
+ * CUDA_DEVICE_MAX_CONNECTIONS=32; each slot holds a 512 MiB split
+ * workspace). hbm_bytes: arena size (0 = half of the free device memory, at
+ * most 64 GiB). flags: CVTX_GB300_SERVER_DRY_RUN
  * runs the scheduler without a GPU (requests complete at admission without
  * computing; for testing admission logic). */
 enum { CVTX_GB300_SERVER_DRY_RUN = 1 };
