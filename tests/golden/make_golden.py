@@ -16,6 +16,8 @@ reference's OpenMP path) and stores inputs and outputs as compressed .npz:
                      LCG of test/testmain.c:87-92) with its outputs
 * kat.npz          -- g, zeta, eta (3D and 2D) of every regularisation on a
                      grid of rho, from the reference's function pointers
+* relax.npz        -- cvtx_P3D_pedrizzetti_relaxation of a vortex ring for
+                     the four regularisations
 * redist.npz       -- cvtx_P3D_redistribute_on_grid / cvtx_P2D_redistribute_on_grid
                      for the five redistribution functions with and without
                      removal of weak particles and with an output limit
@@ -166,6 +168,16 @@ def redist_case(ref):
     np.savez_compressed(OUT / "redist.npz", **d)
 
 
+def relax_case(ref):
+    ring = workloads.vortex_ring(800, seed=31)
+    d = {"particles": ring, "fdt": np.float32(0.3), "sigma": np.float32(0.05)}
+    for reg in REGS:
+        q = ring.copy()
+        ref.relax(q, 0.3, reg, 0.05)
+        d[f"vort_{reg}"] = q["vorticity"]
+    np.savez_compressed(OUT / "relax.npz", **d)
+
+
 def main():
     ref = reference()
     cube = workloads.uniform_cube(700, seed=11)
@@ -178,6 +190,7 @@ def main():
     reftest_case(ref)
     kat_case(ref)
     redist_case(ref)
+    relax_case(ref)
     for f in sorted(OUT.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

@@ -135,6 +135,10 @@ def test_host_path_matches_reference(host, reg):
     _close(host.p3d_vort(p, mes, reg, s), g[f"vort_{reg}"])
     q = golden("p2d_patch")
     _close(host.p2d_vel(q["particles"], q["particles"]["coord"], reg, 0.05), q[f"vel_{reg}"])
+    r = golden("relax")
+    ring = r["particles"].copy()
+    host.relax(ring, float(r["fdt"]), reg, float(r["sigma"]))
+    _close(ring["vorticity"], r[f"vort_{reg}"])
     assert host.launches() == launches     # the host path launched nothing
 
 

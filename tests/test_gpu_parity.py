@@ -52,6 +52,19 @@ def test_p3d_golden(gpu, case, reg):
 
 
 @pytest.mark.parametrize("reg", REGS)
+def test_relaxation_golden(gpu, reg):
+    """cvtx_P3D_pedrizzetti_relaxation (its vorticity field on the GPU)
+    against the reference library's output."""
+    g = golden("relax")
+    ring = g["particles"].copy()
+    launches = gpu.launches()
+    gpu.relax(ring, float(g["fdt"]), reg, float(g["sigma"]))
+    if reg != "singular":                  # singular: zeta = 0, a memset
+        assert gpu.launches() > launches
+    check(ring["vorticity"], g[f"vort_{reg}"], "relax")
+
+
+@pytest.mark.parametrize("reg", REGS)
 def test_p3d_fused_equals_separate(gpu, reg):
     g = golden("p3d_ring")
     p, s = g["particles"], float(g["sigma"])
