@@ -40,6 +40,32 @@ def test_library_exports_every_declared_symbol(built):
     assert exported == set(_declared_symbols()), exported ^ set(_declared_symbols())
 
 
+def test_reference_test_program_passes_against_this_library(built):
+    """The reference's own test program (test/testmain.c with its headers:
+    regularisation KATs, particle directions and zeros, the accelerator
+    API), compiled unchanged and linked against this libcvortex.so instead
+    of the reference library, passes every test. Only where the reference
+    sources are present; the binary goes to oracle/_ref/."""
+    import oracle
+    src = oracle.REFERENCE_ROOT / "test" / "testmain.c"
+    if not src.is_file():
+        pytest.skip("reference sources not present")
+    out_dir = ROOT / "oracle" / "_ref"
+    out_dir.mkdir(parents=True, exist_ok=True)
+    exe = out_dir / "reference_testmain_gb300"
+    lib_dir = abi.LIB_PATH.parent
+    cmd = ["gcc", "-O2", "-fopenmp", "-w", "-I", str(ROOT / "include"),
+           "-I", str(oracle.REFERENCE_ROOT / "include" / "cvortex"),
+           "-I", str(oracle.REFERENCE_ROOT / "test"), "-DCVTX_EXPORT=", str(src), "-o", str(exe),
+           "-L", str(lib_dir), "-lcvortex", "-lm", f"-Wl,-rpath,{lib_dir}"]
+    subprocess.run(cmd, check=True, capture_output=True)
+    res = subprocess.run([str(exe)], capture_output=True, text=True, timeout=600)
+    assert res.returncode == 0, res.stdout[-2000:] + res.stderr[-2000:]
+    m = re.search(r"Passed (\d+) of (\d+) tests \((\d+) failed\)", res.stdout)
+    assert m and m.group(1) == m.group(2) and m.group(3) == "0", res.stdout[-2000:]
+    assert int(m.group(2)) >= 57
+
+
 def test_struct_layouts():
     assert C.sizeof(abi.cvtx_P3D) == 28
     assert C.sizeof(abi.cvtx_F3D) == 28
