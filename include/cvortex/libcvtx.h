@@ -137,29 +137,37 @@ CVTX_EXPORT bsv_V3f cvtx_P3D_M2S_vort(const cvtx_P3D** array_start,
 	const int num_particles, const bsv_V3f mes_point,
 	const cvtx_VortFunc* kernel, float regularisation_radius);
 
+/* M2M: every source against every target. GPU-backed here (the hot path);
+ * each replaces the reference declaration and implementation cited. */
+/* reference libcvtx.h:213-220; src/P3D.cpp:343-366 (GPU: src/ocl_P3D.cpp:150-321) */
 CVTX_EXPORT void cvtx_P3D_M2M_vel(const cvtx_P3D** array_start,
 	const int num_particles, const bsv_V3f* mes_start, const int num_mes,
 	bsv_V3f* result_array, const cvtx_VortFunc* kernel,
 	float regularisation_radius);
+/* reference libcvtx.h:222-229; src/P3D.cpp:387-410 (GPU: src/ocl_P3D.cpp:323-506) */
 CVTX_EXPORT void cvtx_P3D_M2M_dvort(const cvtx_P3D** array_start,
 	const int num_particles, const cvtx_P3D** induced_start,
 	const int num_induced, bsv_V3f* result_array,
 	const cvtx_VortFunc* kernel, float regularisation_radius);
+/* reference libcvtx.h:231-239; src/P3D.cpp:432-456 (GPU: src/ocl_P3D.cpp:508-725) */
 CVTX_EXPORT void cvtx_P3D_M2M_visc_dvort(const cvtx_P3D** array_start,
 	const int num_particles, const cvtx_P3D** induced_start,
 	const int num_induced, bsv_V3f* result_array,
 	const cvtx_VortFunc* kernel, float regularisation_radius,
 	float kinematic_visc);
+/* reference libcvtx.h:241-248; src/P3D.cpp:476-498 (GPU: src/ocl_P3D.cpp:728-899) */
 CVTX_EXPORT void cvtx_P3D_M2M_vort(const cvtx_P3D** array_start,
 	const int num_particles, const bsv_V3f* mes_start, const int num_mes,
 	bsv_V3f* result_array, const cvtx_VortFunc* kernel,
 	float regularisation_radius);
 
+/* reference libcvtx.h:250-257; src/P3D.cpp:508-634 */
 CVTX_EXPORT int cvtx_P3D_redistribute_on_grid(
 	const cvtx_P3D** input_array_start, const int n_input_particles,
 	cvtx_P3D* output_particles, int max_output_particles,
 	const cvtx_RedistFunc* redistributor, float grid_density,
 	float negligible_vort);
+/* reference libcvtx.h:259-264; src/P3D.cpp:669-707 */
 CVTX_EXPORT void cvtx_P3D_pedrizzetti_relaxation(
 	cvtx_P3D** input_array_start, const int n_input_particles, float fdt,
 	const cvtx_VortFunc* kernel, float regularisation_radius);
@@ -173,12 +181,15 @@ CVTX_EXPORT bsv_V3f cvtx_F3D_M2S_vel(const cvtx_F3D** array_start,
 	const int num_filaments, const bsv_V3f mes_point);
 CVTX_EXPORT bsv_V3f cvtx_F3D_M2S_dvort(const cvtx_F3D** array_start,
 	const int num_filaments, const cvtx_P3D* induced_particle);
+/* reference libcvtx.h:285-290; src/F3D.cpp:162-180 (GPU: src/ocl_F3D.cpp:36-420) */
 CVTX_EXPORT void cvtx_F3D_M2M_vel(const cvtx_F3D** array_start,
 	const int num_filaments, const bsv_V3f* mes_start, const int num_mes,
 	bsv_V3f* result_array);
+/* reference libcvtx.h:292-297; src/F3D.cpp:182-202 (GPU: src/ocl_F3D.cpp:422-646) */
 CVTX_EXPORT void cvtx_F3D_M2M_dvort(const cvtx_F3D** array_start,
 	const int num_filaments, const cvtx_P3D** induced_start,
 	const int num_induced, bsv_V3f* result_array);
+/* reference libcvtx.h:299-305; src/F3D.cpp:204-227 (CPU only there) */
 CVTX_EXPORT void cvtx_F3D_inf_mtrx(const cvtx_F3D** array_start,
 	const int num_filaments, const bsv_V3f* mes_start,
 	const bsv_V3f* dir_start, const int num_mes, float* result_matrix);
@@ -193,6 +204,7 @@ CVTX_EXPORT void cvtx_P2D_S2M_vel(const cvtx_P2D* self,
 CVTX_EXPORT bsv_V2f cvtx_P2D_M2S_vel(const cvtx_P2D** array_start,
 	const int num_particles, const bsv_V2f mes_point,
 	const cvtx_VortFunc* kernel, float regularisation_radius);
+/* reference libcvtx.h:329-336; src/P2D.cpp:141-162 (GPU: src/ocl_P2D.cpp:37-424) */
 CVTX_EXPORT void cvtx_P2D_M2M_vel(const cvtx_P2D** array_start,
 	const int num_particles, const bsv_V2f* mes_start, const int num_mes,
 	bsv_V2f* result_array, const cvtx_VortFunc* kernel,
@@ -208,11 +220,13 @@ CVTX_EXPORT float cvtx_P2D_M2S_visc_dvort(const cvtx_P2D** array_start,
 	const int num_particles, const cvtx_P2D* induced_particle,
 	const cvtx_VortFunc* kernel, float regularisation_radius,
 	float kinematic_visc);
+/* reference libcvtx.h:362-370; src/P2D.cpp:252-276 (GPU: src/ocl_P2D.cpp:426-631) */
 CVTX_EXPORT void cvtx_P2D_M2M_visc_dvort(const cvtx_P2D** array_start,
 	const int num_particles, const cvtx_P2D** induced_start,
 	const int num_induced, float* result_array,
 	const cvtx_VortFunc* kernel, float regularisation_radius,
 	float kinematic_visc);
+/* reference libcvtx.h:372-379; src/P2D.cpp:283-404 */
 CVTX_EXPORT int cvtx_P2D_redistribute_on_grid(
 	const cvtx_P2D** input_array_start, const int num_particles,
 	cvtx_P2D* output_particles, int num_output_particles,
