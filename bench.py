@@ -58,7 +58,9 @@ VORT_FLOPS = {1: 22, 2: 15, 3: 17}
 REG = {"singular": 0, "winckelmans": 1, "planetary": 2, "gaussian": 3}
 OPS = {"veldvort": "fused vel+dvort", "vel": "vel", "dvort": "dvort",
        "vort": "vorticity field (5 sigma box cut-off)",
-       "inf": "F3D influence matrix, 25,000 points x 20,000 filaments (2 GB)"}
+       "inf": "F3D influence matrix, 25,000 points x 20,000 filaments (2 GB)",
+       "m2s": "few targets: fused vel+dvort of the first 64 particles from all sources"}
+M2S_TARGETS = 64
 # influence matrix: F3D vel (51) + the dot with the direction (5) per entry
 INF_FLOPS = 56
 INF_SHAPE = (25_000, 20_000)
@@ -267,10 +269,12 @@ def run_ours(args):
     if op == "vort" and reg not in VORT_FLOPS:
         raise SystemExit("--op vort: the singular vorticity field is zero (no kernel)")
     flops_per = (VORT_FLOPS[reg] if op == "vort" else INF_FLOPS if op == "inf"
-                 else FLOPS[(op, reg)])
+                 else FLOPS[("veldvort", reg)] if op == "m2s" else FLOPS[(op, reg)])
     v_out = vel.data_ptr() if op in ("veldvort", "vel") else None
     d_out = dv.data_ptr() if op in ("veldvort", "dvort") else None
     pairs = float(n) * n
+    if op == "m2s":
+        pairs = float(n) * M2S_TARGETS
     if op == "inf":
         nm, ni = INF_SHAPE
         pairs = float(nm) * ni
@@ -288,6 +292,9 @@ def run_ours(args):
         if op == "inf":
             rc = lib.cvtx_gb300_dev_F3D_inf_mtrx(rfd.data_ptr(), ni, tfd.data_ptr(), dd.data_ptr(),
                                                  nm, om.data_ptr(), sh)
+        elif op == "m2s":
+            rc = lib.cvtx_gb300_dev_P3D_M2M(rec.data_ptr(), n, rec.data_ptr(), 2, M2S_TARGETS,
+                                            vel.data_ptr(), dv.data_ptr(), reg, SIGMA, sh)
         elif op == "vort":
             rc = lib.cvtx_gb300_dev_P3D_M2M_vort(rec.data_ptr(), n, rec.data_ptr(), 2, n,
                                                  vel.data_ptr(), reg, SIGMA, sh)
@@ -339,7 +346,8 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": OPS[op] if op == "inf" else
-                   f"P3D vortex ring N={n}, {args.reg}, sigma={SIGMA}, {OPS[op]}, targets = sources",
+                   f"P3D vortex ring N={n}, {args.reg}, sigma={SIGMA}, {OPS[op]}"
+                   + ("" if op == "m2s" else ", targets = sources"),
                    "interactions_per_step": pairs, "l2": "flushed between steps (256 MB write)",
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
