@@ -558,9 +558,8 @@ __global__ void p3_finalize_scaled(float* __restrict__ out, int n_tgt,
 // (src/P3D.cpp:298-322): out = sum_{|dx|,|dy|,|dz| < 5 sigma} zeta(rho) alpha_s
 // / (4 pi sigma^3).
 // ---------------------------------------------------------------------------
+// (singular: zeta = 0, so its field is a memset and needs no kernel)
 template <Reg R> struct ZetaP3D;
-template <> struct ZetaP3D<Reg::Singular> {
-	__device__ __forceinline__ static float z(float, const RegConsts&) { return 0.f; } };
 template <> struct ZetaP3D<Reg::Winckelmans> {
 	__device__ __forceinline__ static float z(float r2, const RegConsts& c) {
 		const float q = fmaf(r2, c.inv_s2, 1.f);
