@@ -842,15 +842,27 @@ struct InduceVariant {
 
 // The few-target form (few.cuh) as configuration 10: Plan.n_tblocks =
 // target groups, n_split = source chunks, src_per_split = chunk length.
+// Targets per CTA: 8 for vel; for stretching 2 below 262,144 sources or up
+// to 64 targets, else 4 (GB300 timings: two resident CTAs per SM at four
+// targets, more at two, which hides the source loads better unless the
+// target groups multiply the source reads).
 template <Reg R, bool VEL, bool DV>
 struct FewVariant {
 	static constexpr int NC = InduceNC<VEL, DV>::value;
-	using Form = FewForm<P3DInduceOp<R, VEL, DV>, (VEL && !DV) ? 8 : 4>;
+	using Op = P3DInduceOp<R, VEL, DV>;
+	using Wide = FewForm<Op, (VEL && !DV) ? 8 : 4>;
+	using Narrow = FewForm<Op, (VEL && !DV) ? 8 : 2>;
+	static bool narrow(int n_src, int n_tgt) {
+		return !(VEL && !DV) && (n_src < 262144 || n_tgt <= 64);
+	}
 	static Plan plan(int n_src, int n_tgt, int num_sms, int max_split, int = 1) {
-		return Form::plan(n_src, n_tgt, num_sms, max_split);
+		return narrow(n_src, n_tgt) ? Narrow::plan(n_src, n_tgt, num_sms, max_split)
+		                            : Wide::plan(n_src, n_tgt, num_sms, max_split);
 	}
 	static cudaError_t launch(const Plan& pl, const P3DInduceProblem& p, const LaunchEnv& env) {
-		return Form::launch(pl, p, make_induce_consts(int(R), p.sigma), p.n_tgt, env);
+		const InduceConsts k = make_induce_consts(int(R), p.sigma);
+		return narrow(p.n_src, p.n_tgt) ? Narrow::launch(pl, p, k, p.n_tgt, env)
+		                                : Wide::launch(pl, p, k, p.n_tgt, env);
 	}
 };
 
