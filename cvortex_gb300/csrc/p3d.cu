@@ -842,18 +842,18 @@ struct InduceVariant {
 
 // The few-target form (few.cuh) as configuration 10: Plan.n_tblocks =
 // target groups, n_split = source chunks, src_per_split = chunk length.
-// Targets per CTA: 8 for vel; for stretching 2 below 262,144 sources or up
-// to 64 targets, else 4 (GB300 timings: two resident CTAs per SM at four
-// targets, more at two, which hides the source loads better unless the
-// target groups multiply the source reads).
+// Targets per CTA: below 262,144 sources or up to 64 targets 4 for vel and
+// 2 for stretching, else 8 and 4 (GB300 timings: fewer targets per CTA
+// means fewer registers and more resident CTAs, which hide the source loads
+// better, until the extra target groups multiply the source reads).
 template <Reg R, bool VEL, bool DV>
 struct FewVariant {
 	static constexpr int NC = InduceNC<VEL, DV>::value;
 	using Op = P3DInduceOp<R, VEL, DV>;
 	using Wide = FewForm<Op, (VEL && !DV) ? 8 : 4>;
-	using Narrow = FewForm<Op, (VEL && !DV) ? 8 : 2>;
+	using Narrow = FewForm<Op, (VEL && !DV) ? 4 : 2>;
 	static bool narrow(int n_src, int n_tgt) {
-		return !(VEL && !DV) && (n_src < 262144 || n_tgt <= 64);
+		return n_src < 262144 || n_tgt <= 64;
 	}
 	static Plan plan(int n_src, int n_tgt, int num_sms, int max_split, int = 1) {
 		return narrow(n_src, n_tgt) ? Narrow::plan(n_src, n_tgt, num_sms, max_split)
