@@ -759,7 +759,7 @@ struct F3DVelOp {
 		p.out[3 * size_t(t) + 2] = float(s[2]);
 	}
 };
-using F3DFew = FewForm<F3DVelOp, 4>;
+using F3DFew = FewForm2<F3DVelOp, 2, 4>;
 constexpr int kF3DFewCfg = 5;   // the few-target form
 
 // Velocity launch configurations: 0 scalar (1 target/thread, 128 threads),
@@ -803,7 +803,7 @@ cudaError_t f3d_vel(const F3DVelProblem& p, const LaunchEnv& env) {
 	if (f3d_vel_cfg(p.n_tgt, p.n_fil) == kF3DFewCfg) {
 		const Plan pl = F3DFew::plan(p.n_fil, p.n_tgt, env.num_sms,
 			env.cap_to_ws ? split_cap_for(env.ws_bytes, 3, p.n_tgt) : -1);
-		return F3DFew::launch(pl, p, F3DVelOp::Consts{0}, p.n_tgt, env);
+		return F3DFew::launch(pl, p, F3DVelOp::Consts{0}, p.n_fil, p.n_tgt, env);
 	}
 	return with_vel_cfg(f3d_vel_cfg(p.n_tgt, p.n_fil), [&](auto t, auto n, auto pk) {
 		return launch_vel<decltype(t)::value, decltype(n)::value, decltype(pk)::value>(p, env);

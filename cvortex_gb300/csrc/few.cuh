@@ -185,4 +185,25 @@ struct FewForm {
 	}
 };
 
+// Two group widths of one operation's few-target form: the narrow one (TTN
+// targets per CTA) below 262,144 sources or up to 64 targets, else the wide
+// one (TTW). Fewer targets per CTA means fewer registers and more resident
+// CTAs, which hide the source loads better, until the extra target groups
+// multiply the source reads (GB300 timings).
+template <class Op, int TTN, int TTW>
+struct FewForm2 {
+	using Narrow = FewForm<Op, TTN>;
+	using Wide = FewForm<Op, TTW>;
+	static bool narrow(int n_src, int n_tgt) { return n_src < 262144 || n_tgt <= 64; }
+	static Plan plan(int n_src, int n_tgt, int num_sms, int max_chunks) {
+		return narrow(n_src, n_tgt) ? Narrow::plan(n_src, n_tgt, num_sms, max_chunks)
+		                            : Wide::plan(n_src, n_tgt, num_sms, max_chunks);
+	}
+	static cudaError_t launch(const Plan& pl, const typename Op::Problem& p,
+		const typename Op::Consts& k, int n_src, int n_tgt, const LaunchEnv& env) {
+		return narrow(n_src, n_tgt) ? Narrow::launch(pl, p, k, n_tgt, env)
+		                            : Wide::launch(pl, p, k, n_tgt, env);
+	}
+};
+
 }  // namespace cvtx

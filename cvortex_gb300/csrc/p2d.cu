@@ -488,7 +488,7 @@ struct P2DVelOp {
 		p.out[2 * size_t(t) + 1] = float(k.scale * s[1]);
 	}
 };
-template <Reg R> using P2DFew = FewForm<P2DVelOp<R>, 8>;
+template <Reg R> using P2DFew = FewForm2<P2DVelOp<R>, 4, 8>;
 
 int vel_cfg(int n_tgt, int n_src) {
 	const int f = p2d_env_cfg();
@@ -522,7 +522,7 @@ cudaError_t vel_r(const P2DVelProblem& p, const LaunchEnv& env) {
 		const Plan pl = P2DFew<R>::plan(p.n_src, p.n_tgt, env.num_sms,
 			env.cap_to_ws ? split_cap_for(env.ws_bytes, 2, p.n_tgt) : -1);
 		typename P2DVelOp<R>::Consts k{make_reg_consts_host(p.sigma), vel_scale(int(R), p.sigma)};
-		return P2DFew<R>::launch(pl, p, k, p.n_tgt, env);
+		return P2DFew<R>::launch(pl, p, k, p.n_src, p.n_tgt, env);
 	}
 	return with_vel_cfg<R>(vel_cfg(p.n_tgt, p.n_src), [&](auto t, auto n, auto pk) {
 		return launch_vel<R, decltype(t)::value, decltype(n)::value, decltype(pk)::value>(p, env);

@@ -842,27 +842,16 @@ struct InduceVariant {
 
 // The few-target form (few.cuh) as configuration 10: Plan.n_tblocks =
 // target groups, n_split = source chunks, src_per_split = chunk length.
-// Targets per CTA: below 262,144 sources or up to 64 targets 4 for vel and
-// 2 for stretching, else 8 and 4 (GB300 timings: fewer targets per CTA
-// means fewer registers and more resident CTAs, which hide the source loads
-// better, until the extra target groups multiply the source reads).
+// Targets per CTA (few.cuh, FewForm2): 4 / 8 for vel, 2 / 4 for stretching.
 template <Reg R, bool VEL, bool DV>
 struct FewVariant {
 	static constexpr int NC = InduceNC<VEL, DV>::value;
-	using Op = P3DInduceOp<R, VEL, DV>;
-	using Wide = FewForm<Op, (VEL && !DV) ? 8 : 4>;
-	using Narrow = FewForm<Op, (VEL && !DV) ? 4 : 2>;
-	static bool narrow(int n_src, int n_tgt) {
-		return n_src < 262144 || n_tgt <= 64;
-	}
+	using Form = FewForm2<P3DInduceOp<R, VEL, DV>, (VEL && !DV) ? 4 : 2, (VEL && !DV) ? 8 : 4>;
 	static Plan plan(int n_src, int n_tgt, int num_sms, int max_split, int = 1) {
-		return narrow(n_src, n_tgt) ? Narrow::plan(n_src, n_tgt, num_sms, max_split)
-		                            : Wide::plan(n_src, n_tgt, num_sms, max_split);
+		return Form::plan(n_src, n_tgt, num_sms, max_split);
 	}
 	static cudaError_t launch(const Plan& pl, const P3DInduceProblem& p, const LaunchEnv& env) {
-		const InduceConsts k = make_induce_consts(int(R), p.sigma);
-		return narrow(p.n_src, p.n_tgt) ? Narrow::launch(pl, p, k, p.n_tgt, env)
-		                                : Wide::launch(pl, p, k, p.n_tgt, env);
+		return Form::launch(pl, p, make_induce_consts(int(R), p.sigma), p.n_src, p.n_tgt, env);
 	}
 };
 
