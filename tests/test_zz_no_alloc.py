@@ -40,6 +40,7 @@ def _records(p):
     ("gaussian", "dvort", 20_000, 9_000),
     ("singular", "vel", 5_000, 20_000),
     ("winckelmans", "fused", 60_000, 200_000),   # scratch caps the split count
+    ("gaussian", "fused", 300_000, 40),           # the few-target form
 ])
 def test_noalloc_matches_existing_entry_point(gpu, reg, ops, n_src, n_tgt):
     import torch
