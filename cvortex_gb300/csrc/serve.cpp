@@ -69,7 +69,7 @@ constexpr size_t kSlotWsBytes = size_t(512) << 20;
 // Sources per CTA in served launches: about 2 ms of FMA work per CTA for
 // the fused P3D kernel, so a newly launched high-priority kernel waits at
 // most that long for SMs held by the CTAs of large requests.
-constexpr int kCtaSrcCap = 8192;
+constexpr int kCtaSrcCap = 4096;
 constexpr size_t kStagingBytes = size_t(1) << 30;        // pinned staging arena
 constexpr size_t kDefaultMaxHbm = size_t(64) << 30;
 // One slot per hardware work queue at CUDA_DEVICE_MAX_CONNECTIONS=32.
