@@ -20,7 +20,7 @@
 //    work per step (smaller = higher), so the block scheduler serves the CTAs
 //    of small requests ahead of the waves of large ones. Running CTAs are
 //    not preempted, so served launches bound the sources per CTA
-//    (kCtaSrcCap) and a small request's kernel waits at most ~2 ms for SMs.
+//    (kCtaSrcCap) and a small request's kernel waits about 1 ms for SMs.
 //    The default 32 slots match the hardware work queues at
 //    CUDA_DEVICE_MAX_CONNECTIONS=32, which serving processes should set
 //    before CUDA starts; the streams are created so that slots do not share
@@ -63,12 +63,14 @@ double now_s() {
 }
 
 constexpr size_t kAlign = 256;
-// Split partials per slot: enough for the splits that kCtaSrcCap asks of a
-// 200,000-particle step (25 splits x 9 FP64 sums x 200,000 targets = 360 MB).
+// Split partials per slot. A 200,000-particle P3D step fits 37 splits
+// (9 FP64 sums per target), about 5,400 sources per CTA.
 constexpr size_t kSlotWsBytes = size_t(512) << 20;
-// Sources per CTA in served launches: about 2 ms of FMA work per CTA for
-// the fused P3D kernel, so a newly launched high-priority kernel waits at
-// most that long for SMs held by the CTAs of large requests.
+// Sources per CTA in served launches (within the workspace): about 1 ms of
+// FMA work per CTA for the fused P3D kernel, so a newly launched
+// high-priority kernel waits about that long for SMs held by the CTAs of
+// large requests. (8,192 gave p50 29-31 ms at 100 req/s and 68-81 ms at
+// 300 req/s; 4,096 gives 24-25 and 55 ms, for 0.2 % of the throughput.)
 constexpr int kCtaSrcCap = 4096;
 constexpr size_t kStagingBytes = size_t(1) << 30;        // pinned staging arena
 constexpr size_t kDefaultMaxHbm = size_t(64) << 30;
