@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <parallel/algorithm>
 #include <string>
 #include <vector>
@@ -182,7 +183,7 @@ float strength_threshold(const float* strs, int n, int n_desired) {
 	return guess[k];
 }
 
-float mean_of(const std::vector<float>& s, size_t n) {
+float mean_of(const float* s, size_t n) {
 	double a = 0.0;
 	for (size_t i = 0; i < n; ++i) a += double(s[i]);
 	return float(a) / float(n);
@@ -192,7 +193,7 @@ float mean_of(const std::vector<float>& s, size_t n) {
 // strength above `thr` among the first `max_keep`, spread the removed
 // vorticity evenly over the kept ones.
 template <class P, class AddDeficit>
-int remove_weak(P* arr, const std::vector<float>& strs, int n, float thr, int max_keep,
+int remove_weak(P* arr, const float* strs, int n, float thr, int max_keep,
 	AddDeficit&& spread)
 {
 	int j = 0;
@@ -233,7 +234,8 @@ bool cells_for(int dims, const float* pos, const float* str, int n,
 		std::lock_guard<std::recursive_mutex> lk(Runtime::get().lock());
 		DeviceContext* ctx = Runtime::get().active_context();
 		if (ctx) {
-			const cudaError_t e = redist_cells_gpu(*g, kind, pos, str, n, cells, ctx->stream);
+			const cudaError_t e = redist_cells_gpu(*g, kind, pos, str, n, cells, &ctx->redist,
+				ctx->stream);
 			if (e != cudaSuccess) {
 				cudaGetLastError();
 				set_error(std::string(what) + ": " + cudaGetErrorString(e));
@@ -258,6 +260,7 @@ CVTX_EXPORT int cvtx_P3D_redistribute_on_grid(const cvtx_P3D** in, const int n,
 {
 	if (n <= 0 || !in || !f || !(gd > 0.f)) return 0;
 	std::vector<float> pos(size_t(n) * 3), str(size_t(n) * 3);
+#pragma omp parallel for schedule(static)
 	for (int i = 0; i < n; ++i)
 		for (int c = 0; c < 3; ++c) {
 			pos[size_t(i) * 3 + c] = in[i]->coord.x[c];
@@ -269,8 +272,11 @@ CVTX_EXPORT int cvtx_P3D_redistribute_on_grid(const cvtx_P3D** in, const int n,
 			"cvtx_P3D_redistribute_on_grid"))
 		return 0;
 	int m = int(cells.code.size());
-	std::vector<cvtx_P3D> np(static_cast<size_t>(m));
+	// default-initialised storage, first touched by the parallel decode
+	std::unique_ptr<cvtx_P3D[]> np(new cvtx_P3D[size_t(m > 0 ? m : 1)]);
+	std::unique_ptr<float[]> strs(new float[size_t(m > 0 ? m : 1)]);
 	const float vol = gd * gd * gd;
+#pragma omp parallel for schedule(static)
 	for (int i = 0; i < m; ++i) {
 		const uint64_t c = cells.code[size_t(i)];
 		const uint32_t k[3] = {gather3(c), gather3(c >> 1), gather3(c >> 2)};
@@ -279,18 +285,20 @@ CVTX_EXPORT int cvtx_P3D_redistribute_on_grid(const cvtx_P3D** in, const int n,
 			np[size_t(i)].vorticity.x[d] = cells.vort[size_t(i) * 3 + d];
 		}
 		np[size_t(i)].volume = vol;
+		strs[size_t(i)] = norm3(np[size_t(i)].vorticity);
 	}
-	std::vector<float> strs(static_cast<size_t>(m));
-	for (int i = 0; i < m; ++i) strs[size_t(i)] = norm3(np[size_t(i)].vorticity);
-	const float thr = (m > 0 ? mean_of(strs, size_t(m)) : 0.f) * negligible;
-	m = remove_weak(np.data(), strs, m, thr, m, add3);
+	// the mean (FP64, in cell order) and the deficit sums of remove_weak
+	// (FP32, in cell order) stay serial: their rounding is part of the result
+	const float thr = (m > 0 ? mean_of(strs.get(), size_t(m)) : 0.f) * negligible;
+	m = remove_weak(np.get(), strs.get(), m, thr, m, add3);
+#pragma omp parallel for schedule(static)
 	for (int i = 0; i < m; ++i) strs[size_t(i)] = norm3(np[size_t(i)].vorticity);
 	if (out) {
 		if (m > max_out) {
-			const float t2 = strength_threshold(strs.data(), m, max_out);
-			m = remove_weak(np.data(), strs, m, t2, max_out, add3);
+			const float t2 = strength_threshold(strs.get(), m, max_out);
+			m = remove_weak(np.get(), strs.get(), m, t2, max_out, add3);
 		}
-		std::memcpy(out, np.data(), sizeof(cvtx_P3D) * size_t(m));
+		std::memcpy(out, np.get(), sizeof(cvtx_P3D) * size_t(m));
 	}
 	return m;
 }
@@ -300,6 +308,7 @@ CVTX_EXPORT int cvtx_P2D_redistribute_on_grid(const cvtx_P2D** in, const int n,
 {
 	if (n <= 0 || !in || !f || !(gd > 0.f)) return 0;
 	std::vector<float> pos(size_t(n) * 2), str(static_cast<size_t>(n));
+#pragma omp parallel for schedule(static)
 	for (int i = 0; i < n; ++i) {
 		pos[size_t(i) * 2] = in[i]->coord.x[0];
 		pos[size_t(i) * 2 + 1] = in[i]->coord.x[1];
@@ -311,26 +320,28 @@ CVTX_EXPORT int cvtx_P2D_redistribute_on_grid(const cvtx_P2D** in, const int n,
 			"cvtx_P2D_redistribute_on_grid"))
 		return 0;
 	int m = int(cells.code.size());
-	std::vector<cvtx_P2D> np(static_cast<size_t>(m));
+	std::unique_ptr<cvtx_P2D[]> np(new cvtx_P2D[size_t(m > 0 ? m : 1)]);
+	std::unique_ptr<float[]> strs(new float[size_t(m > 0 ? m : 1)]);
 	const float area = gd * gd;
+#pragma omp parallel for schedule(static)
 	for (int i = 0; i < m; ++i) {
 		const uint64_t c = cells.code[size_t(i)];
 		np[size_t(i)].coord.x[0] = g.min[0] + gd * float(gather2(c));
 		np[size_t(i)].coord.x[1] = g.min[1] + gd * float(gather2(c >> 1));
 		np[size_t(i)].vorticity = cells.vort[size_t(i)];
 		np[size_t(i)].area = area;
+		strs[size_t(i)] = std::fabs(np[size_t(i)].vorticity);
 	}
-	std::vector<float> strs(static_cast<size_t>(m));
-	for (int i = 0; i < m; ++i) strs[size_t(i)] = std::fabs(np[size_t(i)].vorticity);
-	const float thr = (m > 0 ? mean_of(strs, size_t(m)) : 0.f) * negligible;
-	m = remove_weak(np.data(), strs, m, thr, m, add1);
+	const float thr = (m > 0 ? mean_of(strs.get(), size_t(m)) : 0.f) * negligible;
+	m = remove_weak(np.get(), strs.get(), m, thr, m, add1);
+#pragma omp parallel for schedule(static)
 	for (int i = 0; i < m; ++i) strs[size_t(i)] = std::fabs(np[size_t(i)].vorticity);
 	if (out) {
 		if (m > max_out) {
-			const float t2 = strength_threshold(strs.data(), m, max_out);
-			m = remove_weak(np.data(), strs, m, t2, max_out, add1);
+			const float t2 = strength_threshold(strs.get(), m, max_out);
+			m = remove_weak(np.get(), strs.get(), m, t2, max_out, add1);
 		}
-		std::memcpy(out, np.data(), sizeof(cvtx_P2D) * size_t(m));
+		std::memcpy(out, np.get(), sizeof(cvtx_P2D) * size_t(m));
 	}
 	return m;
 }

@@ -16,6 +16,7 @@
 
 #include "nbody.h"
 #include "redist.h"
+#include "runtime.h"
 
 namespace cvtx {
 namespace {
@@ -137,17 +138,10 @@ __global__ void sum_kernel(const uint64_t* __restrict__ code, const uint32_t* __
 
 inline unsigned blocks_for(size_t m) { return unsigned((m + kThreads - 1) / kThreads); }
 
-// Scratch freed on scope exit (this path allocates per call, like the
-// reference's own vectors).
-struct Scratch {
-	void* p = nullptr;
-	~Scratch() { if (p) cudaFree(p); }
-};
-
 }  // namespace
 
 cudaError_t redist_cells_gpu(const RedistGrid& g, int kind, const float* pos, const float* str,
-	int n, RedistCells* out, cudaStream_t stream)
+	int n, RedistCells* out, DevBuf* scratch, cudaStream_t stream)
 {
 	out->code.clear();
 	out->vort.clear();
@@ -177,11 +171,11 @@ cudaError_t redist_cells_gpu(const RedistGrid& g, int kind, const float* pos, co
 	const size_t b_idx = al(sizeof(uint32_t) * m);
 	const size_t b_val = al(sizeof(float) * m * nc);
 	const size_t total = b_pos + b_str + 2 * b_code + 2 * b_idx + b_val + 2 * b_idx +
-		al(sort_tmp) + al(scan_tmp) + b_code + al(sizeof(float) * m * nc) + 256;
-	Scratch sc;
-	e = cudaMalloc(&sc.p, total);
+		al(sort_tmp) + al(scan_tmp) + al(sizeof(float) * m * nc) + 256;
+	// grow-only: a new allocation only when a call needs more than any before
+	e = scratch->ensure(total);
 	if (e != cudaSuccess) return e;
-	unsigned char* p = static_cast<unsigned char*>(sc.p);
+	unsigned char* p = static_cast<unsigned char*>(scratch->ptr);
 	auto take = [&](size_t b) { unsigned char* r = p; p += b; return r; };
 	float* d_pos = reinterpret_cast<float*>(take(b_pos));
 	float* d_str = reinterpret_cast<float*>(take(b_str));
@@ -194,7 +188,7 @@ cudaError_t redist_cells_gpu(const RedistGrid& g, int kind, const float* pos, co
 	uint32_t* slot = reinterpret_cast<uint32_t*>(take(b_idx));
 	void* sort_buf = take(al(sort_tmp));
 	void* scan_buf = take(al(scan_tmp));
-	uint64_t* ocode = reinterpret_cast<uint64_t*>(take(b_code));
+	uint64_t* ocode = code0;   // the unsorted keys are not read after the sort
 	float* oval = reinterpret_cast<float*>(take(al(sizeof(float) * m * nc)));
 
 	e = cudaMemcpyAsync(d_pos, pos, sizeof(float) * size_t(n) * g.dims, cudaMemcpyHostToDevice,

@@ -54,9 +54,11 @@ bool redist_grid(int dims, const float* pos, int n, const cvtx_RedistFunc* f, fl
 	RedistGrid* g);
 void redist_cells_host(const RedistGrid& g, const cvtx_RedistFunc* f, const float* pos,
 	const float* str, int n, RedistCells* out);
-// GPU path (kind from redist_kind >= 0). Allocates its own device scratch.
+// GPU path (kind from redist_kind >= 0). Device scratch comes from `scratch`
+// (grow-only, kept between calls: a 200,000-particle M4' call needs ~1.5 GB).
+struct DevBuf;
 cudaError_t redist_cells_gpu(const RedistGrid& g, int kind, const float* pos, const float* str,
-	int n, RedistCells* out, cudaStream_t stream);
+	int n, RedistCells* out, DevBuf* scratch, cudaStream_t stream);
 
 // Morton helpers shared by both paths.
 inline uint64_t spread3(uint32_t v) {
