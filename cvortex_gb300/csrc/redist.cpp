@@ -183,6 +183,17 @@ float strength_threshold(const float* strs, int n, int n_desired) {
 	return guess[k];
 }
 
+// dst[0, n) = src[0, n) in parallel chunks (the output can be ~35 MB)
+template <class T>
+void parallel_copy(T* dst, const T* src, size_t n) {
+	const long long chunks = (long long)((n + 65535) / 65536);
+#pragma omp parallel for schedule(static)
+	for (long long c = 0; c < chunks; ++c) {
+		const size_t b = size_t(c) * 65536, e = std::min(n, b + 65536);
+		std::memcpy(dst + b, src + b, sizeof(T) * (e - b));
+	}
+}
+
 float mean_of(const float* s, size_t n) {
 	double a = 0.0;
 	for (size_t i = 0; i < n; ++i) a += double(s[i]);
@@ -298,7 +309,7 @@ CVTX_EXPORT int cvtx_P3D_redistribute_on_grid(const cvtx_P3D** in, const int n,
 			const float t2 = strength_threshold(strs.get(), m, max_out);
 			m = remove_weak(np.get(), strs.get(), m, t2, max_out, add3);
 		}
-		std::memcpy(out, np.get(), sizeof(cvtx_P3D) * size_t(m));
+		parallel_copy(out, np.get(), size_t(m));
 	}
 	return m;
 }
@@ -341,7 +352,7 @@ CVTX_EXPORT int cvtx_P2D_redistribute_on_grid(const cvtx_P2D** in, const int n,
 			const float t2 = strength_threshold(strs.get(), m, max_out);
 			m = remove_weak(np.get(), strs.get(), m, t2, max_out, add1);
 		}
-		std::memcpy(out, np.get(), sizeof(cvtx_P2D) * size_t(m));
+		parallel_copy(out, np.get(), size_t(m));
 	}
 	return m;
 }
