@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <parallel/algorithm>
 #include <string>
 #include <vector>
@@ -124,8 +125,8 @@ void redist_cells_host(const RedistGrid& g, const cvtx_RedistFunc* f, const floa
 	__gnu_parallel::sort(e.begin(), e.end(), [](const Entry& a, const Entry& b) {
 		return a.code != b.code ? a.code < b.code : a.order < b.order;
 	});
-	out->code.clear();
-	out->vort.clear();
+	out->code_v.clear();
+	out->vort_v.clear();
 	for (size_t j = 0; j < e.size();) {
 		size_t q = j;
 		double acc[3] = {0.0, 0.0, 0.0};
@@ -133,10 +134,13 @@ void redist_cells_host(const RedistGrid& g, const cvtx_RedistFunc* f, const floa
 			for (int c = 0; c < nc; ++c) acc[c] += double(v[e[q].order * nc + c]);
 			++q;
 		}
-		out->code.push_back(e[j].code);
-		for (int c = 0; c < nc; ++c) out->vort.push_back(float(acc[c]));
+		out->code_v.push_back(e[j].code);
+		for (int c = 0; c < nc; ++c) out->vort_v.push_back(float(acc[c]));
 		j = q;
 	}
+	out->code = out->code_v.data();
+	out->vort = out->vort_v.data();
+	out->n = out->code_v.size();
 }
 
 namespace {
@@ -246,7 +250,7 @@ bool cells_for(int dims, const float* pos, const float* str, int n,
 		DeviceContext* ctx = Runtime::get().active_context();
 		if (ctx) {
 			const cudaError_t e = redist_cells_gpu(*g, kind, pos, str, n, cells, &ctx->redist,
-				ctx->stream);
+				&ctx->h_redist, ctx->stream);
 			if (e != cudaSuccess) {
 				cudaGetLastError();
 				set_error(std::string(what) + ": " + cudaGetErrorString(e));
@@ -279,10 +283,13 @@ CVTX_EXPORT int cvtx_P3D_redistribute_on_grid(const cvtx_P3D** in, const int n,
 		}
 	RedistGrid g;
 	RedistCells cells;
+	// the GPU path leaves the cells in the device context's pinned buffer:
+	// hold the runtime lock until they are decoded
+	std::unique_lock<std::recursive_mutex> lk(Runtime::get().lock());
 	if (!cells_for(3, pos.data(), str.data(), n, f, gd, &g, &cells,
 			"cvtx_P3D_redistribute_on_grid"))
 		return 0;
-	int m = int(cells.code.size());
+	int m = int(cells.n);
 	// default-initialised storage, first touched by the parallel decode
 	std::unique_ptr<cvtx_P3D[]> np(new cvtx_P3D[size_t(m > 0 ? m : 1)]);
 	std::unique_ptr<float[]> strs(new float[size_t(m > 0 ? m : 1)]);
@@ -298,6 +305,7 @@ CVTX_EXPORT int cvtx_P3D_redistribute_on_grid(const cvtx_P3D** in, const int n,
 		np[size_t(i)].volume = vol;
 		strs[size_t(i)] = norm3(np[size_t(i)].vorticity);
 	}
+	lk.unlock();
 	// the mean (FP64, in cell order) and the deficit sums of remove_weak
 	// (FP32, in cell order) stay serial: their rounding is part of the result
 	const float thr = (m > 0 ? mean_of(strs.get(), size_t(m)) : 0.f) * negligible;
@@ -327,10 +335,11 @@ CVTX_EXPORT int cvtx_P2D_redistribute_on_grid(const cvtx_P2D** in, const int n,
 	}
 	RedistGrid g;
 	RedistCells cells;
+	std::unique_lock<std::recursive_mutex> lk(Runtime::get().lock());   // as for P3D
 	if (!cells_for(2, pos.data(), str.data(), n, f, gd, &g, &cells,
 			"cvtx_P2D_redistribute_on_grid"))
 		return 0;
-	int m = int(cells.code.size());
+	int m = int(cells.n);
 	std::unique_ptr<cvtx_P2D[]> np(new cvtx_P2D[size_t(m > 0 ? m : 1)]);
 	std::unique_ptr<float[]> strs(new float[size_t(m > 0 ? m : 1)]);
 	const float area = gd * gd;
@@ -343,6 +352,7 @@ CVTX_EXPORT int cvtx_P2D_redistribute_on_grid(const cvtx_P2D** in, const int n,
 		np[size_t(i)].area = area;
 		strs[size_t(i)] = std::fabs(np[size_t(i)].vorticity);
 	}
+	lk.unlock();
 	const float thr = (m > 0 ? mean_of(strs.get(), size_t(m)) : 0.f) * negligible;
 	m = remove_weak(np.get(), strs.get(), m, thr, m, add1);
 #pragma omp parallel for schedule(static)

@@ -141,10 +141,11 @@ inline unsigned blocks_for(size_t m) { return unsigned((m + kThreads - 1) / kThr
 }  // namespace
 
 cudaError_t redist_cells_gpu(const RedistGrid& g, int kind, const float* pos, const float* str,
-	int n, RedistCells* out, DevBuf* scratch, cudaStream_t stream)
+	int n, RedistCells* out, DevBuf* scratch, HostBuf* pinned, cudaStream_t stream)
 {
-	out->code.clear();
-	out->vort.clear();
+	out->code = nullptr;
+	out->vort = nullptr;
+	out->n = 0;
 	if (n <= 0) return cudaSuccess;
 	const int w = 2 * g.radius + 1;
 	const int S = g.dims == 3 ? w * w * w : w * w;
@@ -225,15 +226,23 @@ cudaError_t redist_cells_gpu(const RedistGrid& g, int kind, const float* pos, co
 	if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
 	if (e != cudaSuccess) return e;
 	const size_t cells = size_t(last_slot) + size_t(last_head);
-	out->code.resize(cells);
-	out->vort.resize(cells * nc);
 	if (cells) {
-		e = cudaMemcpyAsync(out->code.data(), ocode, sizeof(uint64_t) * cells,
-			cudaMemcpyDeviceToHost, stream);
+		// the cells go to pinned memory (grow-only), read there by the caller
+		const size_t b_c = al(sizeof(uint64_t) * cells);
+		e = pinned->ensure(b_c + sizeof(float) * cells * nc);
+		if (e != cudaSuccess) return e;
+		uint64_t* h_code = static_cast<uint64_t*>(pinned->ptr);
+		float* h_vort = reinterpret_cast<float*>(static_cast<unsigned char*>(pinned->ptr) + b_c);
+		e = cudaMemcpyAsync(h_code, ocode, sizeof(uint64_t) * cells, cudaMemcpyDeviceToHost,
+			stream);
 		if (e == cudaSuccess)
-			e = cudaMemcpyAsync(out->vort.data(), oval, sizeof(float) * cells * nc,
-				cudaMemcpyDeviceToHost, stream);
+			e = cudaMemcpyAsync(h_vort, oval, sizeof(float) * cells * nc, cudaMemcpyDeviceToHost,
+				stream);
 		if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+		if (e != cudaSuccess) return e;
+		out->code = h_code;
+		out->vort = h_vort;
+		out->n = cells;
 	}
 	return e;
 }

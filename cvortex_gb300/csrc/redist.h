@@ -43,10 +43,15 @@ struct RedistGrid {
 };
 
 // Grid cells with their summed vorticity (vort: dims == 3 -> 3 per cell,
-// dims == 2 -> 1 per cell), ascending Morton code.
+// dims == 2 -> 1 per cell), ascending Morton code. `code` and `vort` point
+// into the vectors below (host path) or into pinned memory that the GPU
+// path copied them to.
 struct RedistCells {
-	std::vector<uint64_t> code;
-	std::vector<float> vort;
+	const uint64_t* code = nullptr;
+	const float* vort = nullptr;
+	size_t n = 0;
+	std::vector<uint64_t> code_v;
+	std::vector<float> vort_v;
 };
 
 // Particles as flat arrays: pos (dims per particle), str (3 or 1 per particle).
@@ -55,10 +60,12 @@ bool redist_grid(int dims, const float* pos, int n, const cvtx_RedistFunc* f, fl
 void redist_cells_host(const RedistGrid& g, const cvtx_RedistFunc* f, const float* pos,
 	const float* str, int n, RedistCells* out);
 // GPU path (kind from redist_kind >= 0). Device scratch comes from `scratch`
-// (grow-only, kept between calls: a 200,000-particle M4' call needs ~1.5 GB).
+// and the cells are copied to `pinned` (both grow-only, kept between calls:
+// a 200,000-particle M4' call needs ~1.5 GB and 25 MB).
 struct DevBuf;
+struct HostBuf;
 cudaError_t redist_cells_gpu(const RedistGrid& g, int kind, const float* pos, const float* str,
-	int n, RedistCells* out, DevBuf* scratch, cudaStream_t stream);
+	int n, RedistCells* out, DevBuf* scratch, HostBuf* pinned, cudaStream_t stream);
 
 // Morton helpers shared by both paths.
 inline uint64_t spread3(uint32_t v) {

@@ -79,6 +79,7 @@ void DeviceContext::close() {
 	if (stream) cudaStreamSynchronize(stream);
 	src.release(); tgt.release(); out0.release(); out1.release(); ws.release();
 	redist.release();
+	h_redist.release();
 	h_src.release(); h_tgt.release(); h_out0.release(); h_out1.release();
 	if (d_err) cudaFree(d_err);
 	if (h_err) cudaFreeHost(h_err);

@@ -41,6 +41,7 @@ struct DeviceContext {
 	unsigned* h_err = nullptr;      // pinned copy
 	DevBuf src, tgt, out0, out1, ws;
 	DevBuf redist;                  // particle redistribution scratch (grow-only)
+	HostBuf h_redist;               // its cells, pinned (grow-only)
 	HostBuf h_src, h_tgt, h_out0, h_out1;
 	cudaError_t open(int dev);
 	void close();
