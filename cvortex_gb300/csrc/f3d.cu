@@ -285,21 +285,22 @@ __device__ __forceinline__ void f3d_dvort_pair(float px, float py, float pz,
 	oz = ok ? vz : 0.f;
 }
 
-// f3d_dvort_pair for two particles at once (f32x2). |r1 x r0| comes from
-// X2 * rsqrt(X2) and the division by X2 from rcp refined by one Newton step.
-// The terms the reference keeps are kept with the same value to rounding; a
-// particle exactly on the filament's segment (X2 = 0, where the reference's
-// term is infinite or NaN) has its term dropped.
+// f3d_dvort_pair for two particles at once (f32x2). `c` holds what depends
+// on the filament alone, computed once per staged tile: r0 = e - s (the
+// reference forms r1 - r2 per pair; the two differ by rounding) and
+// 3 g / |r0|. |r1 x r0| comes from X2 * rsqrt(X2) and 1/X2 from the square of
+// that rsqrt. The terms the reference keeps are kept with the same value to
+// rounding; a particle exactly on the filament's line (X2 = 0, where the
+// reference's term is infinite or NaN) has its term dropped.
 __device__ __forceinline__ void f3d_dvort_pair2(float2 px, float2 py, float2 pz,
-	float2 wx, float2 wy, float2 wz, const float4 a, const float4 b,
+	float2 wx, float2 wy, float2 wz, const float4 a, const float4 b, const float4 c,
 	float2& ox, float2& oy, float2& oz)
 {
 	const float2 r1x = __fadd2_rn(px, bc2(-a.x)), r1y = __fadd2_rn(py, bc2(-a.y));
 	const float2 r1z = __fadd2_rn(pz, bc2(-a.z));
 	const float2 r2x = __fadd2_rn(px, bc2(-b.x)), r2y = __fadd2_rn(py, bc2(-b.y));
 	const float2 r2z = __fadd2_rn(pz, bc2(-b.z));
-	const float2 r0x = __fadd2_rn(r1x, neg2f(r2x)), r0y = __fadd2_rn(r1y, neg2f(r2y));
-	const float2 r0z = __fadd2_rn(r1z, neg2f(r2z));
+	const float2 r0x = bc2(c.x), r0y = bc2(c.y), r0z = bc2(c.z);
 	const float2 xx = __ffma2_rn(r1y, r0z, neg2f(__fmul2_rn(r1z, r0y)));
 	const float2 xy = __ffma2_rn(r1z, r0x, neg2f(__fmul2_rn(r1x, r0z)));
 	const float2 xz = __ffma2_rn(r1x, r0y, neg2f(__fmul2_rn(r1y, r0x)));
@@ -308,17 +309,15 @@ __device__ __forceinline__ void f3d_dvort_pair2(float2 px, float2 py, float2 pz,
 	const float2 X = __fmul2_rn(X2, iX);
 	const float2 q1 = __ffma2_rn(r1z, r1z, __ffma2_rn(r1y, r1y, __fmul2_rn(r1x, r1x)));
 	const float2 q2 = __ffma2_rn(r2z, r2z, __ffma2_rn(r2y, r2y, __fmul2_rn(r2x, r2x)));
-	const float2 q0 = __ffma2_rn(r0z, r0z, __ffma2_rn(r0y, r0y, __fmul2_rn(r0x, r0x)));
 	const float2 il1 = make_float2(rsqrt_approx(q1.x), rsqrt_approx(q1.y));
 	const float2 il2 = make_float2(rsqrt_approx(q2.x), rsqrt_approx(q2.y));
-	const float2 il0 = make_float2(rsqrt_approx(q0.x), rsqrt_approx(q0.y));
 	const float2 d1 = __fmul2_rn(__ffma2_rn(r0z, r1z, __ffma2_rn(r0y, r1y, __fmul2_rn(r0x, r1x))), il1);
 	const float2 d2 = __fmul2_rn(__ffma2_rn(r0z, r2z, __ffma2_rn(r0y, r2y, __fmul2_rn(r0x, r2x))), il2);
 	const float2 t212 = __fadd2_rn(d1, neg2f(d2));
-	const float2 t222 = __fadd2_rn(__fmul2_rn(X, il1), neg2f(__fmul2_rn(X, il2)));
-	const float2 kA = __fmul2_rn(__fmul2_rn(bc2(-a.w), t212), rcp2(X2));
+	const float2 t222 = __fmul2_rn(X, __fadd2_rn(il1, neg2f(il2)));
+	const float2 kA = __fmul2_rn(__fmul2_rn(bc2(-a.w), t212), __fmul2_rn(iX, iX));
 	const float2 Ax = __fmul2_rn(r0x, kA), Ay = __fmul2_rn(r0y, kA), Az = __fmul2_rn(r0z, kA);
-	const float2 B = __fmul2_rn(__fmul2_rn(__fmul2_rn(bc2(3.f), il0), bc2(a.w)), t222);
+	const float2 B = __fmul2_rn(bc2(c.w), t222);
 	const float2 vx = __ffma2_rn(wx, B, __ffma2_rn(Ay, wz, neg2f(__fmul2_rn(Az, wy))));
 	const float2 vy = __ffma2_rn(wy, B, __ffma2_rn(Az, wx, neg2f(__fmul2_rn(Ax, wz))));
 	const float2 vz = __ffma2_rn(wz, B, __ffma2_rn(Ax, wy, neg2f(__fmul2_rn(Ay, wx))));
@@ -341,6 +340,7 @@ f3d_dvort2_kernel(const F3DDvortProblem p, double* __restrict__ partial, int src
 	extern __shared__ __align__(16) unsigned char smem[];
 	float* hi = reinterpret_cast<float*>(smem + Stream2::kSmemBytes);
 	float* lo = hi + NC * TPT * NT;
+	float4* fil_c = reinterpret_cast<float4*>(lo + NC * TPT * NT);   // kTile per-filament terms
 	const int tid = threadIdx.x;
 	const int tbase = blockIdx.x * (TPT * NT);
 	const int s_begin = blockIdx.y * src_per_split;
@@ -371,13 +371,23 @@ f3d_dvort2_kernel(const F3DDvortProblem p, double* __restrict__ partial, int src
 		for (int c = 0; c < NC; ++c)
 #pragma unroll
 			for (int h = 0; h < H; ++h) acc[c][h] = make_float2(0.f, 0.f);
+		// the previous tile's readers are done (the stream synchronises the
+		// CTA after every tile), so the table is rewritten here
+		for (int j = tid; j < cnt; j += NT) {
+			const float4 a = st[2 * j], b = st[2 * j + 1];
+			const float r0x = b.x - a.x, r0y = b.y - a.y, r0z = b.z - a.z;
+			const float l0 = sqrtf(fmaf(r0z, r0z, fmaf(r0y, r0y, r0x * r0x)));
+			fil_c[j] = make_float4(r0x, r0y, r0z, (3.f / l0) * a.w);
+		}
+		__syncthreads();
 		auto body = [&](int j) {
 			const float4 a = st[2 * j];
 			const float4 b = st[2 * j + 1];
+			const float4 fc = fil_c[j];
 #pragma unroll
 			for (int h = 0; h < H; ++h) {
 				float2 vx, vy, vz;
-				f3d_dvort_pair2(tx[h], ty[h], tz[h], ax[h], ay[h], az[h], a, b, vx, vy, vz);
+				f3d_dvort_pair2(tx[h], ty[h], tz[h], ax[h], ay[h], az[h], a, b, fc, vx, vy, vz);
 				acc[0][h] = __fadd2_rn(acc[0][h], vx);
 				acc[1][h] = __fadd2_rn(acc[1][h], vy);
 				acc[2][h] = __fadd2_rn(acc[2][h], vz);
@@ -691,7 +701,8 @@ auto dvort_kernel() {
 
 template <int TPT, int NT, bool PK>
 Plan plan_dvort(int n_fil, int n_tgt, int num_sms, int max_split = 64) {
-	constexpr size_t smem = smem_bytes<TPT, NT>();
+	// the packed kernel keeps a table of kTile per-filament terms
+	constexpr size_t smem = smem_bytes<TPT, NT>() + (PK ? size_t(kTile) * sizeof(float4) : 0);
 	static const int occ = resident_ctas(dvort_kernel<TPT, NT, PK>(), NT, smem);
 	return make_plan(n_fil, n_tgt, TPT * NT, kTile, 3, num_sms * occ, smem, max_split);
 }
@@ -809,15 +820,93 @@ cudaError_t f3d_vel(const F3DVelProblem& p, const LaunchEnv& env) {
 		return launch_vel<decltype(t)::value, decltype(n)::value, decltype(pk)::value>(p, env);
 	});
 }
+
+// The F3D stretching pair as an operation of the few-target form: the same
+// per-pair arithmetic as f3d_dvort_kernel (f3d_dvort_pair), 1/(4 pi) applied
+// once per target.
+struct F3DDvortOp {
+	using Problem = F3DDvortProblem;
+	struct Consts { int unused; };
+	static constexpr int NC = 3, NR = 3;
+	struct Tgt { float x, y, z, wx, wy, wz; };
+	struct Src { float4 a, b; };
+	__device__ static int n_src(const Problem& p) { return p.n_fil; }
+	__device__ static int n_tgt(const Problem& p) { return p.n_tgt; }
+	__device__ static Tgt target(const Problem& p, int t) {
+		const float4 q = p.tgt[size_t(t) * p.tstride];
+		const float4 w = p.tgt[size_t(t) * p.tstride + 1];
+		return Tgt{q.x, q.y, q.z, w.x, w.y, w.z};
+	}
+	__device__ static Src source(const Problem& p, long long s) {
+		return Src{p.fil[2 * s], p.fil[2 * s + 1]};
+	}
+	__device__ static void pair(const Consts&, const Tgt& t, const Src& s, float (&acc)[NR]) {
+		float vx, vy, vz;
+		f3d_dvort_pair(t.x, t.y, t.z, t.wx, t.wy, t.wz, s.a, s.b, vx, vy, vz);
+		acc[0] += vx; acc[1] += vy; acc[2] += vz;
+	}
+	__device__ static void combine(const Tgt&, float (&)[NR]) {}
+	__device__ static int slot(int c) { return c; }
+	__device__ static void write(const Problem& p, const Consts&, int t, const double* s) {
+		p.out[3 * size_t(t)] = float(kInv4Pi * s[0]);
+		p.out[3 * size_t(t) + 1] = float(kInv4Pi * s[1]);
+		p.out[3 * size_t(t) + 2] = float(kInv4Pi * s[2]);
+	}
+};
+using F3DDvortFew = FewForm2<F3DDvortOp, 2, 4>;
+constexpr int kF3DDvortFewCfg = 4;   // the few-target form
+
+// Stretching launch configurations: 0 scalar (1 target/thread, 128
+// threads), 1 packed (2, 128), 2 packed (4, 128), 3 packed (2, 256), 4 the
+// few-target form. Default from GB300 timings (wake sheet of 20,000 to
+// 1,000,000 filaments): 4 up to 512 targets (64 x 100,000: 41 us against
+// 248 us for 0 or 1; 1,024 x 100,000: 351 against 304 us for 1), 1 below
+// kSmallTargets (4,096 x 100,000: 787 us, against 1,295 us for 0), else 2
+// (100,000 x 100,000: 16.8 ms, against 17.3 ms for 1 and 17.5 ms for 3).
+// CVTX_GB300_F3D_DVORT_CFG forces one; CVTX_GB300_FEW_MAX moves the first
+// threshold.
+int f3d_dvort_cfg(int n_tgt, int) {
+	static const int forced = [] {
+		const char* e = std::getenv("CVTX_GB300_F3D_DVORT_CFG");
+		if (!e || !*e) return -1;
+		const int c = std::atoi(e);
+		return (c >= 0 && c <= kF3DDvortFewCfg) ? c : -1;
+	}();
+	if (forced >= 0) return forced;
+	const int few_max = few_max_override() >= 0 ? few_max_override() : 512;
+	if (n_tgt <= few_max) return kF3DDvortFewCfg;
+	return n_tgt < kSmallTargets ? 1 : 2;
+}
+template <class F>
+auto with_dvort_cfg(int cfg, F&& f) {
+	switch (cfg) {
+	case 0: return f(std::integral_constant<int, 1>{}, std::integral_constant<int, 128>{}, std::false_type{});
+	case 2: return f(std::integral_constant<int, 4>{}, std::integral_constant<int, 128>{}, std::true_type{});
+	case 3: return f(std::integral_constant<int, 2>{}, std::integral_constant<int, 256>{}, std::true_type{});
+	default: return f(std::integral_constant<int, 2>{}, std::integral_constant<int, 128>{}, std::true_type{});
+	}
+}
+
 size_t f3d_dvort_ws_bytes(int n_fil, int n_tgt, int num_sms) {
 	if (n_tgt <= 0) return 0;
-	return n_tgt < kSmallTargets ? plan_dvort<1, 128, false>(n_fil, n_tgt, num_sms).ws_bytes
-	                             : plan_dvort<2, 128, true>(n_fil, n_tgt, num_sms).ws_bytes;
+	const int cfg = f3d_dvort_cfg(n_tgt, n_fil);
+	if (cfg == kF3DDvortFewCfg) return F3DDvortFew::plan(n_fil, n_tgt, num_sms, -1).ws_bytes;
+	return with_dvort_cfg(cfg, [&](auto t, auto n, auto pk) {
+		return plan_dvort<decltype(t)::value, decltype(n)::value, decltype(pk)::value>(
+			n_fil, n_tgt, num_sms).ws_bytes;
+	});
 }
 cudaError_t f3d_dvort(const F3DDvortProblem& p, const LaunchEnv& env) {
 	if (p.n_tgt <= 0) return cudaSuccess;
-	return p.n_tgt < kSmallTargets ? launch_dvort<1, 128, false>(p, env)
-	                               : launch_dvort<2, 128, true>(p, env);
+	const int cfg = f3d_dvort_cfg(p.n_tgt, p.n_fil);
+	if (cfg == kF3DDvortFewCfg) {
+		const Plan pl = F3DDvortFew::plan(p.n_fil, p.n_tgt, env.num_sms,
+			env.cap_to_ws ? split_cap_for(env.ws_bytes, 3, p.n_tgt) : -1);
+		return F3DDvortFew::launch(pl, p, F3DDvortOp::Consts{0}, p.n_fil, p.n_tgt, env);
+	}
+	return with_dvort_cfg(cfg, [&](auto t, auto n, auto pk) {
+		return launch_dvort<decltype(t)::value, decltype(n)::value, decltype(pk)::value>(p, env);
+	});
 }
 namespace {
 

@@ -59,7 +59,20 @@ def problems(cv, which):
     if which == "f3d":
         f = workloads.wake_sheet(3000, seed=67)
         return {"vel": cv.f3d_vel(f, workloads.sheet_targets(9001, seed=68))}
+    if which == "f3d_dvort":
+        f, pts = f3d_dvort_case()
+        return {"dvort": cv.f3d_dvort(f, pts)}
     raise ValueError(which)
+
+
+def f3d_dvort_case():
+    """A wake sheet and 9,001 particles, some at filament ends."""
+    f = workloads.wake_sheet(3000, seed=67)
+    pts = workloads.uniform_cube(9001, seed=69)
+    pts["coord"] = workloads.sheet_targets(9001, seed=68)
+    pts["coord"][:20] = f["start"][:20]
+    pts["coord"][4000:4020] = f["end"][40:60]
+    return f, pts
 
 
 def run_child(tmp_path, which, var, cfg):
@@ -110,3 +123,10 @@ def test_f3d_vel_configs(tmp_path, cfg):
     f = workloads.wake_sheet(3000, seed=67)
     t = workloads.sheet_targets(9001, seed=68)
     check(got["vel"][SAMPLE], oracle.f3d_vel(f, t[SAMPLE]), tol=1e-5)
+
+
+@pytest.mark.parametrize("cfg", range(5))
+def test_f3d_dvort_configs(tmp_path, cfg):
+    got = run_child(tmp_path, "f3d_dvort", "CVTX_GB300_F3D_DVORT_CFG", cfg)
+    f, pts = f3d_dvort_case()
+    check(got["dvort"][SAMPLE], oracle.f3d_dvort(f, pts[SAMPLE]), tol=1e-5)

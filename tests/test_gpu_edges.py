@@ -85,8 +85,9 @@ def test_few_targets_every_op(gpu, reg, n_tgt):
 
 @pytest.mark.parametrize("n_tgt", [1, 7, 100])
 def test_few_targets_p2d_f3d(gpu, n_tgt):
-    """The few-target form of P2D and F3D velocity: targets on sources, at
-    filament ends and on a filament (the reference drops those terms)."""
+    """The few-target form of P2D velocity and F3D velocity and stretching:
+    targets on sources, at filament ends and on a filament (the reference
+    drops those terms)."""
     q = workloads.gaussian_patch_2d(300_001, seed=53)
     m = workloads.gaussian_patch_2d(n_tgt, seed=54)["coord"].copy()
     m[0] = q["coord"][0]
@@ -98,6 +99,9 @@ def test_few_targets_p2d_f3d(gpu, n_tgt):
     if n_tgt > 2:
         t[1] = 0.5 * (f["start"][9] + f["end"][9])
     close(gpu.f3d_vel(f, t), oracle.f3d_vel(f, t))
+    pts = workloads.uniform_cube(n_tgt, seed=57)
+    pts["coord"] = t
+    close(gpu.f3d_dvort(f, pts), oracle.f3d_dvort(f, pts))
 
 
 def test_few_target_form_beyond_grid_limit(gpu):
