@@ -58,8 +58,10 @@ REG = {"singular": 0, "winckelmans": 1, "planetary": 2, "gaussian": 3}
 OPS = {"veldvort": "fused vel+dvort", "vel": "vel", "dvort": "dvort",
        "vort": "vorticity field (5 sigma box cut-off)",
        "inf": "F3D influence matrix, 25,000 points x 20,000 filaments (2 GB)",
-       "m2s": "few targets: fused vel+dvort of the first 64 particles from all sources"}
+       "m2s": "few targets: fused vel+dvort of the first 64 particles from all sources",
+       "f3d_dvort": "F3D vortex stretching, wake sheet of N filaments on N particles"}
 M2S_TARGETS = 64
+F3D_DVORT_FLOPS = 62
 # influence matrix: F3D vel (51) + the dot with the direction (5) per entry
 INF_FLOPS = 56
 INF_SHAPE = (25_000, 20_000)
@@ -268,6 +270,7 @@ def run_ours(args):
     if op == "vort" and reg not in VORT_FLOPS:
         raise SystemExit("--op vort: the singular vorticity field is zero (no kernel)")
     flops_per = (VORT_FLOPS[reg] if op == "vort" else INF_FLOPS if op == "inf"
+                 else F3D_DVORT_FLOPS if op == "f3d_dvort"
                  else FLOPS[("veldvort", reg)] if op == "m2s" else FLOPS[(op, reg)])
     v_out = vel.data_ptr() if op in ("veldvort", "vel") else None
     d_out = dv.data_ptr() if op in ("veldvort", "dvort") else None
@@ -286,6 +289,12 @@ def run_ours(args):
         dirs[:, 2] = 1.0
         rfd, tfd, dd = (torch.from_numpy(x).cuda() for x in (rf, tf, dirs))
         om = torch.empty((nm, ni), dtype=torch.float32, device="cuda")
+    if op == "f3d_dvort":
+        fil = workloads.wake_sheet(n)
+        rf = np.zeros((n, 8), np.float32)
+        rf[:, 0:3], rf[:, 3], rf[:, 4:7] = fil["start"], fil["strength"], fil["end"]
+        rfd = torch.from_numpy(rf).cuda()
+        rcube = torch.from_numpy(p3d_records(workloads.uniform_cube(n, seed=12)).reshape(n, 8)).cuda()
 
     def step():
         if op == "inf":
@@ -294,6 +303,9 @@ def run_ours(args):
         elif op == "m2s":
             rc = lib.cvtx_gb300_dev_P3D_M2M(rec.data_ptr(), n, rec.data_ptr(), 2, M2S_TARGETS,
                                             vel.data_ptr(), dv.data_ptr(), reg, SIGMA, sh)
+        elif op == "f3d_dvort":
+            rc = lib.cvtx_gb300_dev_F3D_M2M_dvort(rfd.data_ptr(), n, rcube.data_ptr(), 2, n,
+                                                  vel.data_ptr(), sh)
         elif op == "vort":
             rc = lib.cvtx_gb300_dev_P3D_M2M_vort(rec.data_ptr(), n, rec.data_ptr(), 2, n,
                                                  vel.data_ptr(), reg, SIGMA, sh)
@@ -345,6 +357,7 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": OPS[op] if op == "inf" else
+                   OPS[op].replace("N ", f"{n} ") if op == "f3d_dvort" else
                    f"P3D vortex ring N={n}, {args.reg}, sigma={SIGMA}, {OPS[op]}"
                    + ("" if op == "m2s" else ", targets = sources"),
                    "interactions_per_step": pairs, "l2": "flushed between steps (256 MB write)",
