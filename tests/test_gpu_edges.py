@@ -267,8 +267,10 @@ def test_packed_p2d_f3d_ragged_sizes(gpu, n):
 @pytest.mark.parametrize("n", [8192, 12001])
 def test_packed_f3d_dvort(gpu, n):
     """The packed F3D stretching kernel (8,192 particles and up) against the
-    oracle, with particles at filament ends (terms the reference drops)."""
+    oracle, with particles at filament ends (terms the reference drops) and
+    zero-length filaments (whose per-filament 3 g / |r0| is infinite)."""
     f = workloads.wake_sheet(2000, seed=12)
+    f["end"][[7, 300, 1999]] = f["start"][[7, 300, 1999]]
     p = workloads.uniform_cube(n, seed=13)
     p["coord"][:30] = f["start"][:30]
     p["coord"][30:60] = f["end"][30:60]
