@@ -31,6 +31,26 @@ def test_no_sources_gives_zeros(gpu):
     assert not np.any(out)
 
 
+def test_no_sources_few_targets_gives_zeros(gpu):
+    """Zero sources with a few targets (the few-target forms of every op):
+    the outputs, prefilled, are overwritten with zeros."""
+    lib, vf = gpu.lib, C.byref(gpu.vortfunc("winckelmans"))
+    p = workloads.uniform_cube(5, seed=4)
+    q = workloads.gaussian_patch_2d(5, seed=4)
+    f = workloads.wake_sheet(3, seed=4)
+    pp, qp, fp = abi.ptr_array(p), abi.ptr_array(q), abi.ptr_array(f)
+    mes3 = np.ascontiguousarray(p["coord"])
+    mes2 = np.ascontiguousarray(q["coord"])
+    outs = [np.full((5, 3), 5.0, np.float32) for _ in range(4)] + [np.full((5, 2), 5.0, np.float32)]
+    lib.cvtx_P3D_M2M_vel(pp.ctypes.data, 0, mes3.ctypes.data, 5, outs[0].ctypes.data, vf, 0.05)
+    lib.cvtx_P3D_M2M_dvort(pp.ctypes.data, 0, pp.ctypes.data, 5, outs[1].ctypes.data, vf, 0.05)
+    lib.cvtx_F3D_M2M_vel(fp.ctypes.data, 0, mes3.ctypes.data, 5, outs[2].ctypes.data)
+    lib.cvtx_F3D_M2M_dvort(fp.ctypes.data, 0, pp.ctypes.data, 5, outs[3].ctypes.data)
+    lib.cvtx_P2D_M2M_vel(qp.ctypes.data, 0, mes2.ctypes.data, 5, outs[4].ctypes.data, vf, 0.05)
+    for o in outs:
+        assert not np.any(o), o
+
+
 @pytest.mark.parametrize("n", [1, 2, 31, 255, 256, 257, 511, 512, 513, 1023, 8191, 8192, 8193])
 def test_sizes_around_tiles(gpu, n):
     p = workloads.uniform_cube(n, seed=n)
