@@ -1,10 +1,10 @@
 #!/usr/bin/env python
 """Benchmark of the all-pairs P3D velocity + vortex-stretching path.
 
-Workload (one "step"): velocity and stretching of every particle of a vortex
-ring of 100,000 particles (radius 1, offsets N(0, 0.1^2), vorticity tangent
-with magnitude exp(-d^2/(2 0.1^2)), Winckelmans regularisation, sigma 0.05),
-i.e. 10^10 source-target interactions, each contributing to both outputs.
+Workload (one "step"): velocity and stretching of every particle of a
+uniform cube of 1,000,000 particles (coordinates U[-1,1]^3, vorticity
+components N(0, 0.1^2), volume 8/N, Winckelmans regularisation, sigma 0.05),
+i.e. 10^12 source-target interactions, each contributing to both outputs.
 Inputs are seeded synthetic data (no dataset is involved).
 
 Reported (one JSON line on rank 0):
@@ -16,6 +16,12 @@ Reported (one JSON line on rank 0):
   roofline   FP32-pipe roofline of the fused kernel: canonical flops per
              interaction (61 for Winckelmans vel+dvort) x interactions per
              launch / launch time, against the measured FP32 FMA peak;
+  parity     the headline's results on sampled targets against the
+             reference's CPU formulation (the oracle) and against FP64;
+  extras     per-op rates of the scale-up, precision and batched workloads,
+             each with its error against the FP64 oracle on sampled targets;
+  serving    the served mixed-size stream against plain per-request calls
+             (p50/p99 latency and interactions/s per arrival rate);
   cpu_baseline  the reference CPU path (compiled reference library when it
              is loadable on this host, else the oracle's C restatement of it)
              on all host cores over a bounded sample of targets.
@@ -51,10 +57,12 @@ FLOPS = {("vel", 1): 30, ("dvort", 1): 46, ("veldvort", 1): 61,
          ("vel", 0): 25, ("dvort", 0): 39, ("veldvort", 0): 49,
          ("vel", 2): 25, ("dvort", 2): 39, ("veldvort", 2): 49,
          ("vel", 3): 46, ("dvort", 3): 62, ("veldvort", 3): 77}
+VISC_FLOPS = {1: 22, 3: 17}
 # vorticity field (5 sigma box cut-off), FP32 operations per pair:
 # winckelmans 22, planetary 15, gaussian 17
 VORT_FLOPS = {1: 22, 2: 15, 3: 17}
 REG = {"singular": 0, "winckelmans": 1, "planetary": 2, "gaussian": 3}
+REG_NAME = {v: k for k, v in REG.items()}
 OPS = {"veldvort": "fused vel+dvort", "vel": "vel", "dvort": "dvort",
        "vort": "vorticity field (5 sigma box cut-off)",
        "inf": "F3D influence matrix, 25,000 points x 20,000 filaments (2 GB)",
@@ -66,45 +74,50 @@ F3D_DVORT_FLOPS = 62
 INF_FLOPS = 56
 INF_SHAPE = (25_000, 20_000)
 SIGMA = 0.05
-CPU_SAMPLE_TARGETS = 2048
+CPU_SAMPLE_TARGETS = 1024
+CHECK_TARGETS = 256          # sampled targets per FP64 / reference check
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
-    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=100_000, help="particles in the ring")
+    ap.add_argument("--workload", default="cube", choices=["cube", "ring"],
+                    help="cube: uniform cube (the plain workload's distribution); "
+                         "ring: the scale-up vortex ring")
+    ap.add_argument("--n", type=int, default=1_000_000, help="particles")
     ap.add_argument("--reg", default="winckelmans", choices=list(REG))
     ap.add_argument("--quick", action="store_true", help="skip the extra measurements")
     ap.add_argument("--op", default="veldvort", choices=list(OPS),
                     help="the kernel timed as the step; the benchmark is veldvort, the others "
                          "exist to profile one kernel with the same command")
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--serve-requests", type=int, default=64,
                     help="requests per arrival rate in the served-stream measurement")
     return ap.parse_args()
 
 
-def profiled_traffic(n, reg):
-    """DRAM bytes per launch of the benchmark kernel from the committed ncu
-    summary (profiles/), when it covers this workload; else None."""
-    if n != 100_000 or reg != "winckelmans":
-        return None
-    f = ROOT / "profiles" / "p3d_induce2_ring100k_launches.md"
-    try:
-        for line in f.read_text().splitlines():
-            if line.startswith("traffic_bytes_per_launch:"):
-                return int(line.split(":")[1])
-    except OSError:
-        pass
-    return None
-
-
 def dist_env():
     from cvortex_gb300.multi import dist_env as env
     return env()
+
+
+def workload(args):
+    from cvortex_gb300 import workloads
+    if args.workload == "ring":
+        return workloads.vortex_ring(args.n)
+    return workloads.uniform_cube(args.n)
+
+
+def workload_name(args, op="veldvort"):
+    """The workload both arms name identically: velocity and stretching of
+    every particle (the GPU arm runs them fused, the CPU arm as two calls)."""
+    kind = ("P3D vortex ring" if args.workload == "ring" else
+            "P3D uniform cube [-1,1]^3")
+    what = "vel + dvort, targets = sources" if op == "veldvort" else OPS[op]
+    return f"{kind} N={args.n}, {args.reg}, sigma={SIGMA}, {what}"
 
 
 def p3d_records(p):
@@ -113,6 +126,21 @@ def p3d_records(p):
     rec[:, 0, 3] = p["volume"]
     rec[:, 1, :3] = p["vorticity"]
     return rec
+
+
+def r4(x):
+    """Four significant digits (keeps the JSON line short)."""
+    return None if x is None else float(f"{x:.4g}")
+
+
+def sample_idx(n, m=CHECK_TARGETS, seed=11):
+    return np.sort(np.random.Generator(np.random.PCG64(seed)).choice(n, min(m, n), replace=False))
+
+
+def errs(got, ref):
+    """rel L2 and max per-target relative error of `got` against `ref`."""
+    from oracle import exact
+    return {"rel_l2": r4(exact.rel_l2(got, ref)), "max_rel": r4(exact.max_rel(got, ref))}
 
 
 # ---- CPU implementation of the reference path --------------------------------
@@ -165,22 +193,23 @@ def cpu_cores():
 def cpu_baseline(p, reg, min_s=12.0, max_reps=40, sample=CPU_SAMPLE_TARGETS):
     """The reference CPU formulation on all host cores: vel + dvort for
     `sample` seeded targets against all sources, repeated until about `min_s`
-    seconds of CPU work (at least three repeats)."""
+    seconds of CPU work (at least two repeats)."""
     os.environ.setdefault("OMP_NUM_THREADS", str(cpu_cores()))
     os.environ.setdefault("OMP_PROC_BIND", "spread")
     kind, ref = cpu_reference()
     idx = np.random.Generator(np.random.PCG64(7)).choice(len(p), min(sample, len(p)), replace=False)
     sub = p[np.sort(idx)].copy()
-    cpu_step(kind, ref, p, sub[:64].copy(), reg)   # warm caches / thread pool
+    cpu_step(kind, ref, p, sub[:32].copy(), reg)   # warm caches / thread pool
     t0 = time.perf_counter()
     reps = 0
-    while reps < 3 or (time.perf_counter() - t0 < min_s and reps < max_reps):
+    while reps < 2 or (time.perf_counter() - t0 < min_s and reps < max_reps):
         cpu_step(kind, ref, p, sub, reg)
         reps += 1
     dt = time.perf_counter() - t0
     pairs = reps * len(sub) * len(p)
-    return {"value": pairs / dt / 1e9, "unit": UNIT, "cores": int(os.environ["OMP_NUM_THREADS"]),
-            "kind": kind, "cpu_model": cpu_model(), "omp_proc_bind": os.environ["OMP_PROC_BIND"],
+    return {"value": r4(pairs / dt / 1e9), "unit": UNIT,
+            "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": kind,
+            "cpu_model": cpu_model(), "omp_proc_bind": os.environ["OMP_PROC_BIND"],
             "sample": f"{reps} x (vel + dvort) for {len(sub)} sampled targets x {len(p)} sources "
                       f"({dt:.1f} s of CPU time)"}
 
@@ -258,7 +287,7 @@ def run_ours(args):
     reg = REG[args.reg]
     n = args.n
 
-    p = workloads.vortex_ring(n)
+    p = workload(args)
     rec = torch.from_numpy(p3d_records(p).reshape(n, 8)).cuda()
     vel = torch.empty((n, 3), dtype=torch.float32, device="cuda")
     dv = torch.empty((n, 3), dtype=torch.float32, device="cuda")
@@ -335,7 +364,7 @@ def run_ours(args):
     launches0 = cv.launches()
     t_start.record()
     for k in range(args.steps):
-        flush.zero_()            # L2 flush between steps (inputs are 3.2 MB)
+        flush.zero_()            # L2 flush between steps (inputs are 32 MB)
         ev[k][0].record()
         step()
         ev[k][1].record()
@@ -352,22 +381,25 @@ def run_ours(args):
     value = world * args.steps * pairs / (t_max * 1e-3) / 1e9
     flops = flops_per * pairs
     achieved = flops / (kernel_ms * 1e-3) / 1e12
+    if op == "inf":
+        wl = OPS[op]
+    elif op == "f3d_dvort":
+        wl = OPS[op].replace("N ", f"{n} ")
+    else:
+        wl = workload_name(args, op) + ("" if op in ("m2s", "veldvort") else ", targets = sources")
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": OPS[op] if op == "inf" else
-                   OPS[op].replace("N ", f"{n} ") if op == "f3d_dvort" else
-                   f"P3D vortex ring N={n}, {args.reg}, sigma={SIGMA}, {OPS[op]}"
-                   + ("" if op == "m2s" else ", targets = sources"),
-                   "interactions_per_step": pairs, "l2": "flushed between steps (256 MB write)",
+        "config": {"workload": wl, "interactions_per_step": pairs,
+                   "kernel": "fused vel+dvort (device-pointer API)" if op == "veldvort" else op,
+                   "l2": "flushed between steps (256 MB write)",
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
                      "frac": achieved / peak.value if peak.value else None,
-                     "traffic": profiled_traffic(n, args.reg) if op == "veldvort" else None,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
-                                       "launch (profiles/p3d_induce2_ring100k_launches.md); "
-                                       "algorithmic bytes 5.6 MB, the rest FP64 split partials",
+                     "traffic": None,
+                     "traffic_note": "not measured in this run (ncu summaries under profiles/); "
+                                     "algorithmic bytes per launch 32 B x N in, 24 B x N out",
                      "peak_source": "measured FP32 FMA probe, max of scalar FFMA "
                                     f"{p_scalar.value:.2f} and packed f32x2 FFMA "
                                     f"{p_packed.value:.2f} TFLOP/s",
@@ -376,10 +408,12 @@ def run_ours(args):
         "gpu_launches": launches,
         "clocks": clk,
     }
+    if rank == 0 and op == "veldvort":
+        out["parity"] = headline_parity(p, vel, dv, args)
     if rank == 0 and not args.quick and op == "veldvort":
         out["e2e"] = e2e_abi(cv, p, args)
-        out["serving"] = serve_extra(cv, lib, count=args.serve_requests)
         out["extras"] = extras(cv, lib, args, torch, sh, peak.value)
+        out["serving"] = serve_extra(cv, lib, count=args.serve_requests)
     if rank == 0 and world == 1 and op == "veldvort":
         out["cpu_baseline"] = cpu_baseline(p, args.reg)
     if rank == 0:
@@ -388,9 +422,27 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def headline_parity(p, vel, dv, args):
+    """The timed step's last results on sampled targets: against the
+    reference's CPU formulation (oracle, all sources) and against FP64."""
+    import oracle
+    idx = sample_idx(len(p))
+    gv = vel.cpu().numpy()[idx]
+    gd = dv.cpu().numpy()[idx]
+    sub = p[idx].copy()
+    rv = oracle.p3d_vel(p, sub["coord"], args.reg, SIGMA)
+    rd = oracle.p3d_dvort(p, sub, args.reg, SIGMA)
+    ev, ed = oracle.exact_p3d_vel_dvort(p, sub["coord"], sub["vorticity"], args.reg, SIGMA)
+    return {"targets": len(idx), "vel_vs_reference": errs(gv, rv),
+            "dvort_vs_reference": errs(gd, rd), "vel_vs_fp64": errs(gv, ev),
+            "dvort_vs_fp64": errs(gd, ed), "reference_vs_fp64": {
+                "vel": r4(errs(rv, ev)["rel_l2"]), "dvort": r4(errs(rd, ed)["rel_l2"])}}
+
+
 def e2e_abi(cv, p, args):
     """Reference ABI with host buffers: cvtx_P3D_M2M_vel + cvtx_P3D_M2M_dvort."""
     from cvortex_gb300 import abi
+    import oracle
     n = len(p)
     lib = cv.lib
     ptrs = abi.ptr_array(p)
@@ -410,6 +462,9 @@ def e2e_abi(cv, p, args):
     dt = (time.perf_counter() - t0) / args.e2e_steps
     if not (np.all(np.isfinite(o1)) and np.all(np.isfinite(o2))):
         raise RuntimeError(f"e2e produced non-finite results: {cv.last_error()}")
+    idx = sample_idx(n, seed=12)
+    sub = p[idx].copy()
+    ev, ed = oracle.exact_p3d_vel_dvort(p, sub["coord"], sub["vorticity"], args.reg, SIGMA)
     vel_dv = np.zeros((n, 3), np.float32), np.zeros((n, 3), np.float32)
 
     def fused():
@@ -428,7 +483,8 @@ def e2e_abi(cv, p, args):
             "d2h_bytes_per_step": 2 * (n * 12 + 4),
             "ms_per_step": dt * 1e3,
             "calls": "cvtx_P3D_M2M_vel + cvtx_P3D_M2M_dvort (reference ABI, host pointers)",
-            "fused_extension": {"value": n * n / dtf / 1e9, "ms_per_step": dtf * 1e3,
+            "fp64": {"vel": errs(o1[idx], ev), "dvort": errs(o2[idx], ed)},
+            "fused_extension": {"value": r4(n * n / dtf / 1e9), "ms_per_step": r4(dtf * 1e3),
                                 "h2d_bytes_per_step": n * 32,
                                 "d2h_bytes_per_step": 2 * n * 12 + 4,
                                 "call": "cvtx_gb300_P3D_M2M_vel_dvort"}}
@@ -454,64 +510,84 @@ def measured_hbm_gbs():
         return None
 
 
+def rate(pairs, ms, flops, peak):
+    return {"ginter_s": r4(pairs / ms / 1e6),
+            "fp32_frac": r4(flops * pairs / (ms * 1e-3) / 1e12 / peak)}
+
+
 def extras(cv, lib, args, torch, sh, peak):
-    """Per-op rates on the scale-up workloads and the 1M-particle target."""
+    """Per-op rates on the scale-up, precision and batched workloads, each
+    with its error against the FP64 oracle on sampled targets (rel L2 and
+    max relative error per target)."""
+    import oracle
     from cvortex_gb300 import workloads
     hbm_peak = measured_hbm_gbs()
     res = {}
-    n = args.n
+    n = 100_000
     p = workloads.vortex_ring(n)
+    idx = sample_idx(n)
+    sub = p[idx].copy()
     rec = torch.from_numpy(p3d_records(p).reshape(n, 8)).cuda()
     o1 = torch.empty((n, 3), dtype=torch.float32, device="cuda")
     o2 = torch.empty((n, 3), dtype=torch.float32, device="cuda")
     for rname, r in REG.items():
         row = {}
+        ev, ed = oracle.exact_p3d_vel_dvort(p, sub["coord"], sub["vorticity"], rname, SIGMA)
         for op, (a, b) in {"vel": (o1, None), "dvort": (None, o2), "veldvort": (o1, o2)}.items():
             f = lambda: lib.cvtx_gb300_dev_P3D_M2M(rec.data_ptr(), n, rec.data_ptr(), 2, n,
                                                    a.data_ptr() if a is not None else None,
                                                    b.data_ptr() if b is not None else None,
                                                    r, SIGMA, sh)
             ms = timed_dev(f, torch, 5)
-            row[op] = {"ginter_s": n * n / ms / 1e6,
-                       "fp32_frac": FLOPS[(op, r)] * n * n / (ms * 1e-3) / 1e12 / peak}
-        if r in (1, 3):
+            row[op] = rate(n * n, ms, FLOPS[(op, r)], peak)
+            e = []
+            if a is not None:
+                e.append(errs(a.cpu().numpy()[idx], ev)["rel_l2"])
+            if b is not None:
+                e.append(errs(b.cpu().numpy()[idx], ed)["rel_l2"])
+            row[op]["fp64_rel_l2"] = max(e)
+        if r in VISC_FLOPS:
             f = lambda: lib.cvtx_gb300_dev_P3D_M2M_visc(rec.data_ptr(), n, rec.data_ptr(), 2, n,
                                                         o1.data_ptr(), r, SIGMA, 1e-3, sh)
             ms = timed_dev(f, torch, 5)
-            row["visc"] = {"ginter_s": n * n / ms / 1e6,
-                           "fp32_frac": (22 if r == 1 else 17) * n * n / (ms * 1e-3) / 1e12 / peak}
+            row["visc"] = rate(n * n, ms, VISC_FLOPS[r], peak)
+            row["visc"]["fp64_rel_l2"] = errs(o1.cpu().numpy()[idx],
+                                              oracle.exact_p3d_visc(p, sub, rname, SIGMA, 1e-3))["rel_l2"]
         if r in VORT_FLOPS:
             f = lambda: lib.cvtx_gb300_dev_P3D_M2M_vort(rec.data_ptr(), n, rec.data_ptr(), 2, n,
                                                         o1.data_ptr(), r, SIGMA, sh)
             ms = timed_dev(f, torch, 5)
-            row["vort"] = {"ginter_s": n * n / ms / 1e6,
-                           "fp32_frac": VORT_FLOPS[r] * n * n / (ms * 1e-3) / 1e12 / peak}
-        res[f"ring{n}_{rname}"] = row
+            row["vort"] = rate(n * n, ms, VORT_FLOPS[r], peak)
+            row["vort"]["fp64_rel_l2"] = errs(o1.cpu().numpy()[idx],
+                                              oracle.exact_p3d_vort(p, sub["coord"], rname, SIGMA))["rel_l2"]
+        res[f"ring{n // 1000}k_{rname}"] = row
+    del rec, o1, o2
     q = workloads.gaussian_patch_2d(200_000)
+    nq = len(q)
+    qi = sample_idx(nq)
     rq = torch.from_numpy(np.ascontiguousarray(
         np.stack([q["coord"][:, 0], q["coord"][:, 1], q["vorticity"], q["area"]], 1))).cuda()
-    o = torch.empty((len(q), 2), dtype=torch.float32, device="cuda")
-    f = lambda: lib.cvtx_gb300_dev_P2D_M2M_vel(rq.data_ptr(), len(q), rq.data_ptr(), len(q),
-                                               o.data_ptr(), 3, SIGMA, sh)
-    ms = timed_dev(f, torch, 5)
-    res["p2d_patch200k_gaussian_vel"] = {"ginter_s": len(q) ** 2 / ms / 1e6,
-                                         "fp32_frac": 13 * len(q) ** 2 / (ms * 1e-3) / 1e12 / peak}
-    f = lambda: lib.cvtx_gb300_dev_P2D_M2M_vel(rq.data_ptr(), len(q), rq.data_ptr(), len(q),
-                                               o.data_ptr(), 1, SIGMA, sh)
-    ms = timed_dev(f, torch, 5)
-    res["p2d_patch200k_winckelmans_vel"] = {"ginter_s": len(q) ** 2 / ms / 1e6,
-                                            "fp32_frac": 15 * len(q) ** 2 / (ms * 1e-3) / 1e12 / peak}
-    ov = torch.empty((len(q),), dtype=torch.float32, device="cuda")
+    o = torch.empty((nq, 2), dtype=torch.float32, device="cuda")
+    for rname, r, fl in (("gaussian", 3, 13), ("winckelmans", 1, 15)):
+        f = lambda: lib.cvtx_gb300_dev_P2D_M2M_vel(rq.data_ptr(), nq, rq.data_ptr(), nq,
+                                                   o.data_ptr(), r, SIGMA, sh)
+        ms = timed_dev(f, torch, 5)
+        res[f"p2d_patch200k_{rname}_vel"] = rate(nq * nq, ms, fl, peak)
+        res[f"p2d_patch200k_{rname}_vel"]["fp64_rel_l2"] = errs(
+            o.cpu().numpy()[qi], oracle.exact_p2d_vel(q, q["coord"][qi], rname, SIGMA))["rel_l2"]
+    ov = torch.empty((nq,), dtype=torch.float32, device="cuda")
     for rname, r, fl in (("winckelmans", 1, 16), ("gaussian", 3, 10)):
-        f = lambda: lib.cvtx_gb300_dev_P2D_M2M_visc(rq.data_ptr(), len(q), rq.data_ptr(), len(q),
+        f = lambda: lib.cvtx_gb300_dev_P2D_M2M_visc(rq.data_ptr(), nq, rq.data_ptr(), nq,
                                                     ov.data_ptr(), r, SIGMA, 1e-3, sh)
         ms = timed_dev(f, torch, 5)
-        res[f"p2d_patch200k_{rname}_visc"] = {
-            "ginter_s": len(q) ** 2 / ms / 1e6,
-            "fp32_frac": fl * len(q) ** 2 / (ms * 1e-3) / 1e12 / peak}
+        res[f"p2d_patch200k_{rname}_visc"] = rate(nq * nq, ms, fl, peak)
+        res[f"p2d_patch200k_{rname}_visc"]["fp64_rel_l2"] = errs(
+            ov.cpu().numpy()[qi], oracle.exact_p2d_visc(q, q[qi], rname, SIGMA, 1e-3))["rel_l2"]
+    del rq, o, ov
     nf = 100_000
     fil = workloads.wake_sheet(nf)
     pts = workloads.sheet_targets(nf)
+    fi = sample_idx(nf)
     rf = np.zeros((nf, 8), np.float32)
     rf[:, 0:3] = fil["start"]
     rf[:, 3] = fil["strength"]
@@ -523,9 +599,18 @@ def extras(cv, lib, args, torch, sh, peak):
     f = lambda: lib.cvtx_gb300_dev_F3D_M2M_vel(rfd.data_ptr(), nf, tfd.data_ptr(), 1, nf,
                                                of.data_ptr(), sh)
     ms = timed_dev(f, torch, 5)
-    res["f3d_sheet100k_vel"] = {"ginter_s": nf * nf / ms / 1e6,
-                                "fp32_frac": 51 * nf * nf / (ms * 1e-3) / 1e12 / peak}
-    # influence matrix: write-bound (4 B per entry); 25,000 points x 20,000 filaments
+    res["f3d_sheet100k_vel"] = rate(nf * nf, ms, 51, peak)
+    res["f3d_sheet100k_vel"]["fp64_rel_l2"] = errs(
+        of.cpu().numpy()[fi], oracle.exact_f3d_vel(fil, pts[fi]))["rel_l2"]
+    cube = workloads.uniform_cube(nf, seed=12)
+    rc = torch.from_numpy(p3d_records(cube).reshape(nf, 8)).cuda()
+    f = lambda: lib.cvtx_gb300_dev_F3D_M2M_dvort(rfd.data_ptr(), nf, rc.data_ptr(), 2, nf,
+                                                 of.data_ptr(), sh)
+    ms = timed_dev(f, torch, 3)
+    res["f3d_sheet100k_dvort_cube100k"] = rate(nf * nf, ms, 62, peak)
+    res["f3d_sheet100k_dvort_cube100k"]["fp64_rel_l2"] = errs(
+        of.cpu().numpy()[fi], oracle.exact_f3d_dvort(fil, cube[fi]))["rel_l2"]
+    # influence matrix: 25,000 points x 20,000 filaments, 4 B per entry
     nm, ni = INF_SHAPE
     dirs = np.zeros((nm, 4), np.float32)
     dirs[:, 2] = 1.0
@@ -535,41 +620,31 @@ def extras(cv, lib, args, torch, sh, peak):
                                                 nm, om.data_ptr(), sh)
     ms = timed_dev(f, torch, 5)
     gbs = 4.0 * nm * ni / (ms * 1e-3) / 1e9
-    res["f3d_inf_mtrx_25kx20k"] = {"ms": ms, "write_gbs": gbs,
-                                   "hbm_frac": gbs / hbm_peak if hbm_peak else None,
-                                   "hbm_peak_gbs": hbm_peak,
-                                   "fp32_frac": INF_FLOPS * nm * ni / (ms * 1e-3) / 1e12 / peak}
-    del om
-    cube = workloads.uniform_cube(nf, seed=12)
-    rc = torch.from_numpy(p3d_records(cube).reshape(nf, 8)).cuda()
-    f = lambda: lib.cvtx_gb300_dev_F3D_M2M_dvort(rfd.data_ptr(), nf, rc.data_ptr(), 2, nf,
-                                                 of.data_ptr(), sh)
-    ms = timed_dev(f, torch, 3)
-    res["f3d_sheet100k_dvort_cube100k"] = {"ginter_s": nf * nf / ms / 1e6,
-                                           "fp32_frac": 62 * nf * nf / (ms * 1e-3) / 1e12 / peak}
+    rows = sample_idx(nm, 64)
+    res["f3d_inf_mtrx_25kx20k"] = {
+        "ms": r4(ms), "write_gbs": r4(gbs), "hbm_frac": r4(gbs / hbm_peak) if hbm_peak else None,
+        "fp32_frac": r4(INF_FLOPS * nm * ni / (ms * 1e-3) / 1e12 / peak),
+        "fp64_rel_l2": errs(om.cpu().numpy()[rows], oracle.exact_f3d_vel(
+            fil[:ni], pts[rows], dirs[rows, :3]))["rel_l2"]}
+    del om, rfd, tfd, rc, of
     res["batch512"] = batch_extra(cv, lib, torch, sh)
     res["redistribute_ring200k_m4p"] = redistribute_extra(cv, lib)
+    # the precision configuration's input: Gaussian, sigma 0.01, 1 % twins
+    # closer than 1e-3 sigma; errors on sampled targets plus twins
     m = 1_000_000
-    big = workloads.uniform_cube(m)
-    rb = torch.from_numpy(p3d_records(big).reshape(m, 8)).cuda()
+    tw = workloads.cube_with_twins(m, 0.01)
+    rb = torch.from_numpy(p3d_records(tw).reshape(m, 8)).cuda()
     b1 = torch.empty((m, 3), dtype=torch.float32, device="cuda")
     b2 = torch.empty((m, 3), dtype=torch.float32, device="cuda")
     f = lambda: lib.cvtx_gb300_dev_P3D_M2M(rb.data_ptr(), m, rb.data_ptr(), 2, m, b1.data_ptr(),
-                                           b2.data_ptr(), 1, SIGMA, sh)
-    ms = timed_dev(f, torch, 2)
-    res["cube1M_winckelmans_veldvort"] = {
-        "ginter_s": m * m / ms / 1e6, "ms": ms,
-        "fp32_frac": 61 * m * m / (ms * 1e-3) / 1e12 / peak}
-    # the precision configuration's input: Gaussian, sigma 0.01, 1 % twins
-    # closer than 1e-3 sigma (its errors against FP64 come from the tests)
-    tw = workloads.cube_with_twins(m, 0.01)
-    rb.copy_(torch.from_numpy(p3d_records(tw).reshape(m, 8)))
-    f = lambda: lib.cvtx_gb300_dev_P3D_M2M(rb.data_ptr(), m, rb.data_ptr(), 2, m, b1.data_ptr(),
                                            b2.data_ptr(), 3, 0.01, sh)
     ms = timed_dev(f, torch, 2)
-    res["twins1M_gaussian_veldvort"] = {
-        "ginter_s": m * m / ms / 1e6, "ms": ms,
-        "fp32_frac": FLOPS[("veldvort", 3)] * m * m / (ms * 1e-3) / 1e12 / peak}
+    ti = np.unique(np.concatenate([sample_idx(m, 192, seed=13), np.arange(m - 64, m)]))
+    ev, ed = oracle.exact_p3d_vel_dvort(tw, tw["coord"][ti], tw["vorticity"][ti], "gaussian", 0.01)
+    res["twins1M_gaussian_veldvort"] = rate(m * m, ms, FLOPS[("veldvort", 3)], peak)
+    res["twins1M_gaussian_veldvort"].update(
+        {"ms": r4(ms), "vel_fp64": errs(b1.cpu().numpy()[ti], ev),
+         "dvort_fp64": errs(b2.cpu().numpy()[ti], ed), "targets_checked": int(len(ti))})
     return res
 
 
@@ -592,25 +667,29 @@ def redistribute_extra(cv, lib, n=200_000, gd=0.01):
 
     run()
     m_gpu, t_gpu = min((run() for _ in range(3)), key=lambda x: x[1])
+    gpu_out = out[:m_gpu].copy()
     cv.set_accelerated(False)
     try:
         m_host, t_host = run()
     finally:
         cv.set_accelerated(True)
-    if m_gpu != m_host:
+    if m_gpu != m_host or gpu_out.tobytes() != out[:m_host].tobytes():
         raise RuntimeError("redistribution: GPU and host paths disagree")
-    return {"particles_in": n, "particles_out": int(m_gpu), "grid_points_touched": n * 125,
-            "gpu_ms": t_gpu * 1e3, "host_ms": t_host * 1e3, "host_cores": cpu_cores(),
-            "speedup": t_host / t_gpu}
+    return {"particles_out": int(m_gpu), "gpu_ms": r4(t_gpu * 1e3), "host_ms": r4(t_host * 1e3),
+            "host_cores": cpu_cores(), "speedup": r4(t_host / t_gpu),
+            "gpu_equals_host": True}
 
 
 def batch_extra(cv, lib, torch, sh, count=512):
     """512 independent vel+dvort problems (uniform cube each, Winckelmans,
     sigma 0.05), sizes log-uniform in [1,000, 50,000]: one plain device call
-    per problem vs the batched persistent launch (autotuned, graph-captured)."""
+    per problem vs the batched persistent launch (autotuned, graph-captured).
+    The batched results of the three largest and three random problems are
+    checked against FP64 on sampled targets."""
+    import oracle
     from cvortex_gb300 import abi, workloads
     sizes = workloads.batch_sizes(count)
-    keep, probs = [], []
+    keep, probs, parts = [], [], []
     for i, n in enumerate(sizes):
         n = int(n)
         p = workloads.uniform_cube(n, seed=10_000 + i)
@@ -618,6 +697,7 @@ def batch_extra(cv, lib, torch, sh, count=512):
         v = torch.empty((n, 3), dtype=torch.float32, device="cuda")
         d = torch.empty((n, 3), dtype=torch.float32, device="cuda")
         keep.append((n, rec, v, d))
+        parts.append(p)
         probs.append(abi.cvtx_gb300_p3d_problem(rec.data_ptr(), n, rec.data_ptr(), 2, n,
                                                 v.data_ptr(), d.data_ptr(), SIGMA))
     pairs = float(sum(int(n) * int(n) for n in sizes))
@@ -642,6 +722,9 @@ def batch_extra(cv, lib, torch, sh, count=512):
                     raise RuntimeError(cv.last_error())
 
     ms_plain_sep = timed_dev(plain_separate, torch, 2)
+    for _, _, v, d in keep:
+        v.fill_(float("nan"))
+        d.fill_(float("nan"))
     arr = (abi.cvtx_gb300_p3d_problem * count)(*probs)
     b = lib.cvtx_gb300_batch_create(arr, count, 1, 3)
     if not b:
@@ -664,84 +747,42 @@ def batch_extra(cv, lib, torch, sh, count=512):
                                   C.byref(graph), None)
     finally:
         lib.cvtx_gb300_batch_destroy(b)
-    return {"problems": count, "interactions": pairs,
-            "sizes": [int(sizes.min()), int(sizes.max())],
-            "plain_ms": ms_plain, "plain_ginter_s": pairs / ms_plain / 1e6,
-            "plain_separate_ms": ms_plain_sep,
-            "plain_separate_ginter_s": pairs / ms_plain_sep / 1e6,
-            "plain_note": "plain = one fused vel+dvort device call per problem; plain_separate = "
-                          "a vel call then a dvort call per problem",
-            "batched_ms": ms_batch, "batched_ginter_s": pairs / ms_batch / 1e6,
-            "speedup": ms_plain / ms_batch, "speedup_vs_separate": ms_plain_sep / ms_batch,
-            "tuned_shape": [tpt.value, nt.value],
-            "tuned_chunk": chunk.value, "items": items.value, "graph": bool(graph.value),
-            "tune_s": tune_s}
+    order = np.argsort(sizes)
+    chk = list(order[-3:]) + list(np.random.Generator(np.random.PCG64(14)).choice(count, 3, False))
+    worst = {"vel": 0.0, "dvort": 0.0}
+    for i in chk:
+        n, _, v, d = keep[i]
+        ti = sample_idx(n, 64, seed=int(i))
+        sub = parts[i][ti]
+        ev, ed = oracle.exact_p3d_vel_dvort(parts[i], sub["coord"], sub["vorticity"],
+                                            "winckelmans", SIGMA)
+        worst["vel"] = max(worst["vel"], errs(v.cpu().numpy()[ti], ev)["rel_l2"])
+        worst["dvort"] = max(worst["dvort"], errs(d.cpu().numpy()[ti], ed)["rel_l2"])
+    return {"problems": count, "sizes": [int(sizes.min()), int(sizes.max())],
+            "plain_ginter_s": r4(pairs / ms_plain / 1e6),
+            "plain_separate_ginter_s": r4(pairs / ms_plain_sep / 1e6),
+            "batched_ms": r4(ms_batch), "batched_ginter_s": r4(pairs / ms_batch / 1e6),
+            "speedup": r4(ms_plain / ms_batch), "speedup_vs_separate": r4(ms_plain_sep / ms_batch),
+            "tuned": [tpt.value, nt.value, chunk.value], "graph": bool(graph.value),
+            "tune_s": r4(tune_s), "fp64_rel_l2_worst_of_6": {k: r4(x) for k, x in worst.items()}}
 
 
 SERVE_RATES = (100, 300, 1000, 3000, 5000)
+LIGHT_RATES = (100, 300, 1000)
 
 
-def serve_extra(cv, lib, count=64, steps=10, dt=1e-3, rates=SERVE_RATES):
-    """Served mixed-size stream vs plain per-request ABI calls.
-
-    Stream: Poisson arrivals, 60% P3D vel+dvort (uniform cube, Winckelmans,
-    sigma 0.05), 25% P2D vel (Gaussian patch, Winckelmans), 15% F3D vel (wake
-    sheet on as many tracer points), sizes log-uniform on [500, 200,000],
-    `steps` resident forward-Euler steps per client. The same requests are
-    replayed at every rate (arrivals scale with 1/rate).
-
-    served: the serving loop, latency = submit -> results in host memory.
-    plain:  one request at a time through the reference ABI with host
-            buffers (cvtx_P3D_M2M_vel + cvtx_P3D_M2M_dvort / cvtx_P2D_M2M_vel /
-            cvtx_F3D_M2M_vel per step, Euler update on the host); its
-            latencies at each rate are those of a FIFO queue fed the same
-            arrivals, with each request's measured service time.
-    """
-    from cvortex_gb300 import serve, workloads
-    arrival, kinds, sizes, seeds = workloads.serve_stream(count, rate=1.0)
-    inputs = [workloads.serve_request_arrays(int(k), int(n), int(sd))
-              for k, n, sd in zip(kinds, sizes, seeds)]
-
-    def build():
-        out = []
-        for k, (a, b) in zip(kinds, inputs):
-            kw = dict(n_steps=steps, dt=dt)
-            out.append(serve.Request.p3d(a, **kw) if k == 0 else
-                       serve.Request.p2d(a, **kw) if k == 1 else serve.Request.f3d(a, b, **kw))
-        return out
-
-    pairs = float(sum(r.interactions for r in build()))
-    res = {"requests": count, "steps_per_client": steps,
-           "mix": {"p3d_vel_dvort": int((kinds == 0).sum()), "p2d_vel": int((kinds == 1).sum()),
-                   "f3d_vel": int((kinds == 2).sum())},
-           "sizes": [int(sizes.min()), int(sizes.max())], "interactions": pairs, "rates": {}}
-    srv = serve.Server(lib, n_slots=32)
-    try:
-        warm = build()[:4]                        # first-use costs out of the timed runs
-        for r in warm:
-            srv.submit(r)
-        srv.drain()
-        for rate in rates:
-            srv.reset_stats()
-            reqs = build()
-            srv.replay(reqs, arrival / rate)
-            if not srv.drain(600_000):
-                raise RuntimeError("serving drain timed out")
-            st = srv.stats()
-            if st["completed"] != count:
-                raise RuntimeError(f"served {st['completed']}/{count}: {cv.last_error()}")
-            res["rates"][str(rate)] = {
-                "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
-                "queue_p50_ms": st["queue_p50_ms"], "span_s": st["span_s"],
-                "ginter_s": st["interactions"] / st["span_s"] / 1e9,
-                "hbm_peak_bytes": st["hbm_peak"], "gpu_launches": st["kernel_launches"]}
-    finally:
-        srv.close()
-
-    # plain per-request ABI calls, each request's service time measured once
-    svc = []
-    for k, (a, b) in zip(kinds, inputs):
-        t0 = time.perf_counter()
+def plain_measured(cv, kinds, inputs, arrival, steps, dt):
+    """Plain per-request ABI calls served by one worker thread in arrival
+    order: each request waits for its arrival time, then runs its `steps`
+    steps through the reference ABI with host buffers (cvtx_P3D_M2M_vel +
+    cvtx_P3D_M2M_dvort / cvtx_P2D_M2M_vel / cvtx_F3D_M2M_vel, Euler update
+    on the host). Returns (latencies in ms, span in s)."""
+    lat = []
+    t0 = time.perf_counter()
+    for t_arr, k, (a, b) in zip(arrival, kinds, inputs):
+        now = time.perf_counter() - t0
+        if now < t_arr:
+            time.sleep(t_arr - now)
         if k == 0:
             q = a.copy()
             for _ in range(steps):
@@ -759,27 +800,98 @@ def serve_extra(cv, lib, count=64, steps=10, dt=1e-3, rates=SERVE_RATES):
             for _ in range(steps):
                 u = cv.f3d_vel(a, x)
                 x += np.float32(dt) * u
-        svc.append(time.perf_counter() - t0)
+        lat.append((time.perf_counter() - t0 - t_arr) * 1e3)
+    span = time.perf_counter() - t0 - arrival[0]
     if cv.last_error():
         raise RuntimeError(cv.last_error())
-    svc = np.array(svc)
-    plain = {"ginter_s_busy": pairs / svc.sum() / 1e9, "service_s_total": float(svc.sum()),
-             "rates": {}}
-    for rate in rates:
-        arr = arrival / rate
-        end, lat = 0.0, []
-        for t, s in zip(arr, svc):
-            end = max(end, t) + s
-            lat.append(end - t)
-        lat = np.array(lat) * 1e3
-        plain["rates"][str(rate)] = {
-            "p50_ms": float(np.percentile(lat, 50, method="inverted_cdf")),
-            "p99_ms": float(np.percentile(lat, 99, method="inverted_cdf")),
-            "ginter_s": pairs / (end - arr[0]) / 1e9}
-    res["plain"] = plain
-    res["speedup_ginter_s"] = {r: res["rates"][r]["ginter_s"] / plain["rates"][r]["ginter_s"]
-                               for r in res["rates"]}
+    return np.array(lat), span
+
+
+def pct(x, q):
+    return float(np.percentile(x, q, method="inverted_cdf"))
+
+
+def serve_stream_run(cv, lib, count, lo, hi, rates, steps, dt):
+    """One served stream (Poisson arrivals, 60/25/15 mix of P3D vel+dvort,
+    P2D vel, F3D vel, sizes log-uniform on [lo, hi], `steps` resident
+    forward-Euler steps per client) at each rate, and the same arrivals
+    through plain per-request ABI calls (measured, one worker thread)."""
+    from cvortex_gb300 import serve, workloads
+    arrival, kinds, sizes, seeds = workloads.serve_stream(count, rate=1.0, lo=lo, hi=hi)
+    inputs = [workloads.serve_request_arrays(int(k), int(n), int(sd))
+              for k, n, sd in zip(kinds, sizes, seeds)]
+
+    def build():
+        out = []
+        for k, (a, b) in zip(kinds, inputs):
+            kw = dict(n_steps=steps, dt=dt)
+            out.append(serve.Request.p3d(a, **kw) if k == 0 else
+                       serve.Request.p2d(a, **kw) if k == 1 else serve.Request.f3d(a, b, **kw))
+        return out
+
+    pairs = float(sum(r.interactions for r in build()))
+    res = {"requests": count, "sizes": [int(sizes.min()), int(sizes.max())],
+           "mix": [int((kinds == i).sum()) for i in range(3)], "interactions": r4(pairs)}
+    srv = serve.Server(lib, n_slots=32)
+    served = {}
+    try:
+        warm = build()[:4]                        # first-use costs out of the timed runs
+        for r in warm:
+            srv.submit(r)
+        srv.drain()
+        for rt in rates:
+            srv.reset_stats()
+            srv.replay(build(), arrival / rt)
+            if not srv.drain(600_000):
+                raise RuntimeError("serving drain timed out")
+            st = srv.stats()
+            if st["completed"] != count:
+                raise RuntimeError(f"served {st['completed']}/{count}: {cv.last_error()}")
+            served[rt] = st
+    finally:
+        srv.close()
+    res["rates"] = {}
+    for rt in rates:
+        st = served[rt]
+        lat, span = plain_measured(cv, kinds, inputs, arrival / rt, steps, dt)
+        s_g = st["interactions"] / st["span_s"] / 1e9
+        p_g = pairs / span / 1e9
+        res["rates"][str(rt)] = {
+            "served": [r4(st["p50_ms"]), r4(st["p99_ms"]), r4(s_g)],
+            "plain": [r4(pct(lat, 50)), r4(pct(lat, 99)), r4(p_g)],
+            "x": r4(s_g / p_g)}
     return res
+
+
+def serve_extra(cv, lib, count=64, steps=10, dt=1e-3):
+    """Served mixed-size streams vs plain per-request ABI calls: the
+    benchmark's stream (sizes 500-200,000, far above the GPU's capacity at
+    every rate, so latency is queueing) and a light stream (sizes
+    500-20,000) whose offered load stays below capacity at 100-300 req/s.
+    Per rate: served and plain [p50 ms, p99 ms, G interactions/s], and x =
+    served / plain interactions/s; plain latencies are measured."""
+    out = {"fields": "[p50_ms, p99_ms, Ginteractions/s]",
+           "light": serve_stream_run(cv, lib, count, 500, 20_000, LIGHT_RATES, steps, dt),
+           "stream": serve_stream_run(cv, lib, count, 500, 200_000, SERVE_RATES, steps, dt)}
+    out["served_one_p3d_fp64"] = served_one_check(lib)
+    return out
+
+
+def served_one_check(lib, n=200_000):
+    """One served P3D request of 200,000 particles (one step), its velocity
+    on sampled targets against FP64."""
+    import oracle
+    from cvortex_gb300 import serve, workloads
+    p = workloads.uniform_cube(n, seed=31)
+    with serve.Server(lib, n_slots=2) as srv:
+        req = serve.Request.p3d(p, n_steps=1, dt=1e-3)
+        rid = srv.submit(req)
+        if not rid or srv.wait(rid, 120_000) != 0:
+            raise RuntimeError("served check request failed")
+    ti = sample_idx(n, 128, seed=15)
+    ev, _ = oracle.exact_p3d_vel_dvort(p, p["coord"][ti], None, "winckelmans", SIGMA,
+                                       want_dvort=False)
+    return errs(req.vel_out[ti], ev)
 
 
 # ---- reference arm ---------------------------------------------------------------
@@ -787,21 +899,20 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    from cvortex_gb300 import workloads
     os.environ.setdefault("OMP_NUM_THREADS", str(cpu_cores()))
     os.environ.setdefault("OMP_PROC_BIND", "spread")
     kind, ref = cpu_reference()
-    p = workloads.vortex_ring(args.n)
+    p = workload(args)
     order = np.random.Generator(np.random.PCG64(7)).permutation(args.n)
     # size each step's target sample so that all K steps take about a minute
-    probe = p[np.sort(order[:128])].copy()
+    probe = p[np.sort(order[:32])].copy()
     for _ in range(max(args.warmup, 1)):
         t0 = time.perf_counter()
         cpu_step(kind, ref, p, probe, args.reg)
         per_target = (time.perf_counter() - t0) / len(probe)
     budget_s = 60.0
     m = int(budget_s / max(args.steps, 1) / max(per_target, 1e-9))
-    m = max(64, min(CPU_SAMPLE_TARGETS, m, args.n))
+    m = max(32, min(CPU_SAMPLE_TARGETS, m, args.n))
     sub = p[np.sort(order[:m])].copy()
     t0 = time.perf_counter()
     for _ in range(args.steps):
@@ -814,9 +925,9 @@ def run_reference(args):
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic (seeded)",
-           "config": {"workload": f"P3D vortex ring N={args.n}, {args.reg}, sigma={SIGMA}, "
-                                  "vel + dvort, targets = sources",
-                      "interactions_per_step": float(len(sub)) * len(p),
+           "config": {"workload": workload_name(args),
+                      "interactions_per_step": float(args.n) * args.n,
+                      "sampled_interactions_per_step": float(len(sub)) * len(p),
                       "parallelism": f"{cores} host threads (OpenMP)"},
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
                             "cpu_model": cpu_model(),

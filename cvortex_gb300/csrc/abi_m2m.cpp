@@ -94,14 +94,18 @@ class GpuJob {
 	void upload(HostBuf& h, DevBuf& d, size_t bytes) {
 		if (bytes) check(cudaMemcpyAsync(d.ptr, h.ptr, bytes, cudaMemcpyHostToDevice, ctx_->stream), "H2D copy");
 	}
+	// Before the first launch: reset this path's error word and wait for
+	// every earlier user of the workspace (device-pointer calls included).
 	bool begin() {
-		return check(cudaMemsetAsync(ctx_->d_err, 0, sizeof(unsigned), ctx_->stream), "reset error word");
+		return check(cudaMemsetAsync(ctx_->d_err, 0, sizeof(unsigned), ctx_->stream), "reset error word")
+			&& check(cudaStreamWaitEvent(ctx_->stream, ctx_->ws_ev, 0), "workspace order");
 	}
 	bool ensure_out(DevBuf& d, HostBuf& h, size_t bytes) {
 		return check(d.ensure(bytes), "device allocation") && check(h.ensure(bytes), "pinned allocation");
 	}
 	// D2H of result(s) + error word, wait, check the device error word.
 	bool finish(DevBuf& d0, HostBuf& h0, size_t b0, DevBuf* d1 = nullptr, HostBuf* h1 = nullptr, size_t b1 = 0) {
+		check(cudaEventRecord(ctx_->ws_ev, ctx_->stream), "workspace order");
 		check(cudaMemcpyAsync(h0.ptr, d0.ptr, b0, cudaMemcpyDeviceToHost, ctx_->stream), "D2H copy");
 		if (d1 && b1) check(cudaMemcpyAsync(h1->ptr, d1->ptr, b1, cudaMemcpyDeviceToHost, ctx_->stream), "D2H copy");
 		check(cudaMemcpyAsync(ctx_->h_err, ctx_->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx_->stream), "D2H error word");

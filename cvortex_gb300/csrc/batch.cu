@@ -176,6 +176,7 @@ struct cvtx_gb300_batch {
 	int num_sms = 0;
 	// current plan
 	int shape = 0, chunk = 8192, n_items = 0, grid = 0;
+	size_t n_counters = 1;          // per-target-block arrival counters in use
 	size_t smem = 0;
 	DevBuf d_probs, d_items, d_partial, d_counters, d_next, d_err;
 	cudaStream_t stream = nullptr;
@@ -265,6 +266,7 @@ int plan_batch(cvtx_gb300_batch* b, int shape, int chunk) {
 	b->shape = shape;
 	b->chunk = chunk;
 	b->n_items = int(items.size());
+	b->n_counters = std::max<size_t>(counters, 1);
 	with_batch_variant(b->reg, b->ops, shape, [&](auto var) {
 		using V = decltype(var);
 		b->smem = V::kSmem;
@@ -290,11 +292,16 @@ cudaError_t enqueue(cvtx_gb300_batch* b) {
 	return cudaGetLastError();
 }
 
+// A CTA whose wait expired returns before it counts its arrival at its
+// target block, so after a reported error the arrival counters are reset
+// too: otherwise a later run could take a block's last arrival for complete
+// before every split had written its partials.
 int check_err_word(cvtx_gb300_batch* b) {
 	unsigned w = 0;
 	if (cudaMemcpy(&w, b->d_err.ptr, sizeof w, cudaMemcpyDeviceToHost) != cudaSuccess) return -2;
 	if (w) {
 		cudaMemset(b->d_err.ptr, 0, sizeof w);
+		cudaMemset(b->d_counters.ptr, 0, b->n_counters * sizeof(unsigned));
 		return fail(b, device_error_text(w), -4);
 	}
 	return 0;
@@ -327,7 +334,7 @@ CVTX_EXPORT cvtx_gb300_batch* cvtx_gb300_batch_create(const cvtx_gb300_p3d_probl
 		b->device = c->device;
 		b->num_sms = c->num_sms;
 	}
-	cudaSetDevice(b->device);
+	DeviceGuard dg(b->device);
 	cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
 	if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_in, cudaEventDisableTiming);
 	if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_out, cudaEventDisableTiming);
@@ -347,7 +354,7 @@ CVTX_EXPORT cvtx_gb300_batch* cvtx_gb300_batch_create(const cvtx_gb300_p3d_probl
 // each, after one warm run) and keep the fastest.
 CVTX_EXPORT int cvtx_gb300_batch_tune(cvtx_gb300_batch* b, int repeats) {
 	if (!b || repeats < 1) return -1;
-	cudaSetDevice(b->device);
+	DeviceGuard dg(b->device);
 	cudaEvent_t t0, t1;
 	cudaEventCreate(&t0);
 	cudaEventCreate(&t1);
@@ -379,7 +386,7 @@ CVTX_EXPORT int cvtx_gb300_batch_tune(cvtx_gb300_batch* b, int repeats) {
 // Capture the current plan into a CUDA graph; later runs replay it.
 CVTX_EXPORT int cvtx_gb300_batch_capture(cvtx_gb300_batch* b) {
 	if (!b) return -1;
-	cudaSetDevice(b->device);
+	DeviceGuard dg(b->device);
 	drop_graph(b);
 	cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
 	if (e == cudaSuccess) {
@@ -399,7 +406,7 @@ CVTX_EXPORT int cvtx_gb300_batch_capture(cvtx_gb300_batch* b) {
 // on it (the batch executes on its own stream in between).
 CVTX_EXPORT int cvtx_gb300_batch_run(cvtx_gb300_batch* b, void* stream) {
 	if (!b) return -1;
-	cudaSetDevice(b->device);
+	DeviceGuard dg(b->device);
 	cudaStream_t s = static_cast<cudaStream_t>(stream);
 	cudaError_t e = cudaEventRecord(b->ev_in, s);
 	if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, b->ev_in, 0);
@@ -420,7 +427,7 @@ CVTX_EXPORT int cvtx_gb300_batch_run(cvtx_gb300_batch* b, void* stream) {
 // Synchronise and report a device-side timeout of earlier runs.
 CVTX_EXPORT int cvtx_gb300_batch_status(cvtx_gb300_batch* b) {
 	if (!b) return -1;
-	cudaSetDevice(b->device);
+	DeviceGuard dg(b->device);
 	if (cudaStreamSynchronize(b->stream) != cudaSuccess) return -2;
 	return check_err_word(b);
 }
@@ -440,7 +447,7 @@ CVTX_EXPORT int cvtx_gb300_batch_info(const cvtx_gb300_batch* b, int* shape_tpt,
 
 CVTX_EXPORT void cvtx_gb300_batch_destroy(cvtx_gb300_batch* b) {
 	if (!b) return;
-	cudaSetDevice(b->device);
+	DeviceGuard dg(b->device);
 	if (b->stream) cudaStreamSynchronize(b->stream);
 	drop_graph(b);
 	b->d_probs.release(); b->d_items.release(); b->d_partial.release();

@@ -3,8 +3,12 @@
 // For callers whose particles already live in GPU memory (a time-stepping
 // solver, a serving loop, a framework tensor): no gather, no host copies, the
 // kernels run on the caller's stream. Split-source partial sums use the
-// active context's workspace; successive calls are ordered on the workspace
-// through an event so that calls on different streams do not overlap on it.
+// active context's workspace; every call waits on the context's workspace
+// event before its first launch and records it after its last, as the
+// host-pointer calls do on the context's own stream, so that no two calls
+// overlap on the workspace whatever streams they use. Device-side errors of
+// these calls go to their own error word (cvtx_gb300_dev_status), which the
+// host-pointer calls never reset.
 #include <string>
 
 #include "cvortex/cvtx_gb300.h"
@@ -26,7 +30,7 @@ struct DevCall {
 	int prepare(size_t ws_bytes, const char* what) {
 		if (!ctx) return -3;
 		cudaError_t e = ctx->ensure_ws(ws_bytes);
-		if (e == cudaSuccess && ws_event()) e = cudaStreamWaitEvent(stream, ws_event(), 0);
+		if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, ctx->ws_ev, 0);
 		if (e != cudaSuccess) {
 			set_error(std::string(what) + ": " + cudaGetErrorString(e));
 			return -2;
@@ -34,7 +38,7 @@ struct DevCall {
 		return 0;
 	}
 	int done(cudaError_t e, const char* what) {
-		if (e == cudaSuccess && ws_event()) e = cudaEventRecord(ws_event(), stream);
+		if (e == cudaSuccess) e = cudaEventRecord(ctx->ws_ev, stream);
 		if (e != cudaSuccess) {
 			set_error(std::string(what) + ": " + cudaGetErrorString(e));
 			return -2;
@@ -44,12 +48,8 @@ struct DevCall {
 	LaunchEnv env() const {
 		LaunchEnv v = ctx->env();
 		v.stream = stream;
+		v.err = ctx->d_err_dev;
 		return v;
-	}
-	cudaEvent_t ws_event() {
-		static cudaEvent_t ev = nullptr;
-		if (!ev && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) ev = nullptr;
-		return ev;
 	}
 };
 
@@ -244,8 +244,8 @@ CVTX_EXPORT int cvtx_gb300_dev_status(void* stream) {
 	cudaStream_t s = static_cast<cudaStream_t>(stream);
 	unsigned w = 0;
 	if (cudaStreamSynchronize(s) != cudaSuccess) return -2;
-	if (cudaMemcpy(&w, c->d_err, sizeof w, cudaMemcpyDeviceToHost) != cudaSuccess) return -2;
-	if (cudaMemset(c->d_err, 0, sizeof w) != cudaSuccess) return -2;
+	if (cudaMemcpy(&w, c->d_err_dev, sizeof w, cudaMemcpyDeviceToHost) != cudaSuccess) return -2;
+	if (cudaMemset(c->d_err_dev, 0, sizeof w) != cudaSuccess) return -2;
 	if (w) {
 		set_error(device_error_text(w));
 		return -4;

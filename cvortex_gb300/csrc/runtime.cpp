@@ -68,9 +68,15 @@ cudaError_t DeviceContext::open(int dev) {
 	if (e != cudaSuccess) return e;
 	e = cudaMalloc(reinterpret_cast<void**>(&d_err), sizeof(unsigned));
 	if (e != cudaSuccess) return e;
+	e = cudaMalloc(reinterpret_cast<void**>(&d_err_dev), sizeof(unsigned));
+	if (e != cudaSuccess) return e;
 	e = cudaMallocHost(reinterpret_cast<void**>(&h_err), sizeof(unsigned));
 	if (e != cudaSuccess) return e;
 	*h_err = 0u;
+	e = cudaEventCreateWithFlags(&ws_ev, cudaEventDisableTiming);
+	if (e != cudaSuccess) return e;
+	e = cudaMemset(d_err_dev, 0, sizeof(unsigned));
+	if (e != cudaSuccess) return e;
 	return cudaMemset(d_err, 0, sizeof(unsigned));
 }
 
@@ -82,9 +88,11 @@ void DeviceContext::close() {
 	h_redist.release();
 	h_src.release(); h_tgt.release(); h_out0.release(); h_out1.release();
 	if (d_err) cudaFree(d_err);
+	if (d_err_dev) cudaFree(d_err_dev);
 	if (h_err) cudaFreeHost(h_err);
+	if (ws_ev) cudaEventDestroy(ws_ev);
 	if (stream) cudaStreamDestroy(stream);
-	d_err = nullptr; h_err = nullptr; stream = nullptr;
+	d_err = nullptr; d_err_dev = nullptr; h_err = nullptr; ws_ev = nullptr; stream = nullptr;
 }
 
 LaunchEnv DeviceContext::env() const {

@@ -17,6 +17,23 @@
 
 namespace cvtx {
 
+// Makes `dev` current for a scope and restores the caller's current device
+// afterwards, so that entry points working on an object's own device leave
+// the calling thread's device as they found it.
+struct DeviceGuard {
+	int prev = -1;
+	explicit DeviceGuard(int dev) {
+		if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+		if (dev >= 0 && dev != prev) cudaSetDevice(dev);
+	}
+	~DeviceGuard() {
+		int cur = -1;
+		if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+	}
+	DeviceGuard(const DeviceGuard&) = delete;
+	DeviceGuard& operator=(const DeviceGuard&) = delete;
+};
+
 // Grow-only device allocation (256-byte aligned by cudaMalloc).
 struct DevBuf {
 	void* ptr = nullptr;
@@ -37,8 +54,13 @@ struct DeviceContext {
 	int device = -1;
 	int num_sms = 0;
 	cudaStream_t stream = nullptr;
-	unsigned* d_err = nullptr;      // device error word
+	unsigned* d_err = nullptr;      // device error word of the host-pointer calls
 	unsigned* h_err = nullptr;      // pinned copy
+	unsigned* d_err_dev = nullptr;  // device error word of the device-pointer calls
+	// Orders every user of `ws` (host-pointer calls on `stream`, device-pointer
+	// calls on their callers' streams): each waits on it before its first
+	// launch and records it after its last.
+	cudaEvent_t ws_ev = nullptr;
 	DevBuf src, tgt, out0, out1, ws;
 	DevBuf redist;                  // particle redistribution scratch (grow-only)
 	HostBuf h_redist;               // its cells, pinned (grow-only)

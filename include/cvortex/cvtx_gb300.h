@@ -125,7 +125,10 @@ CVTX_EXPORT int cvtx_gb300_dev_F3D_M2M_dvort(const void* fil, int n_fil,
  * 233,016 targets per call (more: returns -1 with a message), any number of
  * sources. Calls that overlap on the GPU share that scratch and race. The
  * first call on a device resolves the scratch address and should precede any
- * stream capture. A device-side wait expiry turns the outputs into NaN. */
+ * stream capture. The resolved address is kept for the life of the process:
+ * do not call this entry point again on a device after cudaDeviceReset on
+ * it (the old address may by then belong to another allocation). A
+ * device-side wait expiry turns the outputs into NaN. */
 CVTX_EXPORT int cvtx_gb300_dev_P3D_M2M_noalloc(const void* src, int n_src,
 	const void* tgt, int tgt_stride, int n_tgt, float* vel_out,
 	float* dvort_out, int reg, float regularisation_radius, void* stream);

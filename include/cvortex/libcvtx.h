@@ -9,6 +9,9 @@
  * Python ctypes) link against libcvortex.so unchanged. Line numbers after
  * each group cite that reference header.
  *
+ * The declarations follow the cvortex header, Copyright (c) 2019 HJA Bird,
+ * distributed under the MIT licence.
+ *
  * Hot path served by CUDA kernels for sm_103a when an accelerator is enabled:
  *   cvtx_P3D_M2M_vel / _dvort / _visc_dvort / _vort
  *   cvtx_P2D_M2M_vel / _visc_dvort

@@ -14,7 +14,8 @@ Three checkers for the GB300 library, none of which the product imports:
 * ``oracle.exact``: the same formulas in float64 with the exact error
   function, i.e. the "error vs FP64" reference (independent of the reference
   implementation and of FP32 rounding); ``exact_p3d_vel_dvort`` is the same
-  in compiled C for large samples.
+  in compiled C for large samples, as are the ``exact_*`` functions of this
+  module for the other ops.
 * ``oracle.redist``: a numpy restatement of the reference's particle
   redistribution, pinned to the reference library's outputs (golden
   fixture ``tests/golden/redist.npz``; see that module).
@@ -32,7 +33,9 @@ HERE = Path(__file__).resolve().parent
 REPO = HERE.parent
 LIB = HERE / "lib" / "libcvtx_oracle.so"
 REF_LIB = HERE / "_ref" / "libcvtx_ref.so"
-REFERENCE_ROOT = Path(os.environ.get("CVTX_REFERENCE_ROOT", "/root/reference"))
+# The reference checkout: $CVTX_REFERENCE_ROOT, else a directory named
+# "reference" beside this repository's root; absent on hosts without it.
+REFERENCE_ROOT = Path(os.environ.get("CVTX_REFERENCE_ROOT") or (REPO.parent / "reference"))
 
 
 def build(force: bool = False) -> Path:
@@ -69,6 +72,14 @@ _SIGS = {
     "oracle_F3D_inf_mtrx": (None, [_vp, _i, _vp, _vp, _i, _vp]),
     "oracle_num_threads": (_i, []),
     "oracle_exact_P3D_vel_dvort": (None, [_vp, _vp, _i, _vp, _vp, _i, _i, C.c_double, _vp, _vp]),
+    "oracle_exact_P3D_visc": (None, [_vp, _vp, _vp, _i, _vp, _vp, _vp, _i, _i, C.c_double,
+                                     C.c_double, _vp]),
+    "oracle_exact_P3D_vort": (None, [_vp, _vp, _i, _vp, _i, _i, C.c_double, _vp]),
+    "oracle_exact_P2D_vel": (None, [_vp, _vp, _i, _vp, _i, _i, C.c_double, _vp]),
+    "oracle_exact_P2D_visc": (None, [_vp, _vp, _vp, _i, _vp, _vp, _vp, _i, _i, C.c_double,
+                                     C.c_double, _vp]),
+    "oracle_exact_F3D_vel": (None, [_vp, _vp, _vp, _i, _vp, _vp, _i, _vp]),
+    "oracle_exact_F3D_dvort": (None, [_vp, _vp, _vp, _i, _vp, _vp, _i, _vp]),
 }
 
 _lib = None
@@ -191,6 +202,70 @@ def exact_p3d_vel_dvort(src, tgt_xyz, tgt_alpha, reg, sigma, want_vel=True, want
                                      None if vel is None else _a(vel),
                                      None if dv is None else _a(dv))
     return vel, dv
+
+
+def _d(x):
+    return np.ascontiguousarray(x, np.float64)
+
+
+def exact_p3d_visc(src, tgt, reg, sigma, nu):
+    """FP64 exact-math P3D viscous exchange at the particles `tgt`."""
+    sx, sa, sv = _d(src["coord"]), _d(src["vorticity"]), _d(src["volume"])
+    tx, ta, tv = _d(tgt["coord"]), _d(tgt["vorticity"]), _d(tgt["volume"])
+    out = np.zeros((len(tgt), 3))
+    lib().oracle_exact_P3D_visc(_a(sx), _a(sa), _a(sv), len(src), _a(tx), _a(ta), _a(tv),
+                                len(tgt), REG[reg], float(sigma), float(nu), _a(out))
+    return out
+
+
+def exact_p3d_vort(src, mes, reg, sigma):
+    """FP64 exact-math P3D vorticity field (5 sigma box) at points `mes`."""
+    sx, sa, tx = _d(src["coord"]), _d(src["vorticity"]), _d(mes)
+    out = np.zeros((tx.shape[0], 3))
+    lib().oracle_exact_P3D_vort(_a(sx), _a(sa), len(src), _a(tx), tx.shape[0], REG[reg],
+                                float(sigma), _a(out))
+    return out
+
+
+def exact_p2d_vel(src, mes, reg, sigma):
+    """FP64 exact-math P2D velocity at points `mes` (M, 2)."""
+    sx, sg, tx = _d(src["coord"]), _d(src["vorticity"]), _d(mes)
+    out = np.zeros((tx.shape[0], 2))
+    lib().oracle_exact_P2D_vel(_a(sx), _a(sg), len(src), _a(tx), tx.shape[0], REG[reg],
+                               float(sigma), _a(out))
+    return out
+
+
+def exact_p2d_visc(src, tgt, reg, sigma, nu):
+    """FP64 exact-math P2D viscous exchange at the particles `tgt`."""
+    sx, sg, sa = _d(src["coord"]), _d(src["vorticity"]), _d(src["area"])
+    tx, tg, ta = _d(tgt["coord"]), _d(tgt["vorticity"]), _d(tgt["area"])
+    out = np.zeros(len(tgt))
+    lib().oracle_exact_P2D_visc(_a(sx), _a(sg), _a(sa), len(src), _a(tx), _a(tg), _a(ta),
+                                len(tgt), REG[reg], float(sigma), float(nu), _a(out))
+    return out
+
+
+def exact_f3d_vel(fil, mes, dirs=None):
+    """FP64 exact-math F3D velocity at points `mes`; with `dirs`, the
+    influence matrix (rows: points, columns: filaments)."""
+    fa, fb, fg, tx = _d(fil["start"]), _d(fil["end"]), _d(fil["strength"]), _d(mes)
+    m = tx.shape[0]
+    dd = None if dirs is None else _d(dirs)
+    out = np.zeros((m, len(fil)) if dirs is not None else (m, 3))
+    lib().oracle_exact_F3D_vel(_a(fa), _a(fb), _a(fg), len(fil), _a(tx),
+                               None if dd is None else _a(dd), m, _a(out))
+    return out
+
+
+def exact_f3d_dvort(fil, ind):
+    """FP64 exact-math F3D vortex stretching of the particles `ind`."""
+    fa, fb, fg = _d(fil["start"]), _d(fil["end"]), _d(fil["strength"])
+    tx, ta = _d(ind["coord"]), _d(ind["vorticity"])
+    out = np.zeros((len(ind), 3))
+    lib().oracle_exact_F3D_dvort(_a(fa), _a(fb), _a(fg), len(fil), _a(tx), _a(ta), len(ind),
+                                 _a(out))
+    return out
 
 
 def regfunc(reg: str, which: str, rho: float) -> float:

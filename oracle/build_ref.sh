@@ -22,11 +22,13 @@
 # _MSC_VER except accelerators.cpp (a compiler name string), which keeps the
 # default flags.
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]
+#   REFERENCE_ROOT defaults to $CVTX_REFERENCE_ROOT, else to a directory named
+#   "reference" beside this repository.
 set -euo pipefail
 here="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 repo="$(cd "$here/.." && pwd)"
-ref="${1:-/root/reference}"
+ref="${1:-${CVTX_REFERENCE_ROOT:-$(cd "$repo/.." && pwd)/reference}}"
 out="$here/_ref"
 if [ ! -d "$ref/src" ]; then
   echo "build_ref: reference sources not found at $ref; skipping" >&2

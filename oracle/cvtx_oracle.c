@@ -538,3 +538,231 @@ void oracle_exact_P3D_vel_dvort(const double* sx, const double* sa, int n_src,
 		if (dvort) for (int k = 0; k < 3; ++k) dvort[3 * i + k] = w[k] / (4 * pi * sigma * sigma * sigma);
 	}
 }
+
+/* ---- FP64 exact-math evaluation of the other ops (same formulas as
+ * oracle/exact.py, in double precision). Inputs are double arrays: xyz
+ * triples (or xy pairs) and per-particle scalars; OpenMP over targets.
+ * Coincident pairs contribute zero, as in the reference. */
+
+/* eta_3D(rho) (reference src/VortFunc.cpp:101-108, 178-182): Winckelmans
+ * 52.5 (1 + rho^2)^-4.5, Gaussian sqrt(2/pi) exp(-rho^2/2); 0 otherwise. */
+static double ex_eta3(int reg, double rho) {
+	const double x = rho * rho;
+	if (reg == 1) return 52.5 * pow(x + 1.0, -4.5);
+	if (reg == 3) return 0.79788456080286535588 * exp(-0.5 * x);
+	return 0.0;
+}
+
+/* zeta_3D(rho) (reference src/VortFunc.cpp:92-99, 138-141, 178-182). */
+static double ex_zeta3(int reg, double rho) {
+	const double x = rho * rho;
+	switch (reg) {
+	case 1: return 7.5 * pow(x + 1.0, -3.5);
+	case 2: return rho < 1.0 ? 3.0 : 0.0;
+	case 3: return 0.79788456080286535588 * exp(-0.5 * x);
+	default: return 0.0;
+	}
+}
+
+/* g_2D(rho) / r^2 (reference src/VortFunc.cpp:78-80, 117-122, 150-153,
+ * 191-194), the Gaussian through expm1 (no cancellation at small rho). */
+static double ex_g2_over_r2(int reg, double r2, double sigma) {
+	const double s2 = sigma * sigma, x = r2 / s2;
+	switch (reg) {
+	case 0: return 1.0 / r2;
+	case 1: return (x + 2.0) / ((x + 1.0) * (x + 1.0) * s2);
+	case 2: return x < 1.0 ? 1.0 / s2 : 1.0 / r2;
+	default: return -expm1(-0.5 * x) / r2;
+	}
+}
+
+/* eta_2D(rho) (reference src/VortFunc.cpp:124-131, 196-199), including the
+ * reference's Winckelmans form 24 exp(4/a^3)/a^4, a = 1 + rho^2. */
+static double ex_eta2(int reg, double rho) {
+	const double x = rho * rho;
+	if (reg == 1) { const double a = x + 1.0; return 24.0 * exp(4.0 / (a * a * a)) / (a * a * a * a); }
+	if (reg == 3) return exp(-0.5 * x);
+	return 0.0;
+}
+
+/* P3D viscous exchange (reference src/P3D.cpp:116-144):
+ * (2 nu / sigma^2) sum_s (alpha_s V_t - alpha_t V_s) eta(rho). */
+void oracle_exact_P3D_visc(const double* sx, const double* sa, const double* sv, int n_src,
+	const double* tx, const double* ta, const double* tv, int n_tgt, int reg, double sigma,
+	double nu, double* out)
+{
+	const double as = fabs(sigma);
+	long i;
+#pragma omp parallel for schedule(dynamic, 16)
+	for (i = 0; i < n_tgt; ++i) {
+		double w[3] = {0, 0, 0}, vsum = 0.0;
+		const double* t = tx + 3 * i;
+		for (long j = 0; j < n_src; ++j) {
+			const double* s = sx + 3 * j;
+			const double d[3] = {s[0] - t[0], s[1] - t[1], s[2] - t[2]};
+			const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+			if (r2 == 0.0) continue;
+			const double e = ex_eta3(reg, sqrt(r2) / as);
+			for (int k = 0; k < 3; ++k) w[k] += e * sa[3 * j + k];
+			vsum += e * sv[j];
+		}
+		for (int k = 0; k < 3; ++k)
+			out[3 * i + k] = (w[k] * tv[i] - ta[3 * i + k] * vsum) * (2.0 * nu / (sigma * sigma));
+	}
+}
+
+/* P3D vorticity field with the CPU path's 5 sigma box (reference
+ * src/P3D.cpp:298-322): sum_s alpha_s zeta(rho) / (4 pi sigma^3) over
+ * sources with every |d_k| < 5 sigma. */
+void oracle_exact_P3D_vort(const double* sx, const double* sa, int n_src,
+	const double* tx, int n_tgt, int reg, double sigma, double* out)
+{
+	const double pi = 3.14159265358979323846;
+	const double cut = 5.0 * sigma;
+	long i;
+#pragma omp parallel for schedule(dynamic, 16)
+	for (i = 0; i < n_tgt; ++i) {
+		double w[3] = {0, 0, 0};
+		const double* t = tx + 3 * i;
+		for (long j = 0; j < n_src; ++j) {
+			const double* s = sx + 3 * j;
+			const double d[3] = {s[0] - t[0], s[1] - t[1], s[2] - t[2]};
+			if (!(fabs(d[0]) < cut && fabs(d[1]) < cut && fabs(d[2]) < cut)) continue;
+			const double z = ex_zeta3(reg, sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) / sigma);
+			for (int k = 0; k < 3; ++k) w[k] += z * sa[3 * j + k];
+		}
+		for (int k = 0; k < 3; ++k) out[3 * i + k] = w[k] / (4.0 * pi * sigma * sigma * sigma);
+	}
+}
+
+/* P2D velocity (reference src/P2D.cpp:49-69):
+ * (1/2pi) sum_s Gamma_s g(rho)/r^2 (dy, -dx), d = x_t - x_s. */
+void oracle_exact_P2D_vel(const double* sx, const double* sg, int n_src,
+	const double* tx, int n_tgt, int reg, double sigma, double* out)
+{
+	const double pi = 3.14159265358979323846;
+	const double as = fabs(sigma);
+	long i;
+#pragma omp parallel for schedule(dynamic, 16)
+	for (i = 0; i < n_tgt; ++i) {
+		double u = 0.0, v = 0.0;
+		for (long j = 0; j < n_src; ++j) {
+			const double dx = tx[2 * i] - sx[2 * j], dy = tx[2 * i + 1] - sx[2 * j + 1];
+			const double r2 = dx * dx + dy * dy;
+			if (r2 == 0.0) continue;
+			const double h = sg[j] * ex_g2_over_r2(reg, r2, as);
+			u += h * dy;
+			v -= h * dx;
+		}
+		out[2 * i] = u / (2.0 * pi);
+		out[2 * i + 1] = v / (2.0 * pi);
+	}
+}
+
+/* P2D viscous exchange (reference src/P2D.cpp:167-194):
+ * (2 nu / sigma^2) sum_s (Gamma_s A_t - Gamma_t A_s) eta(rho). */
+void oracle_exact_P2D_visc(const double* sx, const double* sg, const double* sa, int n_src,
+	const double* tx, const double* tg, const double* ta, int n_tgt, int reg, double sigma,
+	double nu, double* out)
+{
+	const double as = fabs(sigma);
+	long i;
+#pragma omp parallel for schedule(dynamic, 16)
+	for (i = 0; i < n_tgt; ++i) {
+		double gs = 0.0, ar = 0.0;
+		for (long j = 0; j < n_src; ++j) {
+			const double dx = sx[2 * j] - tx[2 * i], dy = sx[2 * j + 1] - tx[2 * i + 1];
+			const double r2 = dx * dx + dy * dy;
+			if (r2 == 0.0) continue;
+			const double e = ex_eta2(reg, sqrt(r2) / as);
+			gs += e * sg[j];
+			ar += e * sa[j];
+		}
+		out[i] = (gs * ta[i] - tg[i] * ar) * (2.0 * nu / (sigma * sigma));
+	}
+}
+
+/* F3D velocity (reference src/F3D.cpp:34-54): straight-segment Biot-Savart,
+ * non-finite terms dropped. */
+static void ex_f3d_vel_pair(const double* a, const double* b, double g, const double* m,
+	double* v)
+{
+	const double pi = 3.14159265358979323846;
+	double r1[3], r2[3], r0[3];
+	for (int k = 0; k < 3; ++k) { r1[k] = m[k] - a[k]; r2[k] = m[k] - b[k]; r0[k] = r1[k] - r2[k]; }
+	const double c[3] = {r1[1] * r2[2] - r1[2] * r2[1], r1[2] * r2[0] - r1[0] * r2[2],
+		r1[0] * r2[1] - r1[1] * r2[0]};
+	const double cc = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
+	const double l1 = sqrt(r1[0] * r1[0] + r1[1] * r1[1] + r1[2] * r1[2]);
+	const double l2 = sqrt(r2[0] * r2[0] + r2[1] * r2[1] + r2[2] * r2[2]);
+	const double t2 = (r1[0] * r0[0] + r1[1] * r0[1] + r1[2] * r0[2]) / l1
+		- (r2[0] * r0[0] + r2[1] * r0[1] + r2[2] * r0[2]) / l2;
+	const double f = g / (4.0 * pi * cc) * t2;
+	for (int k = 0; k < 3; ++k) v[k] = isfinite(f) ? f * c[k] : 0.0;
+}
+
+/* fa, fb: filament start and end xyz; fg: strengths; dirs (optional): when
+ * given, out[i * n_fil + j] = dot(vel of filament j at point i, dirs[i])
+ * (the influence matrix, reference src/F3D.cpp:204-227), else out holds
+ * the summed velocity per point. */
+void oracle_exact_F3D_vel(const double* fa, const double* fb, const double* fg, int n_fil,
+	const double* tx, const double* dirs, int n_tgt, double* out)
+{
+	long i;
+#pragma omp parallel for schedule(dynamic, 16)
+	for (i = 0; i < n_tgt; ++i) {
+		double u[3] = {0, 0, 0};
+		for (long j = 0; j < n_fil; ++j) {
+			double v[3];
+			ex_f3d_vel_pair(fa + 3 * j, fb + 3 * j, fg[j], tx + 3 * i, v);
+			if (dirs) {
+				const double* dd = dirs + 3 * i;
+				out[i * (long)n_fil + j] = v[0] * dd[0] + v[1] * dd[1] + v[2] * dd[2];
+			} else {
+				for (int k = 0; k < 3; ++k) u[k] += v[k];
+			}
+		}
+		if (!dirs) for (int k = 0; k < 3; ++k) out[3 * i + k] = u[k];
+	}
+}
+
+/* F3D vortex stretching (reference src/F3D.cpp:56-85): B alpha + A x alpha
+ * with A = -(gamma/4pi) r0 / |r1 x r0|^2 (r0.r1/|r1| - r0.r2/|r2|) and
+ * B = (3/|r0|)(gamma/4pi) |r0 x r1| (1/|r1| - 1/|r2|); non-finite terms
+ * dropped. */
+void oracle_exact_F3D_dvort(const double* fa, const double* fb, const double* fg, int n_fil,
+	const double* tx, const double* ta, int n_tgt, double* out)
+{
+	const double pi = 3.14159265358979323846;
+	long i;
+#pragma omp parallel for schedule(dynamic, 16)
+	for (i = 0; i < n_tgt; ++i) {
+		double u[3] = {0, 0, 0};
+		const double* p = tx + 3 * i;
+		const double* w = ta + 3 * i;
+		for (long j = 0; j < n_fil; ++j) {
+			const double* a = fa + 3 * j;
+			const double* b = fb + 3 * j;
+			double r1[3], r2[3], r0[3];
+			for (int k = 0; k < 3; ++k) { r1[k] = p[k] - a[k]; r2[k] = p[k] - b[k]; r0[k] = r1[k] - r2[k]; }
+			const double X[3] = {r1[1] * r0[2] - r1[2] * r0[1], r1[2] * r0[0] - r1[0] * r0[2],
+				r1[0] * r0[1] - r1[1] * r0[0]};
+			const double X2 = X[0] * X[0] + X[1] * X[1] + X[2] * X[2];
+			const double l1 = sqrt(r1[0] * r1[0] + r1[1] * r1[1] + r1[2] * r1[2]);
+			const double l2 = sqrt(r2[0] * r2[0] + r2[1] * r2[1] + r2[2] * r2[2]);
+			const double l0 = sqrt(r0[0] * r0[0] + r0[1] * r0[1] + r0[2] * r0[2]);
+			const double t1 = fg[j] / (4.0 * pi);
+			const double t212 = (r0[0] * r1[0] + r0[1] * r1[1] + r0[2] * r1[2]) / l1
+				- (r0[0] * r2[0] + r0[1] * r2[1] + r0[2] * r2[2]) / l2;
+			const double t222 = sqrt(X2) / l1 - sqrt(X2) / l2;
+			const double kA = -t1 * t212 / X2;
+			const double A[3] = {r0[0] * kA, r0[1] * kA, r0[2] * kA};
+			const double B = 3.0 / l0 * t1 * t222;
+			const double v[3] = {w[0] * B + A[1] * w[2] - A[2] * w[1],
+				w[1] * B + A[2] * w[0] - A[0] * w[2], w[2] * B + A[0] * w[1] - A[1] * w[0]};
+			if (isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))
+				for (int k = 0; k < 3; ++k) u[k] += v[k];
+		}
+		for (int k = 0; k < 3; ++k) out[3 * i + k] = u[k];
+	}
+}

@@ -11,9 +11,12 @@ reference's OpenMP path) and stores inputs and outputs as compressed .npz:
                      vortex ring (600 particles, sigma 0.05)
 * p2d_patch.npz    -- P2D vel and visc_dvort for the four regularisations
 * f3d_sheet.npz    -- F3D vel, dvort and influence matrix on a wake sheet
-* reftest_many.npz -- the inputs of the reference's own CPU/GPU comparison
-                     test (reference test/testsamecpugpuresultmany.h:67-89,
-                     LCG of test/testmain.c:87-92) with its outputs
+* reftest.npz      -- the reference's own CPU/GPU comparison tests
+                     (reference test/testsamecpugpuresultsingle.h,
+                     test/testsamecpugpuresultmany.h): the CPU result of every
+                     section of all 10 repeats of both; the inputs come from
+                     their LCG (tests/reftest_inputs.py), the first repeat's
+                     are stored to pin it
 * kat.npz          -- g, zeta, eta (3D and 2D) of every regularisation on a
                      grid of rho, from the reference's function pointers
 * relax.npz        -- cvtx_P3D_pedrizzetti_relaxation of a vortex ring for
@@ -86,34 +89,20 @@ def f3d_case(ref):
     np.savez_compressed(OUT / "f3d_sheet.npz", **d)
 
 
-def reftest_inputs(n=1000):
-    """Inputs of the reference's first comparison repeat: LCG x*214013+2531011
-    seeded 0xF0F0F0F0 (test/testmain.c:87-92), values (float)mrand() /
-    (float)(RAND_MAX / 10) with glibc RAND_MAX = 2^31-1 (integer division)."""
-    state = [0xF0F0F0F0]
-
-    def mrand():
-        state[0] = (state[0] * 214013 + 2531011) & 0xFFFFFFFF
-        s = state[0] - (1 << 32) if state[0] & 0x80000000 else state[0]
-        return ((s >> 16) & 0x7FFF) % 2147483647
-
-    div10 = np.float32(2147483647 // 10)
-    div001 = np.float32(int(2147483647 / 0.01))
-    p = np.zeros(n, abi.P3D_DTYPE)
-    for i in range(n):
-        p["coord"][i] = [np.float32(mrand()) / div10 for _ in range(3)]
-        p["vorticity"][i] = [np.float32(mrand()) / div10 for _ in range(3)]
-        p["volume"][i] = np.float32(mrand()) / div001
-    return p
-
-
 def reftest_case(ref):
-    p = reftest_inputs()
-    d = {"particles": p, "sigma": np.float32(0.3)}
-    for reg in ("singular", "winckelmans", "planetary"):
-        d[f"vel_{reg}"] = ref.p3d_vel(p, p["coord"], reg, 0.3)
-        d[f"dvort_{reg}"] = ref.p3d_dvort(p, p, reg, 0.3, same=True)
-    np.savez_compressed(OUT / "reftest_many.npz", **d)
+    """The reference's own CPU-vs-GPU comparison tests, every section of all
+    10 repeats of both (tests/reftest_inputs.py regenerates their inputs bit
+    for bit from the test program's LCG), computed by the reference's CPU
+    path. Key: <test>_r<repeat>_<section>."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import reftest_inputs as rt
+    d = {"sigma": np.float32(rt.SIGMA), "nu": np.float32(rt.NU)}
+    for test, k, a in rt.all_inputs():
+        if k == 0:
+            d[f"{test}_r0_p3"], d[f"{test}_r0_fil"], d[f"{test}_r0_p2"] = a["p3"], a["fil"], a["p2"]
+        for key, op, reg in rt.SECTIONS:
+            d[f"{test}_r{k}_{key}"] = rt.run_section(ref, op, reg, a)
+    np.savez_compressed(OUT / "reftest.npz", **d)
 
 
 def kat_case(ref):

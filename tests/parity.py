@@ -18,6 +18,8 @@ TOL = 1e-5
 
 def min_rho(src_xyz, tgt_xyz, sigma):
     """Smallest nonzero separation / |sigma| from each target to the sources."""
+    if len(src_xyz) > 50_000:
+        return min_rho_tree(src_xyz, tgt_xyz, sigma)
     s = np.asarray(src_xyz, np.float64)
     out = np.empty(len(tgt_xyz))
     for i, t in enumerate(np.asarray(tgt_xyz, np.float64)):
@@ -25,6 +27,17 @@ def min_rho(src_xyz, tgt_xyz, sigma):
         r2 = r2[r2 > 0]
         out[i] = np.sqrt(r2.min()) / abs(sigma) if len(r2) else np.inf
     return out
+
+
+def min_rho_tree(src_xyz, tgt_xyz, sigma, k=8):
+    """min_rho through a k-d tree (large source sets): the nearest of the k
+    nearest sources at a nonzero distance."""
+    from scipy.spatial import cKDTree
+    s = np.asarray(src_xyz, np.float64)
+    t = np.asarray(tgt_xyz, np.float64)
+    d, _ = cKDTree(s).query(t, k=min(k, len(s)))
+    d = np.where(d > 0, d, np.inf)
+    return d.min(axis=1) / abs(sigma)
 
 
 def check(got, want, reg=None, tgt_xyz=None, src_xyz=None, sigma=None, fp64=None, tol=TOL,

@@ -75,14 +75,6 @@ def test_p3d_fused_equals_separate(gpu, reg):
     assert exact.rel_l2(dv, gpu.p3d_dvort(p, p, reg, s, same=True)) <= 1e-6
 
 
-@pytest.mark.parametrize("reg", ["singular", "winckelmans", "planetary"])
-def test_reference_test_inputs(gpu, reg):
-    g = golden("reftest_many")
-    p, s = g["particles"], float(g["sigma"])
-    check(gpu.p3d_vel(p, p["coord"], reg, s), g[f"vel_{reg}"], reg)
-    check(gpu.p3d_dvort(p, p, reg, s, same=True), g[f"dvort_{reg}"], reg)
-
-
 @pytest.mark.parametrize("reg", REGS)
 def test_p2d_golden(gpu, reg):
     g = golden("p2d_patch")
@@ -132,12 +124,13 @@ def test_p3d_uniform_cube_full_workload(gpu):
 @pytest.mark.parametrize("reg", REGS)
 def test_ring_100k_sampled_targets(gpu, reg):
     """Full-size ring (100,000 particles, sigma 0.05): every target computed on
-    the GPU; parity checked on 384 sampled targets against the oracle over all
-    sources; linearity in vorticity checked on every target."""
+    the GPU; parity checked on 2,048 sampled targets against the oracle over
+    all sources (every thread slot and packed lane of the 512-target CTAs is
+    hit several times); linearity in vorticity checked on every target."""
     p = workloads.vortex_ring(100_000)
     s = 0.05
     vel, dv = gpu.p3d_vel_dvort(p, reg, s)
-    idx = np.random.Generator(np.random.PCG64(5)).choice(len(p), 384, replace=False)
+    idx = np.sort(np.random.Generator(np.random.PCG64(5)).choice(len(p), 2048, replace=False))
     sub = p[idx].copy()
     check(vel[idx], oracle.p3d_vel(p, sub["coord"], reg, s), reg, sub["coord"], p["coord"], s)
     check(dv[idx], oracle.p3d_dvort(p, sub, reg, s), reg, sub["coord"], p["coord"], s)

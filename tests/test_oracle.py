@@ -61,13 +61,55 @@ def test_oracle_f3d_golden(built):
     _same(oracle.f3d_inf_mtrx(f[:200], g["mes"][:40], g["dirs"]), g["inf"], TOL)
 
 
-@pytest.mark.parametrize("reg", ["singular", "winckelmans", "planetary"])
-def test_oracle_reference_test_inputs(built, reg):
-    """The reference's own comparison-test inputs (LCG, sigma 0.3)."""
-    g = golden("reftest_many")
-    p, s = g["particles"], float(g["sigma"])
-    _same(oracle.p3d_vel(p, p["coord"], reg, s), g[f"vel_{reg}"], TOL)
-    _same(oracle.p3d_dvort(p, p, reg, s), g[f"dvort_{reg}"], TOL)
+def test_reference_comparison_inputs_regenerate():
+    """The LCG restatement reproduces the stored first-repeat inputs of both
+    reference comparison tests bit for bit."""
+    import reftest_inputs as rt
+    g = golden("reftest")
+    ins = {(t, k): a for t, k, a in rt.all_inputs()}
+    for test in ("single", "many"):
+        a = ins[(test, 0)]
+        for name in ("p3", "fil", "p2"):
+            assert a[name].tobytes() == g[f"{test}_r0_{name}"].tobytes(), (test, name)
+
+
+def test_oracle_reference_comparison_sections(built):
+    """Every section of all 10 repeats of the reference's two comparison
+    tests: the oracle against the reference library's CPU result, per
+    element (bit for bit on x86-64 except P2D viscous, whose reference sum is
+    an OpenMP reduction)."""
+    import reftest_inputs as rt
+
+    class _Oracle:
+        p3d_vel = staticmethod(lambda s, m, r, sg: oracle.p3d_vel(s, m, r, sg))
+        p3d_dvort = staticmethod(lambda s, t, r, sg, same=False: oracle.p3d_dvort(s, t, r, sg))
+        p3d_visc = staticmethod(lambda s, t, r, sg, nu, same=False: oracle.p3d_visc(s, t, r, sg, nu))
+        f3d_vel = staticmethod(oracle.f3d_vel)
+        f3d_dvort = staticmethod(oracle.f3d_dvort)
+        p2d_vel = staticmethod(lambda s, m, r, sg: oracle.p2d_vel(s, m, r, sg))
+        p2d_visc = staticmethod(lambda s, t, r, sg, nu, same=False: oracle.p2d_visc(s, t, r, sg, nu))
+
+    g = golden("reftest")
+    for test, k, a in rt.all_inputs():
+        for key, op, reg in rt.SECTIONS:
+            want = g[f"{test}_r{k}_{key}"]
+            got = rt.run_section(_Oracle, op, reg, a)
+            if TOL == 0 and op != "p2d_visc":
+                np.testing.assert_array_equal(got, want, err_msg=f"{test} r{k} {key}")
+            else:
+                e = rt.per_element_rel(got, want)
+                assert np.nanmax(e, initial=0.0) <= rt.REL_ACC, (test, k, key)
+
+
+def test_host_path_reference_comparison_sections(host):
+    """The same sections through this library's host path (no accelerator
+    enabled), per element against the reference's CPU result."""
+    import reftest_inputs as rt
+    g = golden("reftest")
+    for test, k, a in rt.all_inputs()[::3]:
+        for key, op, reg in rt.SECTIONS:
+            e = rt.per_element_rel(rt.run_section(host, op, reg, a), g[f"{test}_r{k}_{key}"])
+            assert np.nanmax(e, initial=0.0) <= rt.REL_ACC, (test, k, key, np.nanmax(e))
 
 
 def test_oracle_vs_reference_library(built):
@@ -120,3 +162,33 @@ def test_exact_p2d_f3d_close_to_reference(built):
     f = golden("f3d_sheet")
     assert exact.rel_l2(f["vel"], exact.f3d_vel(f["filaments"], f["mes"])) < 5e-6
     assert exact.rel_l2(f["dvort"], exact.f3d_dvort(f["filaments"], f["particles"])) < 5e-6
+
+
+def test_compiled_exact_matches_numpy_exact(built):
+    """The compiled FP64 oracle (the benchmark's error reports) against the
+    numpy FP64 oracle, op by op; the vorticity field against the reference's
+    formulation on its golden fixture."""
+    g = golden("p3d_cube")
+    p, mes, s, nu = g["particles"], g["mes"], float(g["sigma"]), float(g["nu"])
+    for reg in REGS:
+        np.testing.assert_allclose(oracle.exact_p3d_visc(p, p, reg, s, nu),
+                                   exact.p3d_visc(p, p, reg, s, nu), rtol=1e-11, atol=1e-14)
+        vort = oracle.exact_p3d_vort(p, mes, reg, s)
+        if reg == "singular":
+            assert not np.any(vort)
+        else:
+            assert exact.rel_l2(g[f"vort_{reg}"], vort) < 5e-6
+    q = golden("p2d_patch")["particles"]
+    for reg in REGS:
+        np.testing.assert_allclose(oracle.exact_p2d_vel(q, q["coord"], reg, 0.05),
+                                   exact.p2d_vel(q, q["coord"], reg, 0.05), rtol=1e-11, atol=1e-12)
+        np.testing.assert_allclose(oracle.exact_p2d_visc(q, q, reg, 0.05, 1e-3),
+                                   exact.p2d_visc(q, q, reg, 0.05, 1e-3), rtol=1e-11, atol=1e-14)
+    f = golden("f3d_sheet")
+    fil = f["filaments"]
+    np.testing.assert_allclose(oracle.exact_f3d_vel(fil, f["mes"]), exact.f3d_vel(fil, f["mes"]),
+                               rtol=1e-10, atol=1e-10)
+    np.testing.assert_allclose(oracle.exact_f3d_dvort(fil, f["particles"]),
+                               exact.f3d_dvort(fil, f["particles"]), rtol=1e-10, atol=1e-10)
+    inf = oracle.exact_f3d_vel(fil[:200], f["mes"][:40], f["dirs"])
+    assert exact.rel_l2(f["inf"], inf) < 5e-6
