@@ -342,3 +342,33 @@ def test_dev_inf_mtrx_matches_abi(gpu):
                                                257, out.data_ptr(), stream) == 0
     assert gpu.lib.cvtx_gb300_dev_status(stream) == 0
     np.testing.assert_array_equal(out.cpu().numpy(), ref)
+
+
+def test_device_call_then_abi_call_share_workspace(gpu):
+    """A device-pointer call still running on a side stream, followed at once
+    by a host-pointer ABI call: both use the context's split-sum workspace,
+    so the second must wait for the first; both results match the oracle and
+    each path's error word stays clean."""
+    import torch
+    p = workloads.uniform_cube(400_000, seed=61)
+    rec = np.zeros((len(p), 8), np.float32)
+    rec[:, 0:3], rec[:, 3], rec[:, 4:7] = p["coord"], p["volume"], p["vorticity"]
+    drec = torch.from_numpy(rec).cuda()
+    m = 6000                                   # split path: partials in the workspace
+    vel = torch.empty((m, 3), dtype=torch.float32, device="cuda")
+    dv = torch.empty((m, 3), dtype=torch.float32, device="cuda")
+    side = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    assert gpu.lib.cvtx_gb300_dev_P3D_M2M(drec.data_ptr(), len(p), drec.data_ptr(), 2, m,
+                                          vel.data_ptr(), dv.data_ptr(), 1, 0.05,
+                                          C.c_void_p(side.cuda_stream)) == 0
+    q = workloads.vortex_ring(5000, seed=62)
+    hv = gpu.p3d_vel(q, q["coord"], "winckelmans", 0.05)
+    hd = gpu.p3d_dvort(q, q, "winckelmans", 0.05, same=True)
+    assert gpu.lib.cvtx_gb300_dev_status(C.c_void_p(side.cuda_stream)) == 0
+    check(hv, oracle.p3d_vel(q, q["coord"], "winckelmans", 0.05))
+    check(hd, oracle.p3d_dvort(q, q, "winckelmans", 0.05))
+    idx = np.arange(0, m, 7)
+    sub = p[idx].copy()
+    check(vel.cpu().numpy()[idx], oracle.p3d_vel(p, sub["coord"], "winckelmans", 0.05))
+    check(dv.cpu().numpy()[idx], oracle.p3d_dvort(p, sub, "winckelmans", 0.05))
