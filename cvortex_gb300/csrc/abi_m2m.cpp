@@ -31,6 +31,9 @@ namespace cvtx {
 namespace {
 
 constexpr int kParallelGather = 32768;
+// Velocity calls with at least this many points compare the points with the
+// sources' coordinates (self-interaction form below that is not used).
+constexpr int kSelfCheckMin = 32768;
 
 void gather_p3d_host(const cvtx_P3D* const* src, int n, float4* out) {
 #pragma omp parallel for schedule(static) if (n >= kParallelGather)
@@ -62,6 +65,19 @@ void gather_f3d_host(const cvtx_F3D* const* src, int n, float4* out) {
 		out[2 * i] = make_float4(f->start.x[0], f->start.x[1], f->start.x[2], f->strength);
 		out[2 * i + 1] = make_float4(f->end.x[0], f->end.x[1], f->end.x[2], 0.f);
 	}
+}
+
+// True when the measurement points are the gathered particles' coordinates,
+// bit for bit: the velocity call is then the particles acting on themselves.
+bool points_are_coords(const bsv_V3f* mes, const float4* rec, int n) {
+	int differ = 0;
+#pragma omp parallel for schedule(static) reduction(|: differ) if (n >= kParallelGather)
+	for (int i = 0; i < n; ++i) {
+		const float4 q = rec[2 * i];
+		const float c[3] = {q.x, q.y, q.z};
+		differ |= std::memcmp(c, mes[i].x, sizeof c) != 0;
+	}
+	return !differ;
 }
 
 void fill_nan(float* out, size_t n) {
@@ -130,8 +146,9 @@ bool gpu_usable(const cvtx_VortFunc* k, int* reg) {
 }
 
 // P3D induced velocity and/or stretching. Targets are either points (mes) or
-// particles (ind); when ind is the source pointer array itself, the source
-// records double as target records.
+// particles (ind); when ind is the source pointer array itself, or the
+// points are the sources' own coordinates, the source records double as
+// target records (and the self-interaction form can apply).
 int gpu_p3d_induce(const char* what, const cvtx_P3D** src, int n, const bsv_V3f* mes,
 	const cvtx_P3D** ind, int m, bsv_V3f* vel, bsv_V3f* dvort, int reg, float sigma)
 {
@@ -139,10 +156,11 @@ int gpu_p3d_induce(const char* what, const cvtx_P3D** src, int n, const bsv_V3f*
 	DeviceContext* c = job.ctx();
 	if (!c) return -3;
 	const size_t sb = size_t(n) * 32, ob = size_t(m) * 12;
-	const bool alias = ind && ind == src && m == n;
 	float4* hs = job.stage(c->h_src, c->src, sb);
 	if (!hs) return job.status();
 	gather_p3d_host(src, n, hs);
+	const bool alias = (ind && ind == src && m == n) ||
+		(!ind && m == n && n >= kSelfCheckMin && points_are_coords(mes, hs, n));
 	const float4* dtgt = static_cast<const float4*>(c->src.ptr);
 	int tstride = 2;
 	size_t tb = 0;
@@ -158,17 +176,17 @@ int gpu_p3d_induce(const char* what, const cvtx_P3D** src, int n, const bsv_V3f*
 	const unsigned ops = (vel ? kOpVel : 0u) | (dvort ? kOpDvort : 0u);
 	if (vel && !job.ensure_out(c->out0, c->h_out0, ob)) return job.status();
 	if (dvort && !job.ensure_out(c->out1, c->h_out1, ob)) return job.status();
-	if (!job.check(c->ensure_ws(p3d_induce_ws_bytes(reg, ops, n, m, c->num_sms)), "workspace"))
+	P3DInduceProblem p;
+	p.src = static_cast<const float4*>(c->src.ptr); p.n_src = n;
+	p.tgt = alias ? p.src : dtgt; p.tstride = tstride; p.n_tgt = m;
+	p.out_vel = vel ? static_cast<float*>(c->out0.ptr) : nullptr;
+	p.out_dvort = dvort ? static_cast<float*>(c->out1.ptr) : nullptr;
+	p.sigma = sigma;
+	if (!job.check(c->ensure_ws(p3d_induce_ws_bytes_for(reg, ops, p, c->num_sms)), "workspace"))
 		return job.status();
 	if (!job.begin()) return job.status();
 	job.upload(c->h_src, c->src, sb);
 	if (!alias) job.upload(c->h_tgt, c->tgt, tb);
-	P3DInduceProblem p;
-	p.src = static_cast<const float4*>(c->src.ptr); p.n_src = n;
-	p.tgt = dtgt; p.tstride = tstride; p.n_tgt = m;
-	p.out_vel = vel ? static_cast<float*>(c->out0.ptr) : nullptr;
-	p.out_dvort = dvort ? static_cast<float*>(c->out1.ptr) : nullptr;
-	p.sigma = sigma;
 	if (!job.failed()) job.check(p3d_induce(reg, ops, p, c->env()), "kernel launch");
 	bool ok;
 	if (vel && dvort) ok = job.finish(c->out0, c->h_out0, ob, &c->out1, &c->h_out1, ob);

@@ -76,9 +76,9 @@ p3d_batch_kernel(const BatchProblem* __restrict__ probs, int n_probs,
 		n_s = n_s < sp.src_per_split ? n_s : sp.src_per_split;
 		n_s = n_s > 0 ? n_s : 0;
 		const bool ok = induce2_block<R, VEL, DV, TPT, NT>(sp.p, sp.kc, tbase, s_begin, n_s, smem,
-			err, tcount, [&](int t, const double* acc, float ax, float ay, float az) {
+			err, tcount, [&](int t, const double* acc) {
 				if (sp.n_split == 1) {
-					write_induce<VEL, DV>(sp.p, sp.kc, t, acc, ax, ay, az);
+					write_induce<VEL, DV>(sp.p, sp.kc, t, acc);
 				} else {
 #pragma unroll
 					for (int c = 0; c < NC; ++c)
@@ -105,12 +105,7 @@ p3d_batch_kernel(const BatchProblem* __restrict__ probs, int n_probs,
 #pragma unroll
 						for (int c = 0; c < NC; ++c)
 							s[c] += __ldcg(&sp.partial[(size_t(q) * NC + c) * sp.p.n_tgt + t]);
-					float ax = 0.f, ay = 0.f, az = 0.f;
-					if (DV) {
-						const float4 tv = sp.p.tgt[size_t(t) * sp.p.tstride + 1];
-						ax = tv.x; ay = tv.y; az = tv.z;
-					}
-					write_induce<VEL, DV>(sp.p, sp.kc, t, s, ax, ay, az);
+					write_induce<VEL, DV>(sp.p, sp.kc, t, s);
 				}
 				if (threadIdx.x == 0) sp.counters[w.y] = 0u;
 			}

@@ -72,13 +72,13 @@ CVTX_EXPORT int cvtx_gb300_dev_P3D_M2M(const void* src, int n_src, const void* t
 	if (dvort_out && tgt_stride < 2) return -1;
 	DevCall c(stream);
 	const unsigned ops = (vel_out ? kOpVel : 0u) | (dvort_out ? kOpDvort : 0u);
-	int st = c.prepare(p3d_induce_ws_bytes(reg, ops, n_src, n_tgt, c.ctx ? c.ctx->num_sms : 1),
-		"cvtx_gb300_dev_P3D_M2M");
-	if (st) return st;
 	P3DInduceProblem p;
 	p.src = static_cast<const float4*>(src); p.n_src = n_src;
 	p.tgt = static_cast<const float4*>(tgt); p.tstride = tgt_stride; p.n_tgt = n_tgt;
 	p.out_vel = vel_out; p.out_dvort = dvort_out; p.sigma = sigma;
+	int st = c.prepare(p3d_induce_ws_bytes_for(reg, ops, p, c.ctx ? c.ctx->num_sms : 1),
+		"cvtx_gb300_dev_P3D_M2M");
+	if (st) return st;
 	return c.done(p3d_induce(reg, ops, p, c.env()), "cvtx_gb300_dev_P3D_M2M");
 }
 
@@ -89,14 +89,14 @@ CVTX_EXPORT int cvtx_gb300_dev_P3D_step(void* rec, int n, float* vel, float* dvo
 	if (!rec || !vel || !dvort || bad_reg(reg)) return -1;
 	DevCall c(stream);
 	const unsigned ops = kOpVel | kOpDvort;
-	int st = c.prepare(p3d_induce_ws_bytes(reg, ops, n, n, c.ctx ? c.ctx->num_sms : 1),
-		"cvtx_gb300_dev_P3D_step");
-	if (st) return st;
 	float4* r = static_cast<float4*>(rec);
 	P3DInduceProblem p;
 	p.src = r; p.n_src = n;
 	p.tgt = r; p.tstride = 2; p.n_tgt = n;
 	p.out_vel = vel; p.out_dvort = dvort; p.sigma = sigma;
+	int st = c.prepare(p3d_induce_ws_bytes_for(reg, ops, p, c.ctx ? c.ctx->num_sms : 1),
+		"cvtx_gb300_dev_P3D_step");
+	if (st) return st;
 	cudaError_t e = p3d_induce(reg, ops, p, c.env());
 	if (e == cudaSuccess) e = advance_p3d(r, n, vel, dvort, dt, c.stream);
 	return c.done(e, "cvtx_gb300_dev_P3D_step");

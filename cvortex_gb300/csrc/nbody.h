@@ -122,7 +122,20 @@ float gaussian_rho_c();
 void set_gaussian_rho_c(float rho_c);
 
 size_t p3d_induce_ws_bytes(int reg, unsigned ops, int n_src, int n_tgt, int num_sms);
+// Workspace for p3d_induce on this problem: as above, or the larger
+// workspace of the self-interaction form when that form applies to it.
+size_t p3d_induce_ws_bytes_for(int reg, unsigned ops, const P3DInduceProblem& p, int num_sms);
 cudaError_t p3d_induce(int reg, unsigned ops, const P3DInduceProblem& p, const LaunchEnv& env);
+
+// Self-interaction form (p3d_sym.cu): the particles are their own targets
+// (tgt == src, stride 2, n_tgt == n_src, at least CVTX_GB300_SYM_MIN
+// particles, default 32,768), so each unordered pair is evaluated once.
+// p3d_induce takes it when it applies, the launch is not bound by a CTA
+// lifetime cap (env.cta_src_cap), no launch configuration is forced, and the
+// workspace suffices; results stay deterministic.
+bool p3d_self_form_applies(int reg, unsigned ops, const P3DInduceProblem& p);
+size_t p3d_self_ws_bytes(int reg, unsigned ops, int n, int num_sms, size_t ws_cap = 0);
+cudaError_t p3d_self(int reg, unsigned ops, const P3DInduceProblem& p, const LaunchEnv& env);
 
 // As p3d_induce, with the source-split count capped so that the partial sums
 // fit env.ws_bytes (a fixed scratch area); never needs more than that.

@@ -88,80 +88,52 @@ InduceConsts make_induce_consts(int reg, float sigma) {
 
 namespace {
 
-// Accumulators per target (registers, FP32, reset every tile):
-//   VEL only : u  = sum G c,            c  = d x alpha_s
-//   DV       : A' = sum G da,           da = alpha_s - alpha_t
-//              B  = sum K (alpha_t.c') d, c' = d x da
-//   VEL + DV : also u' = sum G c' and W = sum G d; since d x alpha_s =
-//              c' + d x alpha_t, the velocity partial of a tile is
-//              u' + W x alpha_t, formed once per tile.
-// Working with da rather than alpha_s keeps the stretching terms free of the
-// cancellation of nearly parallel vorticity: alpha_t x alpha_s = alpha_t x da
-// and alpha_t.(d x alpha_s) = alpha_t.c' hold exactly, and da, c' are small
-// when the cross products are.
-// Shared state per target (compensated across tiles): u (3, VEL), A' and B
-// (6, DV).
+// Sums per target (registers, FP32, reset every tile), as in
+// p3d_induce.cuh: VEL u += G (d x alpha_s); DV A += G co, B += K (d.co) d with
+// co = alpha_t x alpha_s rounded as the reference rounds it.
 //
 // One source-target pair in scalar FP32 into the register partials of one
-// target (layout above). d = t - s; sv = source vorticity; a = alpha_t.
+// target. d = t - s; sv = source vorticity; a = alpha_t.
 template <Reg R, bool VEL, bool DV, int NR>
 __device__ __forceinline__ void induce_pair(float dx, float dy, float dz, const float4 sv,
 	float ax, float ay, float az, const InduceConsts& kc, float (&acc)[NR])
 {
 	constexpr bool kFinite = FiniteAtZero<R>::value;
 	const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+	// c = d x alpha_s
+	const float cx = fmaf(dy, sv.z, -dz * sv.y);
+	const float cy = fmaf(dz, sv.x, -dx * sv.z);
+	const float cz = fmaf(dx, sv.y, -dy * sv.x);
 	if (DV) {
-		const float ex = sv.x - ax;
-		const float ey = sv.y - ay;
-		const float ez = sv.z - az;
-		// c' = d x da
-		const float cx = fmaf(dy, ez, -dz * ey);
-		const float cy = fmaf(dz, ex, -dx * ez);
-		const float cz = fmaf(dx, ey, -dy * ex);
 		float G, K;
 		RegP3D<R>::gk(r2, kc.rc, G, K);
 		const bool nz = r2 > 0.f;
 		G = nz ? G : 0.f;
 		if (!kFinite) K = nz ? K : 0.f;
-		constexpr int o = VEL ? 6 : 0;
+		constexpr int o = VEL ? 3 : 0;
 		if (VEL) {
 			acc[0] = fmaf(G, cx, acc[0]);
 			acc[1] = fmaf(G, cy, acc[1]);
 			acc[2] = fmaf(G, cz, acc[2]);
-			acc[3] = fmaf(G, dx, acc[3]);
-			acc[4] = fmaf(G, dy, acc[4]);
-			acc[5] = fmaf(G, dz, acc[5]);
 		}
-		acc[o + 0] = fmaf(G, ex, acc[o + 0]);
-		acc[o + 1] = fmaf(G, ey, acc[o + 1]);
-		acc[o + 2] = fmaf(G, ez, acc[o + 2]);
-		const float pd = fmaf(az, cz, fmaf(ay, cy, ax * cx));
+		// co = alpha_t x alpha_s: two rounded products and their difference
+		const float ox = __fsub_rn(__fmul_rn(ay, sv.z), __fmul_rn(az, sv.y));
+		const float oy = __fsub_rn(__fmul_rn(az, sv.x), __fmul_rn(ax, sv.z));
+		const float oz = __fsub_rn(__fmul_rn(ax, sv.y), __fmul_rn(ay, sv.x));
+		acc[o + 0] = fmaf(G, ox, acc[o + 0]);
+		acc[o + 1] = fmaf(G, oy, acc[o + 1]);
+		acc[o + 2] = fmaf(G, oz, acc[o + 2]);
+		const float pd = fmaf(dz, oz, fmaf(dy, oy, dx * ox));
 		const float kk = K * pd;
 		acc[o + 3] = fmaf(kk, dx, acc[o + 3]);
 		acc[o + 4] = fmaf(kk, dy, acc[o + 4]);
 		acc[o + 5] = fmaf(kk, dz, acc[o + 5]);
 	} else {
-		// c = d x alpha_s
-		const float cx = fmaf(dy, sv.z, -dz * sv.y);
-		const float cy = fmaf(dz, sv.x, -dx * sv.z);
-		const float cz = fmaf(dx, sv.y, -dy * sv.x);
 		float G = RegP3D<R>::g(r2, kc.rc);
 		if (!kFinite) G = r2 > 0.f ? G : 0.f;
 		acc[0] = fmaf(G, cx, acc[0]);
 		acc[1] = fmaf(G, cy, acc[1]);
 		acc[2] = fmaf(G, cz, acc[2]);
-	}
-}
-
-// Fused vel + dvort: the velocity partial u' + W x alpha_t into slots 0..2.
-template <bool VEL, bool DV, int NR>
-__device__ __forceinline__ void induce_combine(float ax, float ay, float az, float (&acc)[NR])
-{
-	if (VEL && DV) {
-		const float wx = acc[3], wy = acc[4], wz = acc[5];
-		acc[0] += fmaf(wy, az, -wz * ay);
-		acc[1] += fmaf(wz, ax, -wx * az);
-		acc[2] += fmaf(wx, ay, -wy * ax);
 	}
 }
 
@@ -171,7 +143,7 @@ p3d_induce_kernel(const P3DInduceProblem p, const InduceConsts kc,
 	double* __restrict__ partial, int src_per_split, unsigned* err)
 {
 	constexpr int NC = (VEL ? 3 : 0) + (DV ? 6 : 0);     // compensated sums
-	constexpr int NR = (VEL ? (DV ? 6 : 3) : 0) + (DV ? 6 : 0);  // register partials
+	constexpr int NR = NC;                               // register partials
 	extern __shared__ __align__(16) unsigned char smem[];
 	float* hi = reinterpret_cast<float*>(smem + Stream2::kSmemBytes);
 	float* lo = hi + NC * TPT * NT;
@@ -223,15 +195,12 @@ p3d_induce_kernel(const P3DInduceProblem p, const InduceConsts kc,
 			for (int j = 0; j < cnt; ++j) body(j);
 		}
 #pragma unroll
-		for (int k = 0; k < TPT; ++k) induce_combine<VEL, DV>(ax[k], ay[k], az[k], acc[k]);
-#pragma unroll
 		for (int c = 0; c < NC; ++c) {
-			const int src_c = (VEL && DV && c >= 3) ? c + 3 : c;
 #pragma unroll
 			for (int k = 0; k < TPT; ++k) {
 				const int i = (c * TPT + k) * NT + tid;
 				float h = hi[i], l = lo[i];
-				fold_twosum(h, l, acc[k][src_c]);
+				fold_twosum(h, l, acc[k][c]);
 				hi[i] = h; lo[i] = l;
 			}
 		}
@@ -250,7 +219,7 @@ p3d_induce_kernel(const P3DInduceProblem p, const InduceConsts kc,
 			s[c] = double(hi[i]) + double(lo[i]);
 		}
 		if (gridDim.y == 1) {
-			write_induce<VEL, DV>(p, kc, t, s, ax[k], ay[k], az[k]);
+			write_induce<VEL, DV>(p, kc, t, s);
 		} else {
 #pragma unroll
 			for (int c = 0; c < NC; ++c)
@@ -276,9 +245,9 @@ p3d_induce2_kernel(const P3DInduceProblem p, const InduceConsts kc,
 	n_s = n_s > 0 ? n_s : 0;
 	induce2_block<R, VEL, DV, TPT, NT, UNROLL, TILE>(p, kc, blockIdx.x * (TPT * NT), s_begin, n_s,
 		smem, err,
-		tcount, [&](int t, const double* acc, float ax, float ay, float az) {
+		tcount, [&](int t, const double* acc) {
 			if (gridDim.y == 1) {
-				write_induce<VEL, DV>(p, kc, t, acc, ax, ay, az);
+				write_induce<VEL, DV>(p, kc, t, acc);
 			} else {
 #pragma unroll
 				for (int c = 0; c < NC; ++c)
@@ -300,12 +269,7 @@ __global__ void p3d_induce_finalize(const P3DInduceProblem p, const InduceConsts
 	for (int sp = 0; sp < n_split; ++sp)
 #pragma unroll
 		for (int c = 0; c < NC; ++c) s[c] += partial[(size_t(sp) * NC + c) * p.n_tgt + t];
-	float ax = 0.f, ay = 0.f, az = 0.f;
-	if (DV) {
-		const float4 tv = p.tgt[size_t(t) * p.tstride + 1];
-		ax = tv.x; ay = tv.y; az = tv.z;
-	}
-	write_induce<VEL, DV>(p, kc, t, s, ax, ay, az);
+	write_induce<VEL, DV>(p, kc, t, s);
 }
 
 // The P3D velocity / stretching pair as an operation of the few-target form
@@ -315,7 +279,7 @@ struct P3DInduceOp {
 	using Problem = P3DInduceProblem;
 	using Consts = InduceConsts;
 	static constexpr int NC = InduceNC<VEL, DV>::value;
-	static constexpr int NR = (VEL ? (DV ? 6 : 3) : 0) + (DV ? 6 : 0);
+	static constexpr int NR = NC;
 	struct Tgt { float x, y, z, ax, ay, az; };
 	struct Src { float4 pos, vort; };
 	__device__ static int n_src(const Problem& p) { return p.n_src; }
@@ -336,13 +300,10 @@ struct P3DInduceOp {
 		induce_pair<R, VEL, DV>(t.x - s.pos.x, t.y - s.pos.y, t.z - s.pos.z, s.vort,
 			t.ax, t.ay, t.az, k, acc);
 	}
-	__device__ static void combine(const Tgt& t, float (&acc)[NR]) {
-		induce_combine<VEL, DV>(t.ax, t.ay, t.az, acc);
-	}
-	__device__ static int slot(int c) { return (VEL && DV && c >= 3) ? c + 3 : c; }
+	__device__ static void combine(const Tgt&, float (&)[NR]) {}
+	__device__ static int slot(int c) { return c; }
 	__device__ static void write(const Problem& p, const Consts& k, int t, const double* s) {
-		const Tgt g = target(p, t);
-		write_induce<VEL, DV>(p, k, t, s, g.ax, g.ay, g.az);
+		write_induce<VEL, DV>(p, k, t, s);
 	}
 };
 
@@ -1056,9 +1017,29 @@ size_t p3d_induce_ws_bytes(int reg, unsigned ops, int n_src, int n_tgt, int num_
 	return induce_ws(reg, ops, n_src, n_tgt, num_sms, choose_cfg(reg, ops, n_tgt, n_src));
 }
 
+// The self-interaction form when it applies to the problem and the launch
+// (no CTA lifetime cap, no forced or tuned configuration).
+static bool use_self_form(int reg, unsigned ops, const P3DInduceProblem& p, int cta_src_cap) {
+	if (cta_src_cap > 0 || env_cfg() >= 0) return false;
+	if (g_tuned[reg & 3][ops & 3][size_bucket(p.n_tgt)].load(std::memory_order_relaxed) >= 0)
+		return false;
+	return p3d_self_form_applies(reg, ops, p);
+}
+
+size_t p3d_induce_ws_bytes_for(int reg, unsigned ops, const P3DInduceProblem& p, int num_sms) {
+	if (p.n_tgt <= 0) return 0;
+	const size_t base = p3d_induce_ws_bytes(reg, ops, p.n_src, p.n_tgt, num_sms);
+	if (!use_self_form(reg, ops, p, 0)) return base;
+	return std::max(base, p3d_self_ws_bytes(reg, ops, p.n_tgt, num_sms));
+}
+
 cudaError_t p3d_induce(int reg, unsigned ops, const P3DInduceProblem& p, const LaunchEnv& env) {
 	if (p.n_tgt <= 0) return cudaSuccess;
 	if (reg < 0 || reg > 3 || ops < 1 || ops > 3) return cudaErrorInvalidValue;
+	if (use_self_form(reg, ops, p, env.cta_src_cap) &&
+		p3d_self_ws_bytes(reg, ops, p.n_tgt, env.num_sms, env.cap_to_ws ? env.ws_bytes : 0) <=
+			env.ws_bytes)
+		return p3d_self(reg, ops, p, env);
 	return induce_launch(reg, ops, p, env, choose_cfg(reg, ops, p.n_tgt, p.n_src), false);
 }
 

@@ -1,19 +1,20 @@
 // p3d_induce.cuh -- the P3D velocity / vortex-stretching CTA body shared by
 // the per-call kernels (p3d.cu) and the batched persistent kernel (batch.cu).
 //
-// Accumulators per target (registers, FP32, reset every tile):
-//   VEL only : u  = sum G c,            c  = d x alpha_s
-//   DV       : A' = sum G da,           da = alpha_s - alpha_t
-//              B  = sum K (alpha_t.c') d, c' = d x da
-//   VEL + DV : also u' = sum G c' and W = sum G d; since d x alpha_s =
-//              c' + d x alpha_t, the velocity partial of a tile is
-//              u' + W x alpha_t, formed once per tile.
-// Working with da rather than alpha_s keeps the stretching terms free of the
-// cancellation of nearly parallel vorticity: alpha_t x alpha_s = alpha_t x da
-// and alpha_t.(d x alpha_s) = alpha_t.c' hold exactly, and da, c' are small
-// when the cross products are. Per target, the compensated state across
-// tiles is u (3, VEL), A' and B (6, DV), kept in shared memory as (hi, lo).
-// Final outputs: vel = S_vel u, dvort = S_dv (alpha_t x A' + K_scale B).
+// Per pair (t, s), d = x_t - x_s, the sums per target (registers, FP32,
+// reset every tile) are
+//   VEL: u += G c,  c  = d x alpha_s
+//   DV : A += G co, co = alpha_t x alpha_s
+//        B += K (d.co) d
+// with the reference's own per-pair terms (src/P3D.cpp:51-72, 86-114). The
+// stretching cross product co is rounded as the reference rounds it (two
+// products and a difference, no fused multiply-add), so that it is the
+// reference's term bit for bit: its rounding is what decides the result
+// both where the vorticity of a pair is nearly parallel (co small against
+// |alpha_t||alpha_s|) and where a target's vorticity dwarfs its sources'
+// (a factored or centred sum over the sources would cancel there).
+// Across tiles the sums are compensated (hi, lo) pairs in shared memory.
+// Final outputs: vel = S_vel u, dvort = S_dv (A - K_scale B).
 #pragma once
 #include "nbody.h"
 #include "regfuncs.cuh"
@@ -47,7 +48,7 @@ constexpr size_t induce_smem_bytes() {
 
 template <bool VEL, bool DV>
 __device__ __forceinline__ void write_induce(const P3DInduceProblem& p,
-	const InduceConsts& kc, int t, const double* s, float ax, float ay, float az)
+	const InduceConsts& kc, int t, const double* s)
 {
 	int o = 0;
 	if (VEL) {
@@ -58,25 +59,33 @@ __device__ __forceinline__ void write_induce(const P3DInduceProblem& p,
 		o = 3;
 	}
 	if (DV) {
-		const double Ax = s[o], Ay = s[o + 1], Az = s[o + 2];
-		const double cx = double(ay) * Az - double(az) * Ay;
-		const double cy = double(az) * Ax - double(ax) * Az;
-		const double cz = double(ax) * Ay - double(ay) * Ax;
 		float* w = p.out_dvort + 3 * size_t(t);
-		w[0] = float(kc.s_dv * (cx + kc.k_scale * s[o + 3]));
-		w[1] = float(kc.s_dv * (cy + kc.k_scale * s[o + 4]));
-		w[2] = float(kc.s_dv * (cz + kc.k_scale * s[o + 5]));
+		w[0] = float(kc.s_dv * (s[o + 0] - kc.k_scale * s[o + 3]));
+		w[1] = float(kc.s_dv * (s[o + 1] - kc.k_scale * s[o + 4]));
+		w[2] = float(kc.s_dv * (s[o + 2] - kc.k_scale * s[o + 5]));
 	}
 }
 
 __device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
 
+// co = a x b per lane, rounded as the reference rounds it: each component is
+// the difference of two rounded products (nb = -b, so that the second
+// product carries its sign and needs no separate negation).
+__device__ __forceinline__ void cross_ref2(float2 ax, float2 ay, float2 az,
+	float2 bx, float2 by, float2 bz, float2 nbx, float2 nby, float2 nbz,
+	float2& cx, float2& cy, float2& cz)
+{
+	cx = __fadd2_rn(__fmul2_rn(ay, bz), __fmul2_rn(az, nby));
+	cy = __fadd2_rn(__fmul2_rn(az, bx), __fmul2_rn(ax, nbz));
+	cz = __fadd2_rn(__fmul2_rn(ax, by), __fmul2_rn(ay, nbx));
+}
+
 // Packed CTA body: targets tbase + k*NT + threadIdx.x (k < TPT; thread-local
 // pairs (2h, 2h+1) share one f32x2 lane pair) against sources
 // [s_begin, s_begin + n_s) streamed through `smem` (barriers initialised by
 // P3DStream::init; `tcount` carries the stage phase across calls). For every
-// valid target calls sink(t, sums[NC], alpha_t). Returns false if the tile
-// pipeline timed out (results were not produced).
+// valid target calls sink(t, sums[NC]). Returns false if the tile pipeline
+// timed out (results were not produced).
 template <Reg R, bool VEL, bool DV, int TPT, int NT, int UNROLL = 2, int TILE = kP3DTile,
 	class Sink>
 __device__ __forceinline__ bool induce2_block(const P3DInduceProblem& p, const InduceConsts& kc,
@@ -86,7 +95,7 @@ __device__ __forceinline__ bool induce2_block(const P3DInduceProblem& p, const I
 	static_assert(TPT % 2 == 0, "packed kernel: even TPT");
 	constexpr int H = TPT / 2;
 	constexpr int NC = InduceNC<VEL, DV>::value;
-	constexpr int NR = (VEL ? (DV ? 6 : 3) : 0) + (DV ? 6 : 0);
+	constexpr int NR = NC;
 	constexpr bool kFinite = FiniteAtZero<R>::value;
 	using Stream = P3DStreamT<TILE>;
 	float* hi = reinterpret_cast<float*>(smem + Stream::kSmemBytes);
@@ -125,6 +134,7 @@ __device__ __forceinline__ bool induce2_block(const P3DInduceProblem& p, const I
 			const float4 sv = st[2 * j + 1];
 			const float2 sx = bc2(sp.x), sy = bc2(sp.y), sz = bc2(sp.z);
 			const float2 wx = bc2(sv.x), wy = bc2(sv.y), wz = bc2(sv.z);
+			const float2 nwx = bc2(-sv.x), nwy = bc2(-sv.y), nwz = bc2(-sv.z);
 #pragma unroll
 			for (int h = 0; h < H; ++h) {
 				// d = t - s as s * (-1) + t: one rounding, no per-source negation
@@ -132,11 +142,11 @@ __device__ __forceinline__ bool induce2_block(const P3DInduceProblem& p, const I
 				const float2 dy = __ffma2_rn(sy, bc2(-1.f), ty[h]);
 				const float2 dz = __ffma2_rn(sz, bc2(-1.f), tz[h]);
 				const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+				// c = d x alpha_s
+				const float2 cx = __ffma2_rn(dy, wz, __fmul2_rn(dz, nwy));
+				const float2 cy = __ffma2_rn(dz, wx, __fmul2_rn(dx, nwz));
+				const float2 cz = __ffma2_rn(dx, wy, __fmul2_rn(dy, nwx));
 				if (!DV) {
-					// c = d x alpha_s
-					const float2 cx = __ffma2_rn(dy, wz, neg2(__fmul2_rn(dz, wy)));
-					const float2 cy = __ffma2_rn(dz, wx, neg2(__fmul2_rn(dx, wz)));
-					const float2 cz = __ffma2_rn(dx, wy, neg2(__fmul2_rn(dy, wx)));
 					float2 G = RegP3D2<R>::g2(r2, rc);
 					if (!kFinite) {
 						G.x = r2.x > 0.f ? G.x : 0.f;
@@ -147,13 +157,6 @@ __device__ __forceinline__ bool induce2_block(const P3DInduceProblem& p, const I
 					acc[2][h] = __ffma2_rn(G, cz, acc[2][h]);
 					continue;
 				}
-				// da = alpha_s - alpha_t, c' = d x da
-				const float2 ex = __ffma2_rn(ax[h], bc2(-1.f), wx);
-				const float2 ey = __ffma2_rn(ay[h], bc2(-1.f), wy);
-				const float2 ez = __ffma2_rn(az[h], bc2(-1.f), wz);
-				const float2 cx = __ffma2_rn(dy, ez, neg2(__fmul2_rn(dz, ey)));
-				const float2 cy = __ffma2_rn(dz, ex, neg2(__fmul2_rn(dx, ez)));
-				const float2 cz = __ffma2_rn(dx, ey, neg2(__fmul2_rn(dy, ex)));
 				float2 G, K;
 				RegP3D2<R>::gk2(r2, rc, G, K);
 				G.x = r2.x > 0.f ? G.x : 0.f;
@@ -162,19 +165,19 @@ __device__ __forceinline__ bool induce2_block(const P3DInduceProblem& p, const I
 					K.x = r2.x > 0.f ? K.x : 0.f;
 					K.y = r2.y > 0.f ? K.y : 0.f;
 				}
-				constexpr int o = VEL ? 6 : 0;
+				constexpr int o = VEL ? 3 : 0;
 				if (VEL) {
 					acc[0][h] = __ffma2_rn(G, cx, acc[0][h]);
 					acc[1][h] = __ffma2_rn(G, cy, acc[1][h]);
 					acc[2][h] = __ffma2_rn(G, cz, acc[2][h]);
-					acc[3][h] = __ffma2_rn(G, dx, acc[3][h]);
-					acc[4][h] = __ffma2_rn(G, dy, acc[4][h]);
-					acc[5][h] = __ffma2_rn(G, dz, acc[5][h]);
 				}
-				acc[o + 0][h] = __ffma2_rn(G, ex, acc[o + 0][h]);
-				acc[o + 1][h] = __ffma2_rn(G, ey, acc[o + 1][h]);
-				acc[o + 2][h] = __ffma2_rn(G, ez, acc[o + 2][h]);
-				const float2 pd = __ffma2_rn(az[h], cz, __ffma2_rn(ay[h], cy, __fmul2_rn(ax[h], cx)));
+				// co = alpha_t x alpha_s (reference rounding)
+				float2 ox, oy, oz;
+				cross_ref2(ax[h], ay[h], az[h], wx, wy, wz, nwx, nwy, nwz, ox, oy, oz);
+				acc[o + 0][h] = __ffma2_rn(G, ox, acc[o + 0][h]);
+				acc[o + 1][h] = __ffma2_rn(G, oy, acc[o + 1][h]);
+				acc[o + 2][h] = __ffma2_rn(G, oz, acc[o + 2][h]);
+				const float2 pd = __ffma2_rn(dz, oz, __ffma2_rn(dy, oy, __fmul2_rn(dx, ox)));
 				const float2 kk = __fmul2_rn(K, pd);
 				acc[o + 3][h] = __ffma2_rn(kk, dx, acc[o + 3][h]);
 				acc[o + 4][h] = __ffma2_rn(kk, dy, acc[o + 4][h]);
@@ -188,18 +191,8 @@ __device__ __forceinline__ bool induce2_block(const P3DInduceProblem& p, const I
 #pragma unroll 1
 			for (int j = 0; j < cnt; ++j) body(j);
 		}
-		if (VEL && DV) {
-#pragma unroll
-			for (int h = 0; h < H; ++h) {
-				const float2 wx_ = acc[3][h], wy_ = acc[4][h], wz_ = acc[5][h];
-				acc[0][h] = __fadd2_rn(acc[0][h], __ffma2_rn(wy_, az[h], neg2(__fmul2_rn(wz_, ay[h]))));
-				acc[1][h] = __fadd2_rn(acc[1][h], __ffma2_rn(wz_, ax[h], neg2(__fmul2_rn(wx_, az[h]))));
-				acc[2][h] = __fadd2_rn(acc[2][h], __ffma2_rn(wx_, ay[h], neg2(__fmul2_rn(wy_, ax[h]))));
-			}
-		}
 #pragma unroll
 		for (int c = 0; c < NC; ++c) {
-			const int src_c = (VEL && DV && c >= 3) ? c + 3 : c;
 #pragma unroll
 			for (int h = 0; h < H; ++h) {
 #pragma unroll
@@ -207,7 +200,7 @@ __device__ __forceinline__ bool induce2_block(const P3DInduceProblem& p, const I
 					const int k = 2 * h + e;
 					const int i = (c * TPT + k) * NT + tid;
 					float hh = hi[i], ll = lo[i];
-					fold_twosum(hh, ll, e == 0 ? acc[src_c][h].x : acc[src_c][h].y);
+					fold_twosum(hh, ll, e == 0 ? acc[c][h].x : acc[c][h].y);
 					hi[i] = hh; lo[i] = ll;
 				}
 			}
@@ -229,10 +222,7 @@ __device__ __forceinline__ bool induce2_block(const P3DInduceProblem& p, const I
 				const int i = (c * TPT + k) * NT + tid;
 				sacc[c] = double(hi[i]) + double(lo[i]);
 			}
-			const float tax = e == 0 ? ax[h].x : ax[h].y;
-			const float tay = e == 0 ? ay[h].x : ay[h].y;
-			const float taz = e == 0 ? az[h].x : az[h].y;
-			sink(t, sacc, tax, tay, taz);
+			sink(t, sacc);
 		}
 	}
 	return true;

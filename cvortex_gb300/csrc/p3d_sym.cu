@@ -1,0 +1,468 @@
+// p3d_sym.cu -- P3D velocity / vortex stretching of a particle set on itself,
+// each unordered pair evaluated once.
+//
+// The all-pairs calls of the reference (src/P3D.cpp:343-366, 387-410) are
+// most often made with the particles as their own targets (a vortex-particle
+// time step; the reference's benchmark, bench/benchP3D.c:338-345). For such a
+// call the terms of the pair (t, s) that the two particles receive are
+// related (d = x_t - x_s; p3d_induce.cuh gives the sums):
+//   vel:   t gets G d x alpha_s,            s gets -G d x alpha_t
+//   dvort: t gets G co + K (d.co) d,        s gets the negation,
+// since co = alpha_t x alpha_s changes sign with the pair and d.co does not.
+// One evaluation of G, K, co and d.co (co rounded as the reference rounds
+// it) thus serves both particles: about 29 instead of 43 FP32-pipe
+// operations per interaction for the fused pair.
+//
+// Work decomposition (deterministic, no floating-point atomics):
+// * The particles are cut into nb blocks of S (a multiple of the 512-target
+//   pass of a CTA; the last block may be shorter). A work item is a block
+//   pair (bi, bj), bi <= bj; a persistent grid claims items through an atomic
+//   counter, largest first.
+// * Item (bi, bj), bi < bj: for each pass of 512 particles of block bi (held
+//   in registers, two per f32x2 lane pair), the records of block bj stream
+//   through shared memory in 256-record tiles (bulk copies). Within a warp
+//   the 32 records of a group are visited in a rotation: at step k lane l
+//   pairs its four particles with record (l + k) mod 32, whose running sums
+//   travel with it from lane to lane by shuffles and are back at their home
+//   lane after 32 steps. The four warps' sums per record are added in warp
+//   order in shared memory and accumulated over the passes into the
+//   workspace slot (bi, record). The bi particles' own sums are folded per
+//   tile into compensated (hi, lo) pairs and written to slot (bj, particle)
+//   after the pass.
+// * Item (b, b): every ordered pair of the block by the per-call CTA body
+//   (induce2_block), into slot (b, particle).
+// * Every particle thus has exactly nb slot partials (one per partner
+//   block); a finalize kernel adds them in block order in FP64 and applies
+//   the output transforms. The result does not depend on scheduling.
+//
+// Coincident distinct particles contribute nothing to each other, as in the
+// reference; every wait on a tile is bounded (tile_stream.cuh).
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+
+#include "nbody.h"
+#include "p3d_induce.cuh"
+#include "plan.cuh"
+
+namespace cvtx {
+namespace {
+
+constexpr int kSymNT = 128;                    // threads per CTA
+constexpr int kSymTPT = 4;                     // particles per thread and pass
+constexpr int kSymPass = kSymNT * kSymTPT;     // particles of block bi per pass
+constexpr int kSymWarps = kSymNT / 32;
+constexpr int kSymMinBlocks = 3;               // resident CTAs per SM
+
+template <bool VEL, bool DV> struct SymNR {
+	// register sums per particle: vel 3 (u); dvort 6 (A, B); fused 9
+	static constexpr int value = InduceNC<VEL, DV>::value;
+};
+
+// Shared memory: tile stages, then (hi, lo) per pass particle and sum, then
+// two buffers of per-warp record sums [2][warps][NC][32].
+template <bool VEL, bool DV>
+constexpr size_t sym_smem_bytes() {
+	constexpr int NC = InduceNC<VEL, DV>::value;
+	return P3DStream::kSmemBytes + size_t(2) * NC * kSymPass * sizeof(float) +
+		size_t(2) * kSymWarps * NC * 32 * sizeof(float);
+}
+
+// One rotation step: this lane's particles (packed) against record (sp, sv),
+// whose running sums are `js`. FULL = false zeroes the pair for lanes whose
+// record lies past the end of the block (`valid` false).
+template <Reg R, bool VEL, bool DV, bool FULL>
+__device__ __forceinline__ void sym_step(const RegConsts& rc, float4 sp, float4 sv, bool valid,
+	const float2 (&tx)[2], const float2 (&ty)[2], const float2 (&tz)[2],
+	const float2 (&ax)[2], const float2 (&ay)[2], const float2 (&az)[2],
+	const float2 (&nax)[2], const float2 (&nay)[2], const float2 (&naz)[2],
+	float2 (&acc)[SymNR<VEL, DV>::value][2], float (&js)[SymNR<VEL, DV>::value])
+{
+	constexpr bool kFinite = FiniteAtZero<R>::value;
+	if (!FULL && !valid) {
+		sp = make_float4(0.f, 0.f, 0.f, 0.f);
+		sv = make_float4(0.f, 0.f, 0.f, 0.f);
+	}
+	const float2 sx = bc2(sp.x), sy = bc2(sp.y), sz = bc2(sp.z);
+	const float2 wx = bc2(sv.x), wy = bc2(sv.y), wz = bc2(sv.z);
+	const float2 nwx = bc2(-sv.x), nwy = bc2(-sv.y), nwz = bc2(-sv.z);
+#pragma unroll
+	for (int h = 0; h < 2; ++h) {
+		const float2 dx = __ffma2_rn(sx, bc2(-1.f), tx[h]);
+		const float2 dy = __ffma2_rn(sy, bc2(-1.f), ty[h]);
+		const float2 dz = __ffma2_rn(sz, bc2(-1.f), tz[h]);
+		const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+		float2 G, K;
+		if (DV) {
+			RegP3D2<R>::gk2(r2, rc, G, K);
+			G.x = r2.x > 0.f ? G.x : 0.f;
+			G.y = r2.y > 0.f ? G.y : 0.f;
+			if (!kFinite) {
+				K.x = r2.x > 0.f ? K.x : 0.f;
+				K.y = r2.y > 0.f ? K.y : 0.f;
+			}
+		} else {
+			G = RegP3D2<R>::g2(r2, rc);
+			if (!kFinite) {
+				G.x = r2.x > 0.f ? G.x : 0.f;
+				G.y = r2.y > 0.f ? G.y : 0.f;
+			}
+		}
+		if (!FULL && !valid) {
+			G = make_float2(0.f, 0.f);
+			K = make_float2(0.f, 0.f);
+		}
+		if (VEL) {
+			// t: G d x alpha_s; s: -G d x alpha_t
+			const float2 cx = __ffma2_rn(dy, wz, __fmul2_rn(dz, nwy));
+			const float2 cy = __ffma2_rn(dz, wx, __fmul2_rn(dx, nwz));
+			const float2 cz = __ffma2_rn(dx, wy, __fmul2_rn(dy, nwx));
+			const float2 qx = __ffma2_rn(dy, az[h], __fmul2_rn(dz, nay[h]));
+			const float2 qy = __ffma2_rn(dz, ax[h], __fmul2_rn(dx, naz[h]));
+			const float2 qz = __ffma2_rn(dx, ay[h], __fmul2_rn(dy, nax[h]));
+			acc[0][h] = __ffma2_rn(G, cx, acc[0][h]);
+			acc[1][h] = __ffma2_rn(G, cy, acc[1][h]);
+			acc[2][h] = __ffma2_rn(G, cz, acc[2][h]);
+			js[0] = fmaf(-G.x, qx.x, fmaf(-G.y, qx.y, js[0]));
+			js[1] = fmaf(-G.x, qy.x, fmaf(-G.y, qy.y, js[1]));
+			js[2] = fmaf(-G.x, qz.x, fmaf(-G.y, qz.y, js[2]));
+		}
+		if (DV) {
+			constexpr int o = VEL ? 3 : 0;
+			// co = alpha_t x alpha_s (reference rounding)
+			float2 ox, oy, oz;
+			cross_ref2(ax[h], ay[h], az[h], wx, wy, wz, nwx, nwy, nwz, ox, oy, oz);
+			const float2 pd = __ffma2_rn(dz, oz, __ffma2_rn(dy, oy, __fmul2_rn(dx, ox)));
+			const float2 kk = __fmul2_rn(K, pd);
+			acc[o + 0][h] = __ffma2_rn(G, ox, acc[o + 0][h]);
+			acc[o + 1][h] = __ffma2_rn(G, oy, acc[o + 1][h]);
+			acc[o + 2][h] = __ffma2_rn(G, oz, acc[o + 2][h]);
+			acc[o + 3][h] = __ffma2_rn(kk, dx, acc[o + 3][h]);
+			acc[o + 4][h] = __ffma2_rn(kk, dy, acc[o + 4][h]);
+			acc[o + 5][h] = __ffma2_rn(kk, dz, acc[o + 5][h]);
+			js[o + 0] = fmaf(-G.x, ox.x, fmaf(-G.y, ox.y, js[o + 0]));
+			js[o + 1] = fmaf(-G.x, oy.x, fmaf(-G.y, oy.y, js[o + 1]));
+			js[o + 2] = fmaf(-G.x, oz.x, fmaf(-G.y, oz.y, js[o + 2]));
+			js[o + 3] = fmaf(-kk.x, dx.x, fmaf(-kk.y, dx.y, js[o + 3]));
+			js[o + 4] = fmaf(-kk.x, dy.x, fmaf(-kk.y, dy.y, js[o + 4]));
+			js[o + 5] = fmaf(-kk.x, dz.x, fmaf(-kk.y, dz.y, js[o + 5]));
+		}
+	}
+}
+
+// One 32-record group: 32 rotation steps; returns the group records' sums
+// at their home lanes in js.
+template <Reg R, bool VEL, bool DV, bool FULL>
+__device__ __forceinline__ void sym_group(const RegConsts& rc, const float4* __restrict__ grp,
+	int gcnt, int lane,
+	const float2 (&tx)[2], const float2 (&ty)[2], const float2 (&tz)[2],
+	const float2 (&ax)[2], const float2 (&ay)[2], const float2 (&az)[2],
+	const float2 (&nax)[2], const float2 (&nay)[2], const float2 (&naz)[2],
+	float2 (&acc)[SymNR<VEL, DV>::value][2], float (&js)[SymNR<VEL, DV>::value])
+{
+	constexpr int NR = SymNR<VEL, DV>::value;
+	const int from = (lane + 1) & 31;
+#pragma unroll 2
+	for (int k = 0; k < 32; ++k) {
+		const int jl = (lane + k) & 31;
+		const float4 sp = grp[2 * jl];
+		const float4 sv = grp[2 * jl + 1];
+		sym_step<R, VEL, DV, FULL>(rc, sp, sv, jl < gcnt, tx, ty, tz, ax, ay, az, nax, nay, naz,
+			acc, js);
+#pragma unroll
+		for (int c = 0; c < NR; ++c) js[c] = __shfl_sync(0xffffffffu, js[c], from);
+	}
+}
+
+struct SymArgs {
+	int S;            // block length (multiple of kSymPass)
+	int nb;           // blocks
+	float* slots;     // [nb][NC][n] partial sums
+};
+
+// Item (bi, bj), bi < bj: all passes of block bi against block bj.
+template <Reg R, bool VEL, bool DV>
+__device__ __forceinline__ bool sym_item(const P3DInduceProblem& p, const InduceConsts& kc,
+	const SymArgs& a, int bi, int bj, unsigned char* smem, unsigned* err, unsigned& tcount)
+{
+	constexpr int NC = InduceNC<VEL, DV>::value;
+	constexpr int NR = SymNR<VEL, DV>::value;
+	const int n = p.n_tgt;
+	float* hi = reinterpret_cast<float*>(smem + P3DStream::kSmemBytes);
+	float* lo = hi + NC * kSymPass;
+	float* jbuf = lo + NC * kSymPass;            // [2][warps][NC][32]
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const RegConsts rc = kc.rc;
+	const int i0 = bi * a.S;
+	const int j0 = bj * a.S;
+	const int nj = min(n, j0 + a.S) - j0;
+	int par = 0;
+	for (int tb = i0; tb < i0 + a.S; tb += kSymPass) {
+		const bool first = tb == i0;
+		float2 tx[2], ty[2], tz[2], ax[2], ay[2], az[2], nax[2], nay[2], naz[2];
+#pragma unroll
+		for (int h = 0; h < 2; ++h) {
+			const int t0 = tb + (2 * h) * kSymNT + tid, t1 = t0 + kSymNT;
+			const float4 q0 = p.tgt[2 * size_t(t0)], q1 = p.tgt[2 * size_t(t1)];
+			const float4 v0 = p.tgt[2 * size_t(t0) + 1], v1 = p.tgt[2 * size_t(t1) + 1];
+			tx[h] = make_float2(q0.x, q1.x); ty[h] = make_float2(q0.y, q1.y);
+			tz[h] = make_float2(q0.z, q1.z);
+			ax[h] = make_float2(v0.x, v1.x); ay[h] = make_float2(v0.y, v1.y);
+			az[h] = make_float2(v0.z, v1.z);
+			nax[h] = make_float2(-v0.x, -v1.x); nay[h] = make_float2(-v0.y, -v1.y);
+			naz[h] = make_float2(-v0.z, -v1.z);
+		}
+#pragma unroll
+		for (int i = 0; i < NC * kSymTPT; ++i) { hi[i * kSymNT + tid] = 0.f; lo[i * kSymNT + tid] = 0.f; }
+		int toff = 0;   // first record of the current tile within block bj
+
+		auto tile_fn = [&](const float4* __restrict__ st, int cnt) {
+			float2 acc[NR][2];
+#pragma unroll
+			for (int c = 0; c < NR; ++c) { acc[c][0] = make_float2(0.f, 0.f); acc[c][1] = acc[c][0]; }
+			const int ng = (cnt + 31) >> 5;
+			for (int g = 0; g < ng; ++g) {
+				const int gcnt = min(32, cnt - 32 * g);
+				const float4* grp = st + 2 * 32 * g;
+				float js[NR];
+#pragma unroll
+				for (int c = 0; c < NR; ++c) js[c] = 0.f;
+				if (gcnt == 32)
+					sym_group<R, VEL, DV, true>(rc, grp, gcnt, lane, tx, ty, tz, ax, ay, az,
+						nax, nay, naz, acc, js);
+				else
+					sym_group<R, VEL, DV, false>(rc, grp, gcnt, lane, tx, ty, tz, ax, ay, az,
+						nax, nay, naz, acc, js);
+				// the group's record sums are back at their home lanes
+				float* wb = jbuf + ((par * kSymWarps + warp) * NC) * 32;
+#pragma unroll
+				for (int c = 0; c < NC; ++c) wb[c * 32 + lane] = js[c];
+				__syncthreads();
+				// warp-ordered sum per record, accumulated over the passes
+				const float* rb = jbuf + (par * kSymWarps * NC) * 32;
+				for (int v = tid; v < NC * 32; v += kSymNT) {
+					const int c = v >> 5, l = v & 31;
+					if (l >= gcnt) continue;
+					float s = rb[v];
+#pragma unroll
+					for (int w = 1; w < kSymWarps; ++w) s += rb[w * NC * 32 + v];
+					float* slot = a.slots + (size_t(bi) * NC + c) * n + (j0 + toff + 32 * g + l);
+					*slot = first ? s : *slot + s;
+				}
+				par ^= 1;
+			}
+#pragma unroll
+			for (int c = 0; c < NC; ++c) {
+#pragma unroll
+				for (int h = 0; h < 2; ++h)
+#pragma unroll
+					for (int e = 0; e < 2; ++e) {
+						const int i = (c * kSymTPT + 2 * h + e) * kSymNT + tid;
+						float hh = hi[i], ll = lo[i];
+						fold_twosum(hh, ll, e == 0 ? acc[c][h].x : acc[c][h].y);
+						hi[i] = hh; lo[i] = ll;
+					}
+			}
+			toff += cnt;
+		};
+		if (!P3DStream::run_continue(smem, p.src, j0, nj, err, tcount, tile_fn)) return false;
+#pragma unroll
+		for (int k = 0; k < kSymTPT; ++k) {
+			const int t = tb + k * kSymNT + tid;
+#pragma unroll
+			for (int c = 0; c < NC; ++c) {
+				const int i = (c * kSymTPT + k) * kSymNT + tid;
+				a.slots[(size_t(bj) * NC + c) * n + t] = float(double(hi[i]) + double(lo[i]));
+			}
+		}
+	}
+	return true;
+}
+
+// Item `it` of nb blocks, largest first: the full off-diagonal pairs column
+// by column (bj = 1 .. nb-2, bi < bj; items running at the same time share
+// their bj block in L2), then the pairs with the short last block, then the
+// diagonal blocks (about 2/3 of an off-diagonal pair's time).
+__device__ __forceinline__ int2 sym_item_at(int it, int nb) {
+	const long long a = (long long)(nb - 1) * (nb - 2) / 2;
+	if (it < a) {
+		long long j = (long long)((1.0 + sqrt(1.0 + 8.0 * double(it))) * 0.5);
+		while (j * (j - 1) / 2 > it) --j;
+		while ((j + 1) * j / 2 <= it) ++j;
+		return make_int2(int(it - j * (j - 1) / 2), int(j));
+	}
+	if (it < a + nb - 1) return make_int2(int(it - a), nb - 1);
+	const int b = int(it - a - (nb - 1));
+	return make_int2(b, b);
+}
+
+template <Reg R, bool VEL, bool DV>
+__global__ void __launch_bounds__(kSymNT, kSymMinBlocks)
+p3d_sym_kernel(const P3DInduceProblem p, const InduceConsts kc, const SymArgs a,
+	int n_items, unsigned* next, unsigned* err)
+{
+	constexpr int NC = InduceNC<VEL, DV>::value;
+	extern __shared__ __align__(16) unsigned char smem[];
+	__shared__ int item_s;
+	if (blockDim.x != kSymNT) {
+		if (threadIdx.x == 0) atomicOr(err, kErrBadLaunch);
+		return;
+	}
+	if (!P3DStream::init(smem, err)) return;
+	unsigned tcount = 0;
+	const int n = p.n_tgt;
+	for (;;) {
+		if (threadIdx.x == 0) item_s = int(atomicAdd(next, 1u));
+		__syncthreads();
+		const int it = item_s;
+		__syncthreads();
+		if (it >= n_items) return;
+		const int2 w = sym_item_at(it, a.nb);
+		const int bi = w.x, bj = w.y;
+		if (bi < 0 || bj < bi || bj >= a.nb || bi * a.S >= n) {
+			if (threadIdx.x == 0) atomicOr(err, kErrBadWork);
+			continue;
+		}
+		if (bi == bj) {
+			const int b0 = bi * a.S;
+			const int b1 = min(n, b0 + a.S);
+			P3DInduceProblem q = p;
+			q.n_tgt = b1;      // targets of this block only; loads clamp below b1
+			for (int tb = b0; tb < b1; tb += kSymPass) {
+				const bool ok = induce2_block<R, VEL, DV, kSymTPT, kSymNT, 2>(q, kc, tb, b0, b1 - b0,
+					smem, err, tcount, [&](int t, const double* s) {
+#pragma unroll
+						for (int c = 0; c < NC; ++c)
+							a.slots[(size_t(bi) * NC + c) * n + t] = float(s[c]);
+					});
+				if (!ok) return;
+			}
+			continue;
+		}
+		if (!sym_item<R, VEL, DV>(p, kc, a, bi, bj, smem, err, tcount)) return;
+	}
+}
+
+// Sum of every particle's nb slot partials in block order (FP64), then the
+// output transforms.
+template <bool VEL, bool DV>
+__global__ void p3d_sym_finalize(const P3DInduceProblem p, const InduceConsts kc,
+	const float* __restrict__ slots, int nb)
+{
+	constexpr int NC = InduceNC<VEL, DV>::value;
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	const int n = p.n_tgt;
+	if (t >= n) return;
+	double s[NC];
+#pragma unroll
+	for (int c = 0; c < NC; ++c) s[c] = 0.0;
+	for (int b = 0; b < nb; ++b)
+#pragma unroll
+		for (int c = 0; c < NC; ++c) s[c] += double(slots[(size_t(b) * NC + c) * n + t]);
+	write_induce<VEL, DV>(p, kc, t, s);
+}
+
+template <Reg R, bool VEL, bool DV>
+int sym_occupancy() {
+	static const int occ = resident_ctas(p3d_sym_kernel<R, VEL, DV>, kSymNT,
+		sym_smem_bytes<VEL, DV>());
+	return occ;
+}
+
+// Block plan: about eight items per resident CTA (so that the last items
+// leave little of the GPU idle), blocks a multiple of the 512-particle pass,
+// and a workspace within `ws_cap` bytes (fewer, longer blocks otherwise).
+struct SymPlan {
+	int S = 0, nb = 0, n_items = 0;
+	size_t slots_bytes = 0, counter_off = 0, ws_bytes = 0;
+};
+
+SymPlan sym_plan(int n, int nc, int capacity, size_t ws_cap) {
+	SymPlan pl;
+	int nb = int(std::ceil(std::sqrt(16.0 * capacity)));
+	for (;; nb = nb * 7 / 8) {
+		nb = std::max(nb, 2);
+		int S = (n + nb - 1) / nb;
+		S = ((S + kSymPass - 1) / kSymPass) * kSymPass;
+		const int nbr = (n + S - 1) / S;
+		pl.S = S;
+		pl.nb = nbr;
+		pl.n_items = nbr * (nbr + 1) / 2;
+		pl.slots_bytes = size_t(nbr) * nc * size_t(n) * sizeof(float);
+		pl.slots_bytes = (pl.slots_bytes + 255) & ~size_t(255);
+		pl.counter_off = pl.slots_bytes;
+		pl.ws_bytes = pl.counter_off + 256;
+		if (pl.ws_bytes <= ws_cap || nb == 2) break;
+	}
+	return pl;
+}
+
+template <class F>
+auto with_reg_ops_sym(int reg, unsigned ops, F&& f) {
+	auto by_ops = [&](auto rt) {
+		if (ops == kOpVel) return f(rt, std::true_type{}, std::false_type{});
+		if (ops == kOpDvort) return f(rt, std::false_type{}, std::true_type{});
+		return f(rt, std::true_type{}, std::true_type{});
+	};
+	switch (reg) {
+	case 0: return by_ops(std::integral_constant<Reg, Reg::Singular>{});
+	case 1: return by_ops(std::integral_constant<Reg, Reg::Winckelmans>{});
+	case 2: return by_ops(std::integral_constant<Reg, Reg::Planetary>{});
+	default: return by_ops(std::integral_constant<Reg, Reg::Gaussian>{});
+	}
+}
+
+// Largest workspace the self-interaction form asks of its caller.
+constexpr size_t kSymWsCap = size_t(4) << 30;
+
+}  // namespace
+
+bool p3d_self_form_applies(int reg, unsigned ops, const P3DInduceProblem& p) {
+	(void)reg; (void)ops;
+	static const int min_n = [] {
+		const char* e = std::getenv("CVTX_GB300_SYM_MIN");
+		return (e && *e) ? std::atoi(e) : 32768;
+	}();
+	return min_n > 0 && p.tgt == p.src && p.tstride == 2 && p.n_tgt == p.n_src &&
+		p.n_tgt >= min_n && p.n_tgt >= 2 * kSymPass;
+}
+
+size_t p3d_self_ws_bytes(int reg, unsigned ops, int n, int num_sms, size_t ws_cap) {
+	return with_reg_ops_sym(reg, ops, [&](auto rt, auto vt, auto dt) {
+		constexpr Reg R = decltype(rt)::value;
+		constexpr bool VEL = decltype(vt)::value, DV = decltype(dt)::value;
+		return sym_plan(n, InduceNC<VEL, DV>::value, num_sms * sym_occupancy<R, VEL, DV>(),
+			ws_cap ? ws_cap : kSymWsCap).ws_bytes;
+	});
+}
+
+cudaError_t p3d_self(int reg, unsigned ops, const P3DInduceProblem& p, const LaunchEnv& env) {
+	return with_reg_ops_sym(reg, ops, [&](auto rt, auto vt, auto dt) {
+		constexpr Reg R = decltype(rt)::value;
+		constexpr bool VEL = decltype(vt)::value, DV = decltype(dt)::value;
+		constexpr int NC = InduceNC<VEL, DV>::value;
+		const int occ = sym_occupancy<R, VEL, DV>();
+		const SymPlan pl = sym_plan(p.n_tgt, NC, env.num_sms * occ,
+			env.cap_to_ws ? env.ws_bytes : std::min(env.ws_bytes, kSymWsCap));
+		if (pl.ws_bytes > env.ws_bytes || !env.ws) return cudaErrorInvalidValue;
+		unsigned char* ws = static_cast<unsigned char*>(env.ws);
+		unsigned* d_next = reinterpret_cast<unsigned*>(ws + pl.counter_off);
+		const cudaError_t e = cudaMemsetAsync(d_next, 0, sizeof(unsigned), env.stream);
+		if (e != cudaSuccess) return e;
+		SymArgs a;
+		a.S = pl.S;
+		a.nb = pl.nb;
+		a.slots = reinterpret_cast<float*>(ws);
+		const InduceConsts kc = make_induce_consts(reg, p.sigma);
+		const int grid = std::max(1, std::min(pl.n_items, env.num_sms * occ));
+		p3d_sym_kernel<R, VEL, DV><<<grid, kSymNT, sym_smem_bytes<VEL, DV>(), env.stream>>>(
+			p, kc, a, pl.n_items, d_next, env.err);
+		count_launch();
+		p3d_sym_finalize<VEL, DV><<<(p.n_tgt + 255) / 256, 256, 0, env.stream>>>(
+			p, kc, a.slots, pl.nb);
+		count_launch();
+		return cudaGetLastError();
+	});
+}
+
+}  // namespace cvtx

@@ -1,0 +1,92 @@
+"""Self-interaction form (each unordered pair once; csrc/p3d_sym.cu): the
+particles acting on themselves through the device API and through the cvtx_
+ABI (velocity at the particles' own coordinates, stretching with the pointer
+array as its own target array), for every regularisation and op, on ragged
+sizes, against the oracle on sampled targets and against the ordered-pair
+kernels (forced through the tuning table) on every target."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import REGS
+from cvortex_gb300 import abi, workloads
+from oracle import exact
+from parity import TOL, check
+
+pytestmark = pytest.mark.gpu
+
+OPS = {"vel": 1, "dvort": 2, "veldvort": 3}
+
+
+def _records(p):
+    r = np.zeros((len(p), 8), np.float32)
+    r[:, 0:3], r[:, 3], r[:, 4:7] = p["coord"], p["volume"], p["vorticity"]
+    return r
+
+
+def _dev(gpu, torch, rec, n, reg, ops):
+    v = torch.full((n, 3), float("nan"), dtype=torch.float32, device="cuda")
+    d = torch.full((n, 3), float("nan"), dtype=torch.float32, device="cuda")
+    sh = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert gpu.lib.cvtx_gb300_dev_P3D_M2M(rec.data_ptr(), n, rec.data_ptr(), 2, n,
+                                          v.data_ptr() if ops & 1 else None,
+                                          d.data_ptr() if ops & 2 else None,
+                                          abi.REG_IDS[reg], 0.05, sh) == 0
+    assert gpu.lib.cvtx_gb300_dev_status(sh) == 0
+    return (v.cpu().numpy() if ops & 1 else None), (d.cpu().numpy() if ops & 2 else None)
+
+
+@pytest.mark.parametrize("reg", REGS)
+@pytest.mark.parametrize("n", [33_001, 70_000])
+def test_self_form_vs_oracle_and_ordered_pairs(gpu, reg, n):
+    import torch
+    p = workloads.vortex_ring(n, seed=71) if n == 70_000 else workloads.uniform_cube(n, seed=72)
+    rec = torch.from_numpy(_records(p)).cuda()
+    idx = np.sort(np.random.Generator(np.random.PCG64(73)).choice(n, 1024, replace=False))
+    sub = p[idx].copy()
+    ref_v = oracle.p3d_vel(p, sub["coord"], reg, 0.05)
+    ref_d = oracle.p3d_dvort(p, sub, reg, 0.05)
+    bucket = gpu.lib.cvtx_gb300_size_bucket(n)
+    for name, ops in OPS.items():
+        v, d = _dev(gpu, torch, rec, n, reg, ops)
+        # the ordered-pair kernel: a tuned configuration switches the form off
+        assert gpu.lib.cvtx_gb300_p3d_set_tuned(abi.REG_IDS[reg], ops, bucket, 2) == 0
+        try:
+            v2, d2 = _dev(gpu, torch, rec, n, reg, ops)
+        finally:
+            gpu.lib.cvtx_gb300_p3d_set_tuned(abi.REG_IDS[reg], ops, bucket, -1)
+        if ops & 1:
+            check(v[idx], ref_v, reg, sub["coord"], p["coord"], 0.05)
+            assert exact.rel_l2(v, v2) <= 2e-6, (name, exact.rel_l2(v, v2))
+        if ops & 2:
+            check(d[idx], ref_d, reg, sub["coord"], p["coord"], 0.05)
+            assert exact.rel_l2(d, d2) <= 2e-6, (name, exact.rel_l2(d, d2))
+
+
+def test_self_form_through_the_abi(gpu):
+    """cvtx_P3D_M2M_vel at the particles' own coordinates and
+    cvtx_P3D_M2M_dvort with the pointer array as its own targets."""
+    p = workloads.uniform_cube(50_000, seed=74)
+    vel = gpu.p3d_vel(p, p["coord"].copy(), "winckelmans", 0.05)
+    dv = gpu.p3d_dvort(p, p, "winckelmans", 0.05, same=True)
+    idx = np.arange(0, len(p), 37)
+    sub = p[idx].copy()
+    check(vel[idx], oracle.p3d_vel(p, sub["coord"], "winckelmans", 0.05))
+    check(dv[idx], oracle.p3d_dvort(p, sub, "winckelmans", 0.05))
+    fv, fd = gpu.p3d_vel_dvort(p, "winckelmans", 0.05)
+    assert exact.rel_l2(fv, vel) <= 1e-6 and exact.rel_l2(fd, dv) <= 1e-6
+
+
+def test_self_form_coincident_particles(gpu):
+    """Distinct particles at one position contribute nothing to each other
+    (reference src/P3D.cpp:94-95) in the self-interaction form too."""
+    p = workloads.uniform_cube(40_000, seed=75)
+    p["coord"][20_000:20_100] = p["coord"][0]
+    vel, dv = gpu.p3d_vel_dvort(p, "singular", 0.05)
+    assert np.all(np.isfinite(vel)) and np.all(np.isfinite(dv))
+    idx = np.concatenate([np.arange(0, 40_000, 97), [0, 20_000, 20_050]])
+    sub = p[idx].copy()
+    check(vel[idx], oracle.p3d_vel(p, sub["coord"], "singular", 0.05))
+    check(dv[idx], oracle.p3d_dvort(p, sub, "singular", 0.05))
