@@ -67,7 +67,12 @@ OPS = {"veldvort": "fused vel+dvort", "vel": "vel", "dvort": "dvort",
        "vort": "vorticity field (5 sigma box cut-off)",
        "inf": "F3D influence matrix, 25,000 points x 20,000 filaments (2 GB)",
        "m2s": "few targets: fused vel+dvort of the first 64 particles from all sources",
-       "f3d_dvort": "F3D vortex stretching, wake sheet of N filaments on N particles"}
+       "f3d_dvort": "F3D vortex stretching, wake sheet of N filaments on N particles",
+       "visc": "P3D viscous exchange (nu 1e-3)",
+       "p2d_vel": "P2D velocity, Gaussian vortex patch of N particles",
+       "p2d_visc": "P2D viscous exchange (nu 1e-3), Gaussian vortex patch of N particles"}
+P2D_FLOPS = {("vel", 0): 10, ("vel", 1): 15, ("vel", 2): 10, ("vel", 3): 13,
+             ("visc", 1): 16, ("visc", 3): 10}
 M2S_TARGETS = 64
 F3D_DVORT_FLOPS = 62
 # influence matrix: F3D vel (51) + the dot with the direction (5) per entry
@@ -298,8 +303,12 @@ def run_ours(args):
     op = args.op
     if op == "vort" and reg not in VORT_FLOPS:
         raise SystemExit("--op vort: the singular vorticity field is zero (no kernel)")
+    if op in ("visc", "p2d_visc") and reg not in VISC_FLOPS:
+        raise SystemExit(f"--op {op}: only winckelmans and gaussian have a viscous kernel")
     flops_per = (VORT_FLOPS[reg] if op == "vort" else INF_FLOPS if op == "inf"
-                 else F3D_DVORT_FLOPS if op == "f3d_dvort"
+                 else F3D_DVORT_FLOPS if op == "f3d_dvort" else VISC_FLOPS[reg] if op == "visc"
+                 else P2D_FLOPS[("vel", reg)] if op == "p2d_vel"
+                 else P2D_FLOPS[("visc", reg)] if op == "p2d_visc"
                  else FLOPS[("veldvort", reg)] if op == "m2s" else FLOPS[(op, reg)])
     v_out = vel.data_ptr() if op in ("veldvort", "vel") else None
     d_out = dv.data_ptr() if op in ("veldvort", "dvort") else None
@@ -318,6 +327,10 @@ def run_ours(args):
         dirs[:, 2] = 1.0
         rfd, tfd, dd = (torch.from_numpy(x).cuda() for x in (rf, tf, dirs))
         om = torch.empty((nm, ni), dtype=torch.float32, device="cuda")
+    if op in ("p2d_vel", "p2d_visc"):
+        q = workloads.gaussian_patch_2d(n)
+        rq = torch.from_numpy(np.ascontiguousarray(
+            np.stack([q["coord"][:, 0], q["coord"][:, 1], q["vorticity"], q["area"]], 1))).cuda()
     if op == "f3d_dvort":
         fil = workloads.wake_sheet(n)
         rf = np.zeros((n, 8), np.float32)
@@ -338,6 +351,15 @@ def run_ours(args):
         elif op == "vort":
             rc = lib.cvtx_gb300_dev_P3D_M2M_vort(rec.data_ptr(), n, rec.data_ptr(), 2, n,
                                                  vel.data_ptr(), reg, SIGMA, sh)
+        elif op == "visc":
+            rc = lib.cvtx_gb300_dev_P3D_M2M_visc(rec.data_ptr(), n, rec.data_ptr(), 2, n,
+                                                 vel.data_ptr(), reg, SIGMA, 1e-3, sh)
+        elif op == "p2d_vel":
+            rc = lib.cvtx_gb300_dev_P2D_M2M_vel(rq.data_ptr(), n, rq.data_ptr(), n, vel.data_ptr(),
+                                                reg, SIGMA, sh)
+        elif op == "p2d_visc":
+            rc = lib.cvtx_gb300_dev_P2D_M2M_visc(rq.data_ptr(), n, rq.data_ptr(), n, vel.data_ptr(),
+                                                 reg, SIGMA, 1e-3, sh)
         else:
             rc = lib.cvtx_gb300_dev_P3D_M2M(rec.data_ptr(), n, rec.data_ptr(), 2, n, v_out, d_out,
                                             reg, SIGMA, sh)
@@ -383,8 +405,9 @@ def run_ours(args):
     achieved = flops / (kernel_ms * 1e-3) / 1e12
     if op == "inf":
         wl = OPS[op]
-    elif op == "f3d_dvort":
-        wl = OPS[op].replace("N ", f"{n} ")
+    elif op in ("f3d_dvort", "p2d_vel", "p2d_visc"):
+        wl = OPS[op].replace("N ", f"{n} ") + (f", {args.reg}, sigma={SIGMA}" if op != "f3d_dvort"
+                                                else "")
     else:
         wl = workload_name(args, op) + ("" if op in ("m2s", "veldvort") else ", targets = sources")
     out = {

@@ -26,7 +26,7 @@
 //   travel with it from lane to lane by shuffles and are back at their home
 //   lane after 32 steps. The four warps' sums per record are added in warp
 //   order in shared memory and accumulated over the passes into the
-//   workspace slot (bi, record). The bi particles' own sums are folded per
+//   workspace slot (bi, record) by reductions. The bi particles' own sums are folded per
 //   tile into compensated (hi, lo) pairs and written to slot (bj, particle)
 //   after the pass.
 // * Item (b, b): every ordered pair of the block by the per-call CTA body
@@ -150,6 +150,12 @@ __device__ __forceinline__ void sym_step(const RegConsts& rc, float4 sp, float4 
 	}
 }
 
+// Fire-and-forget add to global memory (no value returned, so the thread
+// does not wait for it).
+__device__ __forceinline__ void red_add_f32(float* p, float v) {
+	asm volatile("red.global.add.f32 [%0], %1;" :: "l"(p), "f"(v) : "memory");
+}
+
 // One 32-record group: 32 rotation steps; returns the group records' sums
 // at their home lanes in js.
 template <Reg R, bool VEL, bool DV, bool FULL>
@@ -198,7 +204,6 @@ __device__ __forceinline__ bool sym_item(const P3DInduceProblem& p, const Induce
 	const int nj = min(n, j0 + a.S) - j0;
 	int par = 0;
 	for (int tb = i0; tb < i0 + a.S; tb += kSymPass) {
-		const bool first = tb == i0;
 		float2 tx[2], ty[2], tz[2], ax[2], ay[2], az[2], nax[2], nay[2], naz[2];
 #pragma unroll
 		for (int h = 0; h < 2; ++h) {
@@ -238,7 +243,10 @@ __device__ __forceinline__ bool sym_item(const P3DInduceProblem& p, const Induce
 #pragma unroll
 				for (int c = 0; c < NC; ++c) wb[c * 32 + lane] = js[c];
 				__syncthreads();
-				// warp-ordered sum per record, accumulated over the passes
+				// warp-ordered sum per record, added to its slot (zeroed before
+				// the launch). A slot element is only ever added to by this
+				// thread of this CTA, in pass order, so the sum is
+				// deterministic; the reduction does not wait for the memory.
 				const float* rb = jbuf + (par * kSymWarps * NC) * 32;
 				for (int v = tid; v < NC * 32; v += kSymNT) {
 					const int c = v >> 5, l = v & 31;
@@ -246,8 +254,7 @@ __device__ __forceinline__ bool sym_item(const P3DInduceProblem& p, const Induce
 					float s = rb[v];
 #pragma unroll
 					for (int w = 1; w < kSymWarps; ++w) s += rb[w * NC * 32 + v];
-					float* slot = a.slots + (size_t(bi) * NC + c) * n + (j0 + toff + 32 * g + l);
-					*slot = first ? s : *slot + s;
+					red_add_f32(a.slots + (size_t(bi) * NC + c) * n + (j0 + toff + 32 * g + l), s);
 				}
 				par ^= 1;
 			}
@@ -447,7 +454,8 @@ cudaError_t p3d_self(int reg, unsigned ops, const P3DInduceProblem& p, const Lau
 		if (pl.ws_bytes > env.ws_bytes || !env.ws) return cudaErrorInvalidValue;
 		unsigned char* ws = static_cast<unsigned char*>(env.ws);
 		unsigned* d_next = reinterpret_cast<unsigned*>(ws + pl.counter_off);
-		const cudaError_t e = cudaMemsetAsync(d_next, 0, sizeof(unsigned), env.stream);
+		// the slots and the item counter start at zero
+		const cudaError_t e = cudaMemsetAsync(ws, 0, pl.ws_bytes, env.stream);
 		if (e != cudaSuccess) return e;
 		SymArgs a;
 		a.S = pl.S;
