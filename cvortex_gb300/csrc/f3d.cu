@@ -27,27 +27,49 @@ constexpr double kInv4Pi = 1.0 / (4.0 * 3.14159265358979323846);
 constexpr float kBig = 3.40282346e38f;
 constexpr float kInv4PiF = float(kInv4Pi);
 
-// Velocity induced at m by filament (s -> e) of strength gamma (including the
-// 1/(4 pi) factor, which the reference folds into t1 before its guard).
+// The reference's straight-segment factor t2 / |r1 x r2|^2 with
+// t2 = r0.r1/|r1| - r0.r2/|r2| (src/F3D.cpp:34-54), r1 = m - s, r2 = m - e,
+// r0 = r1 - r2, in whichever of two exact rewritings has no cancellation
+// for the pair (with q = |r|^2, d = r1.r2, l = |r|):
+//   d < 0:  t2 = (q1 - d)/l1 + (q2 - d)/l2           over |r1 x r2|^2
+//   d >= 0: t2 / |r1 x r2|^2 = (l1 + l2) / (l1 l2 (l1 l2 + d))
+// (|r1 x r2|^2 = (l1 l2 - d)(l1 l2 + d)). The reference's own form cancels
+// where the point is far from the segment or near the line beyond its ends,
+// which costs it up to about 1e-4 relative accuracy on single terms; these
+// forms keep every term to a few ulp. Returns the numerator and denominator;
+// the caller divides and drops the term when the quotient is not finite (a
+// point on the segment or at an end point, where the reference's term is
+// infinite or NaN and dropped too).
+__device__ __forceinline__ void f3d_factor(float q1, float q2, float d, float il1, float il2,
+	float cc, float& num, float& den)
+{
+	const float l1 = q1 * il1, l2 = q2 * il2;
+	const float L = l1 * l2;
+	const bool inner = d < 0.f;
+	num = inner ? fmaf(q1 - d, il1, (q2 - d) * il2) : l1 + l2;
+	den = inner ? cc : L * (L + d);
+}
+
+// Velocity induced at m by filament (s -> e) of strength gamma, including the
+// 1/(4 pi) factor (reference src/F3D.cpp:34-54); a term whose factor is not
+// finite is dropped, as the reference drops it.
 __device__ __forceinline__ void f3d_vel_pair(float mx, float my, float mz,
 	const float4 a, const float4 b, float& vx, float& vy, float& vz)
 {
 	const float r1x = mx - a.x, r1y = my - a.y, r1z = mz - a.z;
 	const float r2x = mx - b.x, r2y = my - b.y, r2z = mz - b.z;
-	const float r0x = r1x - r2x, r0y = r1y - r2y, r0z = r1z - r2z;
 	const float cx = fmaf(r1y, r2z, -r1z * r2y);
 	const float cy = fmaf(r1z, r2x, -r1x * r2z);
 	const float cz = fmaf(r1x, r2y, -r1y * r2x);
 	const float cc = fmaf(cz, cz, fmaf(cy, cy, cx * cx));
-	const float t1 = (a.w * kInv4PiF) / cc;
-	const float l1 = rsqrt_approx(fmaf(r1z, r1z, fmaf(r1y, r1y, r1x * r1x)));
-	const float l2 = rsqrt_approx(fmaf(r2z, r2z, fmaf(r2y, r2y, r2x * r2x)));
-	const float t21 = fmaf(r1z, r0z, fmaf(r1y, r0y, r1x * r0x)) * l1;
-	const float t22 = fmaf(r2z, r0z, fmaf(r2y, r0y, r2x * r0x)) * l2;
-	const float t2 = t21 - t22;
-	// |t1| <= FLT_MAX and |t2| <= FLT_MAX; NaN fails both tests.
-	const bool ok = fabsf(t1) <= kBig && fabsf(t2) <= kBig;
-	const float f = ok ? t1 * t2 : 0.f;
+	const float q1 = fmaf(r1z, r1z, fmaf(r1y, r1y, r1x * r1x));
+	const float q2 = fmaf(r2z, r2z, fmaf(r2y, r2y, r2x * r2x));
+	const float d = fmaf(r1z, r2z, fmaf(r1y, r2y, r1x * r2x));
+	float num, den;
+	f3d_factor(q1, q2, d, rsqrt_approx(q1), rsqrt_approx(q2), cc, num, den);
+	const float f = (a.w * kInv4PiF) * num / den;
+	// |f| <= FLT_MAX; NaN fails
+	const bool ok = fabsf(f) <= kBig;
 	vx = ok ? cx * f : 0.f;
 	vy = ok ? cy * f : 0.f;
 	vz = ok ? cz * f : 0.f;
@@ -128,9 +150,22 @@ f3d_vel_kernel(const F3DVelProblem p, double* __restrict__ partial, int src_per_
 
 __device__ __forceinline__ float2 neg2f(float2 a) { return make_float2(-a.x, -a.y); }
 
+// f3d_factor for two points at once (per lane).
+__device__ __forceinline__ void f3d_factor2(float2 q1, float2 q2, float2 d, float2 il1,
+	float2 il2, float2 cc, float2& num, float2& den)
+{
+	const float2 l1 = __fmul2_rn(q1, il1), l2 = __fmul2_rn(q2, il2);
+	const float2 L = __fmul2_rn(l1, l2);
+	const float2 nd = neg2f(d);
+	const float2 na = __ffma2_rn(__fadd2_rn(q1, nd), il1, __fmul2_rn(__fadd2_rn(q2, nd), il2));
+	const float2 nb = __fadd2_rn(l1, l2);
+	const float2 db = __fmul2_rn(L, __fadd2_rn(L, d));
+	num = make_float2(d.x < 0.f ? na.x : nb.x, d.y < 0.f ? na.y : nb.y);
+	den = make_float2(d.x < 0.f ? cc.x : db.x, d.y < 0.f ? cc.y : db.y);
+}
+
 // f3d_vel_pair for two measurement points at once (f32x2), with the
-// division by |r1 x r2|^2 done as a reciprocal refined by one Newton step;
-// same guards.
+// division done as a reciprocal refined by one Newton step; same guard.
 __device__ __forceinline__ void f3d_vel_pair2(float2 mx, float2 my, float2 mz,
 	const float4 a, const float4 b, float2& vx, float2& vy, float2& vz)
 {
@@ -138,25 +173,20 @@ __device__ __forceinline__ void f3d_vel_pair2(float2 mx, float2 my, float2 mz,
 	const float2 r1z = __fadd2_rn(mz, bc2(-a.z));
 	const float2 r2x = __fadd2_rn(mx, bc2(-b.x)), r2y = __fadd2_rn(my, bc2(-b.y));
 	const float2 r2z = __fadd2_rn(mz, bc2(-b.z));
-	const float2 r0x = __fadd2_rn(r1x, neg2f(r2x)), r0y = __fadd2_rn(r1y, neg2f(r2y));
-	const float2 r0z = __fadd2_rn(r1z, neg2f(r2z));
 	const float2 cx = __ffma2_rn(r1y, r2z, neg2f(__fmul2_rn(r1z, r2y)));
 	const float2 cy = __ffma2_rn(r1z, r2x, neg2f(__fmul2_rn(r1x, r2z)));
 	const float2 cz = __ffma2_rn(r1x, r2y, neg2f(__fmul2_rn(r1y, r2x)));
 	const float2 cc = __ffma2_rn(cz, cz, __ffma2_rn(cy, cy, __fmul2_rn(cx, cx)));
-	const float2 t1 = __fmul2_rn(bc2(a.w * kInv4PiF), rcp2(cc));
 	const float2 q1 = __ffma2_rn(r1z, r1z, __ffma2_rn(r1y, r1y, __fmul2_rn(r1x, r1x)));
 	const float2 q2 = __ffma2_rn(r2z, r2z, __ffma2_rn(r2y, r2y, __fmul2_rn(r2x, r2x)));
-	const float2 l1 = make_float2(rsqrt_approx(q1.x), rsqrt_approx(q1.y));
-	const float2 l2 = make_float2(rsqrt_approx(q2.x), rsqrt_approx(q2.y));
-	const float2 t21 = __fmul2_rn(__ffma2_rn(r1z, r0z, __ffma2_rn(r1y, r0y, __fmul2_rn(r1x, r0x))), l1);
-	const float2 t22 = __fmul2_rn(__ffma2_rn(r2z, r0z, __ffma2_rn(r2y, r0y, __fmul2_rn(r2x, r0x))), l2);
-	const float2 t2 = __fadd2_rn(t21, neg2f(t22));
-	const bool okx = fabsf(t1.x) <= kBig && fabsf(t2.x) <= kBig;
-	const bool oky = fabsf(t1.y) <= kBig && fabsf(t2.y) <= kBig;
-	float2 f = __fmul2_rn(t1, t2);
-	f.x = okx ? f.x : 0.f;
-	f.y = oky ? f.y : 0.f;
+	const float2 d = __ffma2_rn(r1z, r2z, __ffma2_rn(r1y, r2y, __fmul2_rn(r1x, r2x)));
+	const float2 il1 = make_float2(rsqrt_approx(q1.x), rsqrt_approx(q1.y));
+	const float2 il2 = make_float2(rsqrt_approx(q2.x), rsqrt_approx(q2.y));
+	float2 num, den;
+	f3d_factor2(q1, q2, d, il1, il2, cc, num, den);
+	const float2 f = __fmul2_rn(__fmul2_rn(bc2(a.w * kInv4PiF), num), rcp2(den));
+	const bool okx = fabsf(f.x) <= kBig;
+	const bool oky = fabsf(f.y) <= kBig;
 	vx = __fmul2_rn(cx, f);
 	vy = __fmul2_rn(cy, f);
 	vz = __fmul2_rn(cz, f);
@@ -251,10 +281,14 @@ f3d_vel2_kernel(const F3DVelProblem p, double* __restrict__ partial, int src_per
 
 // Vortex stretching of particle (x, alpha) by filament (s -> e), strength g,
 // without the 1/(4 pi) factor (reference src/F3D.cpp:56-85):
-//   r1 = x - s, r2 = x - e, r0 = r1 - r2, X = |r1 x r0|
+//   r1 = x - s, r2 = x - e, r0 = r1 - r2, X = |r1 x r0| (= |r1 x r2|)
 //   A = -r0 / X^2 * g * (r0.r1/|r1| - r0.r2/|r2|)
 //   B = 3/|r0| * g * (X/|r1| - X/|r2|)
 //   out = B alpha + A x alpha
+// The factor of A is the velocity factor t2 / X^2, evaluated as f3d_factor
+// does. A particle exactly on the filament's line (X = 0), where the
+// reference's term is infinite or NaN, has its term dropped, as has any term
+// that is not finite.
 __device__ __forceinline__ void f3d_dvort_pair(float px, float py, float pz,
 	float wx, float wy, float wz, const float4 a, const float4 b,
 	float& ox, float& oy, float& oz)
@@ -267,19 +301,22 @@ __device__ __forceinline__ void f3d_dvort_pair(float px, float py, float pz,
 	const float xz = fmaf(r1x, r0y, -r1y * r0x);
 	const float X2 = fmaf(xz, xz, fmaf(xy, xy, xx * xx));
 	const float X = sqrtf(X2);
-	const float il1 = rsqrt_approx(fmaf(r1z, r1z, fmaf(r1y, r1y, r1x * r1x)));
-	const float il2 = rsqrt_approx(fmaf(r2z, r2z, fmaf(r2y, r2y, r2x * r2x)));
+	const float q1 = fmaf(r1z, r1z, fmaf(r1y, r1y, r1x * r1x));
+	const float q2 = fmaf(r2z, r2z, fmaf(r2y, r2y, r2x * r2x));
+	const float d = fmaf(r1z, r2z, fmaf(r1y, r2y, r1x * r2x));
+	const float il1 = rsqrt_approx(q1);
+	const float il2 = rsqrt_approx(q2);
 	const float il0 = rsqrt_approx(fmaf(r0z, r0z, fmaf(r0y, r0y, r0x * r0x)));
-	const float t212 = fmaf(r0z, r1z, fmaf(r0y, r1y, r0x * r1x)) * il1
-		- fmaf(r0z, r2z, fmaf(r0y, r2y, r0x * r2x)) * il2;
-	const float t222 = X * il1 - X * il2;
-	const float kA = -a.w * t212 / X2;
+	float num, den;
+	f3d_factor(q1, q2, d, il1, il2, X2, num, den);
+	const float kA = -a.w * num / den;
 	const float Ax = r0x * kA, Ay = r0y * kA, Az = r0z * kA;
+	const float t222 = X * il1 - X * il2;
 	const float B = 3.f * il0 * a.w * t222;
 	const float vx = fmaf(wx, B, fmaf(Ay, wz, -Az * wy));
 	const float vy = fmaf(wy, B, fmaf(Az, wx, -Ax * wz));
 	const float vz = fmaf(wz, B, fmaf(Ax, wy, -Ay * wx));
-	const bool ok = (vx == vx) && (vy == vy) && (vz == vz) && (t222 == t222) && (t212 == t212);
+	const bool ok = X2 > 0.f && fabsf(vx) <= kBig && fabsf(vy) <= kBig && fabsf(vz) <= kBig;
 	ox = ok ? vx : 0.f;
 	oy = ok ? vy : 0.f;
 	oz = ok ? vz : 0.f;
@@ -288,10 +325,8 @@ __device__ __forceinline__ void f3d_dvort_pair(float px, float py, float pz,
 // f3d_dvort_pair for two particles at once (f32x2). `c` holds what depends
 // on the filament alone, computed once per staged tile: r0 = e - s (the
 // reference forms r1 - r2 per pair; the two differ by rounding) and
-// 3 g / |r0|. |r1 x r0| comes from X2 * rsqrt(X2) and 1/X2 from the square of
-// that rsqrt. The terms the reference keeps are kept with the same value to
-// rounding; a particle exactly on the filament's line (X2 = 0, where the
-// reference's term is infinite or NaN) has its term dropped.
+// 3 g / |r0|. |r1 x r0| comes from X2 * rsqrt(X2); the factor of A from
+// f3d_factor2 with a Newton-refined reciprocal.
 __device__ __forceinline__ void f3d_dvort_pair2(float2 px, float2 py, float2 pz,
 	float2 wx, float2 wy, float2 wz, const float4 a, const float4 b, const float4 c,
 	float2& ox, float2& oy, float2& oz)
@@ -309,22 +344,22 @@ __device__ __forceinline__ void f3d_dvort_pair2(float2 px, float2 py, float2 pz,
 	const float2 X = __fmul2_rn(X2, iX);
 	const float2 q1 = __ffma2_rn(r1z, r1z, __ffma2_rn(r1y, r1y, __fmul2_rn(r1x, r1x)));
 	const float2 q2 = __ffma2_rn(r2z, r2z, __ffma2_rn(r2y, r2y, __fmul2_rn(r2x, r2x)));
+	const float2 d = __ffma2_rn(r1z, r2z, __ffma2_rn(r1y, r2y, __fmul2_rn(r1x, r2x)));
 	const float2 il1 = make_float2(rsqrt_approx(q1.x), rsqrt_approx(q1.y));
 	const float2 il2 = make_float2(rsqrt_approx(q2.x), rsqrt_approx(q2.y));
-	const float2 d1 = __fmul2_rn(__ffma2_rn(r0z, r1z, __ffma2_rn(r0y, r1y, __fmul2_rn(r0x, r1x))), il1);
-	const float2 d2 = __fmul2_rn(__ffma2_rn(r0z, r2z, __ffma2_rn(r0y, r2y, __fmul2_rn(r0x, r2x))), il2);
-	const float2 t212 = __fadd2_rn(d1, neg2f(d2));
+	float2 num, den;
+	f3d_factor2(q1, q2, d, il1, il2, X2, num, den);
 	const float2 t222 = __fmul2_rn(X, __fadd2_rn(il1, neg2f(il2)));
-	const float2 kA = __fmul2_rn(__fmul2_rn(bc2(-a.w), t212), __fmul2_rn(iX, iX));
+	const float2 kA = __fmul2_rn(__fmul2_rn(bc2(-a.w), num), rcp2(den));
 	const float2 Ax = __fmul2_rn(r0x, kA), Ay = __fmul2_rn(r0y, kA), Az = __fmul2_rn(r0z, kA);
 	const float2 B = __fmul2_rn(bc2(c.w), t222);
 	const float2 vx = __ffma2_rn(wx, B, __ffma2_rn(Ay, wz, neg2f(__fmul2_rn(Az, wy))));
 	const float2 vy = __ffma2_rn(wy, B, __ffma2_rn(Az, wx, neg2f(__fmul2_rn(Ax, wz))));
 	const float2 vz = __ffma2_rn(wz, B, __ffma2_rn(Ax, wy, neg2f(__fmul2_rn(Ay, wx))));
-	const bool okx = X2.x > 0.f && (vx.x == vx.x) && (vy.x == vy.x) && (vz.x == vz.x) &&
-		(t222.x == t222.x) && (t212.x == t212.x);
-	const bool oky = X2.y > 0.f && (vx.y == vx.y) && (vy.y == vy.y) && (vz.y == vz.y) &&
-		(t222.y == t222.y) && (t212.y == t212.y);
+	const bool okx = X2.x > 0.f && fabsf(vx.x) <= kBig && fabsf(vy.x) <= kBig &&
+		fabsf(vz.x) <= kBig;
+	const bool oky = X2.y > 0.f && fabsf(vx.y) <= kBig && fabsf(vy.y) <= kBig &&
+		fabsf(vz.y) <= kBig;
 	ox = make_float2(okx ? vx.x : 0.f, oky ? vx.y : 0.f);
 	oy = make_float2(okx ? vy.x : 0.f, oky ? vy.y : 0.f);
 	oz = make_float2(okx ? vz.x : 0.f, oky ? vz.y : 0.f);
@@ -566,11 +601,8 @@ template <int PAIRS> constexpr int inf_rows() { return 8 * 2 * PAIRS; }
 
 // One influence entry per lane: dir . (velocity of filament a -> b at m), the
 // terms of f3d_vel_pair2 with the direction dotted in before the guard, so
-// one test and one select drop a non-finite term (the reference tests t1 and
-// t2 separately, src/F3D.cpp:51-52; the single test on t1 t2 differs only
-// where two finite factors overflow, when the reference's entry is not finite
-// either). ga = gamma / (4 pi). Differences are formed as fma(x, -1, y): one
-// rounding, as y - x.
+// one test and one select drop a non-finite term. ga = gamma / (4 pi).
+// Differences are formed as fma(x, -1, y): one rounding, as y - x.
 // One filament's operands, each held twice (one per point of a lane pair).
 struct InfFil2 { float2 ax, ay, az, bx, by, bz, ga; };
 
@@ -582,23 +614,21 @@ __device__ __forceinline__ float2 f3d_inf_pair2(float2 mx, float2 my, float2 mz,
 	const float2 r1z = __ffma2_rn(f2.az, m1, mz);
 	const float2 r2x = __ffma2_rn(f2.bx, m1, mx), r2y = __ffma2_rn(f2.by, m1, my);
 	const float2 r2z = __ffma2_rn(f2.bz, m1, mz);
-	const float2 r0x = __ffma2_rn(r2x, m1, r1x), r0y = __ffma2_rn(r2y, m1, r1y);
-	const float2 r0z = __ffma2_rn(r2z, m1, r1z);
 	const float2 cx = __ffma2_rn(r1y, r2z, neg2f(__fmul2_rn(r1z, r2y)));
 	const float2 cy = __ffma2_rn(r1z, r2x, neg2f(__fmul2_rn(r1x, r2z)));
 	const float2 cz = __ffma2_rn(r1x, r2y, neg2f(__fmul2_rn(r1y, r2x)));
 	const float2 cc = __ffma2_rn(cz, cz, __ffma2_rn(cy, cy, __fmul2_rn(cx, cx)));
 	const float2 q1 = __ffma2_rn(r1z, r1z, __ffma2_rn(r1y, r1y, __fmul2_rn(r1x, r1x)));
 	const float2 q2 = __ffma2_rn(r2z, r2z, __ffma2_rn(r2y, r2y, __fmul2_rn(r2x, r2x)));
-	const float2 l1 = make_float2(rsqrt_approx(q1.x), rsqrt_approx(q1.y));
-	const float2 l2 = make_float2(rsqrt_approx(q2.x), rsqrt_approx(q2.y));
-	const float2 t21 = __fmul2_rn(__ffma2_rn(r1z, r0z, __ffma2_rn(r1y, r0y, __fmul2_rn(r1x, r0x))), l1);
-	const float2 t22 = __fmul2_rn(__ffma2_rn(r2z, r0z, __ffma2_rn(r2y, r0y, __fmul2_rn(r2x, r0x))), l2);
-	const float2 t2 = __ffma2_rn(t22, m1, t21);
-	const float2 f = __fmul2_rn(__fmul2_rn(f2.ga, rcp2(cc)), t2);
+	const float2 d = __ffma2_rn(r1z, r2z, __ffma2_rn(r1y, r2y, __fmul2_rn(r1x, r2x)));
+	const float2 il1 = make_float2(rsqrt_approx(q1.x), rsqrt_approx(q1.y));
+	const float2 il2 = make_float2(rsqrt_approx(q2.x), rsqrt_approx(q2.y));
+	float2 num, den;
+	f3d_factor2(q1, q2, d, il1, il2, cc, num, den);
+	const float2 f = __fmul2_rn(__fmul2_rn(f2.ga, num), rcp2(den));
 	const float2 cd = __ffma2_rn(cz, ez, __ffma2_rn(cy, ey, __fmul2_rn(cx, ex)));
 	float2 r = __fmul2_rn(f, cd);
-	// |t1 t2| <= FLT_MAX; NaN fails
+	// |f| <= FLT_MAX; NaN fails
 	r.x = fabsf(f.x) <= kBig ? r.x : 0.f;
 	r.y = fabsf(f.y) <= kBig ? r.y : 0.f;
 	return r;

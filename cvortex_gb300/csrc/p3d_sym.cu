@@ -52,7 +52,6 @@ constexpr int kSymNT = 128;                    // threads per CTA
 constexpr int kSymTPT = 4;                     // particles per thread and pass
 constexpr int kSymPass = kSymNT * kSymTPT;     // particles of block bi per pass
 constexpr int kSymWarps = kSymNT / 32;
-constexpr int kSymMinBlocks = 3;               // resident CTAs per SM
 
 template <bool VEL, bool DV> struct SymNR {
 	// register sums per particle: vel 3 (u); dvort 6 (A, B); fused 9
@@ -157,8 +156,10 @@ __device__ __forceinline__ void red_add_f32(float* p, float v) {
 }
 
 // One 32-record group: 32 rotation steps; returns the group records' sums
-// at their home lanes in js.
-template <Reg R, bool VEL, bool DV, bool FULL>
+// at their home lanes in js. ROT: the records' data travel with their sums
+// by shuffles (read from shared memory once per group) instead of being
+// read from shared memory at every step.
+template <Reg R, bool VEL, bool DV, bool FULL, bool ROT>
 __device__ __forceinline__ void sym_group(const RegConsts& rc, const float4* __restrict__ grp,
 	int gcnt, int lane,
 	const float2 (&tx)[2], const float2 (&ty)[2], const float2 (&tz)[2],
@@ -168,15 +169,28 @@ __device__ __forceinline__ void sym_group(const RegConsts& rc, const float4* __r
 {
 	constexpr int NR = SymNR<VEL, DV>::value;
 	const int from = (lane + 1) & 31;
+	float4 rp = make_float4(0.f, 0.f, 0.f, 0.f), rv = rp;
+	if (ROT) {
+		rp = grp[2 * lane];
+		rv = grp[2 * lane + 1];
+	}
 #pragma unroll 2
 	for (int k = 0; k < 32; ++k) {
 		const int jl = (lane + k) & 31;
-		const float4 sp = grp[2 * jl];
-		const float4 sv = grp[2 * jl + 1];
+		const float4 sp = ROT ? rp : grp[2 * jl];
+		const float4 sv = ROT ? rv : grp[2 * jl + 1];
 		sym_step<R, VEL, DV, FULL>(rc, sp, sv, jl < gcnt, tx, ty, tz, ax, ay, az, nax, nay, naz,
 			acc, js);
 #pragma unroll
 		for (int c = 0; c < NR; ++c) js[c] = __shfl_sync(0xffffffffu, js[c], from);
+		if (ROT) {
+			rp.x = __shfl_sync(0xffffffffu, rp.x, from);
+			rp.y = __shfl_sync(0xffffffffu, rp.y, from);
+			rp.z = __shfl_sync(0xffffffffu, rp.z, from);
+			rv.x = __shfl_sync(0xffffffffu, rv.x, from);
+			rv.y = __shfl_sync(0xffffffffu, rv.y, from);
+			rv.z = __shfl_sync(0xffffffffu, rv.z, from);
+		}
 	}
 }
 
@@ -187,7 +201,7 @@ struct SymArgs {
 };
 
 // Item (bi, bj), bi < bj: all passes of block bi against block bj.
-template <Reg R, bool VEL, bool DV>
+template <Reg R, bool VEL, bool DV, bool ROT>
 __device__ __forceinline__ bool sym_item(const P3DInduceProblem& p, const InduceConsts& kc,
 	const SymArgs& a, int bi, int bj, unsigned char* smem, unsigned* err, unsigned& tcount)
 {
@@ -233,10 +247,10 @@ __device__ __forceinline__ bool sym_item(const P3DInduceProblem& p, const Induce
 #pragma unroll
 				for (int c = 0; c < NR; ++c) js[c] = 0.f;
 				if (gcnt == 32)
-					sym_group<R, VEL, DV, true>(rc, grp, gcnt, lane, tx, ty, tz, ax, ay, az,
+					sym_group<R, VEL, DV, true, ROT>(rc, grp, gcnt, lane, tx, ty, tz, ax, ay, az,
 						nax, nay, naz, acc, js);
 				else
-					sym_group<R, VEL, DV, false>(rc, grp, gcnt, lane, tx, ty, tz, ax, ay, az,
+					sym_group<R, VEL, DV, false, ROT>(rc, grp, gcnt, lane, tx, ty, tz, ax, ay, az,
 						nax, nay, naz, acc, js);
 				// the group's record sums are back at their home lanes
 				float* wb = jbuf + ((par * kSymWarps + warp) * NC) * 32;
@@ -303,8 +317,8 @@ __device__ __forceinline__ int2 sym_item_at(int it, int nb) {
 	return make_int2(b, b);
 }
 
-template <Reg R, bool VEL, bool DV>
-__global__ void __launch_bounds__(kSymNT, kSymMinBlocks)
+template <Reg R, bool VEL, bool DV, bool ROT, int MINB>
+__global__ void __launch_bounds__(kSymNT, MINB)
 p3d_sym_kernel(const P3DInduceProblem p, const InduceConsts kc, const SymArgs a,
 	int n_items, unsigned* next, unsigned* err)
 {
@@ -346,7 +360,7 @@ p3d_sym_kernel(const P3DInduceProblem p, const InduceConsts kc, const SymArgs a,
 			}
 			continue;
 		}
-		if (!sym_item<R, VEL, DV>(p, kc, a, bi, bj, smem, err, tcount)) return;
+		if (!sym_item<R, VEL, DV, ROT>(p, kc, a, bi, bj, smem, err, tcount)) return;
 	}
 }
 
@@ -369,10 +383,31 @@ __global__ void p3d_sym_finalize(const P3DInduceProblem p, const InduceConsts kc
 	write_induce<VEL, DV>(p, kc, t, s);
 }
 
+// Kernel variants: (ROT, resident CTAs per SM the registers are sized for).
+// CVTX_GB300_SYM_VARIANT selects one: 0 (false, 3), 1 (true, 3), 2 (true, 2).
+int sym_variant() {
+	static const int v = [] {
+		const char* e = std::getenv("CVTX_GB300_SYM_VARIANT");
+		const int x = (e && *e) ? std::atoi(e) : 0;
+		return (x >= 0 && x <= 2) ? x : 0;
+	}();
+	return v;
+}
+
+template <Reg R, bool VEL, bool DV, class F>
+auto with_sym_variant(F&& f) {
+	switch (sym_variant()) {
+	case 1: return f(p3d_sym_kernel<R, VEL, DV, true, 3>);
+	case 2: return f(p3d_sym_kernel<R, VEL, DV, true, 2>);
+	default: return f(p3d_sym_kernel<R, VEL, DV, false, 3>);
+	}
+}
+
 template <Reg R, bool VEL, bool DV>
 int sym_occupancy() {
-	static const int occ = resident_ctas(p3d_sym_kernel<R, VEL, DV>, kSymNT,
-		sym_smem_bytes<VEL, DV>());
+	static const int occ = with_sym_variant<R, VEL, DV>([](auto k) {
+		return resident_ctas(k, kSymNT, sym_smem_bytes<VEL, DV>());
+	});
 	return occ;
 }
 
@@ -463,8 +498,11 @@ cudaError_t p3d_self(int reg, unsigned ops, const P3DInduceProblem& p, const Lau
 		a.slots = reinterpret_cast<float*>(ws);
 		const InduceConsts kc = make_induce_consts(reg, p.sigma);
 		const int grid = std::max(1, std::min(pl.n_items, env.num_sms * occ));
-		p3d_sym_kernel<R, VEL, DV><<<grid, kSymNT, sym_smem_bytes<VEL, DV>(), env.stream>>>(
-			p, kc, a, pl.n_items, d_next, env.err);
+		with_sym_variant<R, VEL, DV>([&](auto k) {
+			k<<<grid, kSymNT, sym_smem_bytes<VEL, DV>(), env.stream>>>(
+				p, kc, a, pl.n_items, d_next, env.err);
+			return 0;
+		});
 		count_launch();
 		p3d_sym_finalize<VEL, DV><<<(p.n_tgt + 255) / 256, 256, 0, env.stream>>>(
 			p, kc, a.slots, pl.nb);
