@@ -32,7 +32,7 @@ namespace {
 
 constexpr int kParallelGather = 32768;
 // Velocity calls with at least this many points compare the points with the
-// sources' coordinates (self-interaction form below that is not used).
+// sources' coordinates, to use the source records as the targets.
 constexpr int kSelfCheckMin = 32768;
 
 void gather_p3d_host(const cvtx_P3D* const* src, int n, float4* out) {
@@ -148,7 +148,8 @@ bool gpu_usable(const cvtx_VortFunc* k, int* reg) {
 // P3D induced velocity and/or stretching. Targets are either points (mes) or
 // particles (ind); when ind is the source pointer array itself, or the
 // points are the sources' own coordinates, the source records double as
-// target records (and the self-interaction form can apply).
+// target records (no target upload; with the stretching, the
+// self-interaction form can apply).
 int gpu_p3d_induce(const char* what, const cvtx_P3D** src, int n, const bsv_V3f* mes,
 	const cvtx_P3D** ind, int m, bsv_V3f* vel, bsv_V3f* dvort, int reg, float sigma)
 {

@@ -196,28 +196,13 @@ p2d_vel2_kernel(const P2DVelProblem p, const RegConsts rc, double scale,
 	}
 }
 
-// Viscous exchange (reference src/P2D.cpp:167-194):
-//   out_t = S sum_s eta_s (Gamma_s A_t - Gamma_t A_s)
-//         = S (A_t sum_s eta_s Gamma_s - Gamma_t sum_s eta_s A_s),
-// accumulated as the two sums per target (compensated across tiles) and
-// combined once per target in FP64: two multiply-adds per pair, and the
-// cancellation between the two parts happens once, in FP64, instead of in
-// every FP32 term and partial sum.
-constexpr int kViscNC = 2;
-
-__device__ __forceinline__ void write_visc2d(const P2DViscProblem& p, int t, double scale,
-	double sg, double sa)
-{
-	const float4 tp = p.tgt[t];
-	p.out[t] = float(scale * (double(tp.w) * sg - double(tp.z) * sa));
-}
-
+// Viscous exchange: out = S * sum_s Es (Gamma_s A_t - Gamma_t A_s).
 template <Reg R, int TPT, int NT>
 __global__ void __launch_bounds__(NT)
 p2d_visc_kernel(const P2DViscProblem p, const RegConsts rc, double scale,
 	double* __restrict__ partial, int src_per_split, unsigned* err)
 {
-	constexpr int NC = kViscNC;
+	constexpr int NC = 1;
 	extern __shared__ __align__(16) unsigned char smem[];
 	float* hi = reinterpret_cast<float*>(smem + Stream1::kSmemBytes);
 	float* lo = hi + NC * TPT * NT;
@@ -227,20 +212,20 @@ p2d_visc_kernel(const P2DViscProblem p, const RegConsts rc, double scale,
 	int n_s = p.n_src - s_begin;
 	n_s = n_s < src_per_split ? n_s : src_per_split;
 	n_s = n_s > 0 ? n_s : 0;
-	float tx[TPT], ty[TPT];
+	float tx[TPT], ty[TPT], tg[TPT], ta[TPT];
 #pragma unroll
 	for (int k = 0; k < TPT; ++k) {
 		int t = tbase + k * NT + tid;
 		t = t < p.n_tgt ? t : p.n_tgt - 1;
 		const float4 tp = p.tgt[t];
-		tx[k] = tp.x; ty[k] = tp.y;
+		tx[k] = tp.x; ty[k] = tp.y; tg[k] = tp.z; ta[k] = tp.w;
 	}
 #pragma unroll
 	for (int i = 0; i < NC * TPT; ++i) { hi[i * NT + tid] = 0.f; lo[i * NT + tid] = 0.f; }
 	auto tile_fn = [&](const float4* __restrict__ st, int cnt) {
-		float ag[TPT], aa[TPT];
+		float acc[TPT];
 #pragma unroll
-		for (int k = 0; k < TPT; ++k) { ag[k] = 0.f; aa[k] = 0.f; }
+		for (int k = 0; k < TPT; ++k) acc[k] = 0.f;
 		auto body = [&](int j) {
 			const float4 s = st[j];
 #pragma unroll
@@ -250,8 +235,8 @@ p2d_visc_kernel(const P2DViscProblem p, const RegConsts rc, double scale,
 				const float r2 = fmaf(dy, dy, dx * dx);
 				float e = RegP2D<R>::eta(r2, rc);
 				e = r2 > 0.f ? e : 0.f;
-				ag[k] = fmaf(e, s.z, ag[k]);
-				aa[k] = fmaf(e, s.w, aa[k]);
+				const float w = fmaf(s.z, ta[k], -tg[k] * s.w);
+				acc[k] = fmaf(e, w, acc[k]);
 			}
 		};
 		if (cnt == kTile) {
@@ -263,13 +248,10 @@ p2d_visc_kernel(const P2DViscProblem p, const RegConsts rc, double scale,
 		}
 #pragma unroll
 		for (int k = 0; k < TPT; ++k) {
-#pragma unroll
-			for (int c = 0; c < NC; ++c) {
-				const int i = (c * TPT + k) * NT + tid;
-				float h = hi[i], l = lo[i];
-				fold_twosum(h, l, c == 0 ? ag[k] : aa[k]);
-				hi[i] = h; lo[i] = l;
-			}
+			const int i = k * NT + tid;
+			float h = hi[i], l = lo[i];
+			fold_twosum(h, l, acc[k]);
+			hi[i] = h; lo[i] = l;
 		}
 	};
 	if (!Stream1::run(smem, p.src, s_begin, n_s, err, tile_fn)) return;
@@ -277,18 +259,10 @@ p2d_visc_kernel(const P2DViscProblem p, const RegConsts rc, double scale,
 	for (int k = 0; k < TPT; ++k) {
 		const int t = tbase + k * NT + tid;
 		if (t >= p.n_tgt) continue;
-		double sum[NC];
-#pragma unroll
-		for (int c = 0; c < NC; ++c) {
-			const int i = (c * TPT + k) * NT + tid;
-			sum[c] = double(hi[i]) + double(lo[i]);
-		}
-		if (gridDim.y == 1) {
-			write_visc2d(p, t, scale, sum[0], sum[1]);
-		} else {
-#pragma unroll
-			for (int c = 0; c < NC; ++c) partial[(size_t(blockIdx.y) * NC + c) * p.n_tgt + t] = sum[c];
-		}
+		const int i = k * NT + tid;
+		const double s = double(hi[i]) + double(lo[i]);
+		if (gridDim.y == 1) p.out[t] = float(scale * s);
+		else partial[size_t(blockIdx.y) * p.n_tgt + t] = s;
 	}
 }
 
@@ -299,17 +273,17 @@ p2d_visc2_kernel(const P2DViscProblem p, const RegConsts rc, double scale,
 	double* __restrict__ partial, int src_per_split, unsigned* err)
 {
 	static_assert(TPT % 2 == 0, "packed kernel: even TPT");
-	constexpr int H = TPT / 2, NC = kViscNC;
+	constexpr int H = TPT / 2;
 	extern __shared__ __align__(16) unsigned char smem[];
 	float* hi = reinterpret_cast<float*>(smem + Stream1::kSmemBytes);
-	float* lo = hi + NC * TPT * NT;
+	float* lo = hi + TPT * NT;
 	const int tid = threadIdx.x;
 	const int tbase = blockIdx.x * (TPT * NT);
 	const int s_begin = blockIdx.y * src_per_split;
 	int n_s = p.n_src - s_begin;
 	n_s = n_s < src_per_split ? n_s : src_per_split;
 	n_s = n_s > 0 ? n_s : 0;
-	float2 ntx[H], nty[H];
+	float2 ntx[H], nty[H], ntg[H], ta[H];
 #pragma unroll
 	for (int h = 0; h < H; ++h) {
 		float4 q[2];
@@ -320,13 +294,14 @@ p2d_visc2_kernel(const P2DViscProblem p, const RegConsts rc, double scale,
 			q[e] = p.tgt[t];
 		}
 		ntx[h] = make_float2(-q[0].x, -q[1].x); nty[h] = make_float2(-q[0].y, -q[1].y);
+		ntg[h] = make_float2(-q[0].z, -q[1].z); ta[h] = make_float2(q[0].w, q[1].w);
 	}
 #pragma unroll
-	for (int i = 0; i < NC * TPT; ++i) { hi[i * NT + tid] = 0.f; lo[i * NT + tid] = 0.f; }
+	for (int i = 0; i < TPT; ++i) { hi[i * NT + tid] = 0.f; lo[i * NT + tid] = 0.f; }
 	auto tile_fn = [&](const float4* __restrict__ st, int cnt) {
-		float2 ag[H], aa[H];
+		float2 acc[H];
 #pragma unroll
-		for (int h = 0; h < H; ++h) { ag[h] = make_float2(0.f, 0.f); aa[h] = ag[h]; }
+		for (int h = 0; h < H; ++h) acc[h] = make_float2(0.f, 0.f);
 		auto body = [&](int j) {
 			const float4 s = st[j];
 			const float2 sx = bc2(s.x), sy = bc2(s.y), sg = bc2(s.z), sa = bc2(s.w);
@@ -338,8 +313,9 @@ p2d_visc2_kernel(const P2DViscProblem p, const RegConsts rc, double scale,
 				float2 e = RegEta2D2<R>::eta2(r2, rc);
 				e.x = r2.x > 0.f ? e.x : 0.f;
 				e.y = r2.y > 0.f ? e.y : 0.f;
-				ag[h] = __ffma2_rn(e, sg, ag[h]);
-				aa[h] = __ffma2_rn(e, sa, aa[h]);
+				// Gamma_s A_t - Gamma_t A_s
+				const float2 w = __ffma2_rn(sg, ta[h], __fmul2_rn(ntg[h], sa));
+				acc[h] = __ffma2_rn(e, w, acc[h]);
 			}
 		};
 		if (cnt == kTile) {
@@ -352,48 +328,23 @@ p2d_visc2_kernel(const P2DViscProblem p, const RegConsts rc, double scale,
 #pragma unroll
 		for (int h = 0; h < H; ++h)
 #pragma unroll
-			for (int e = 0; e < 2; ++e)
-#pragma unroll
-				for (int c = 0; c < NC; ++c) {
-					const int i = (c * TPT + 2 * h + e) * NT + tid;
-					const float2 v = c == 0 ? ag[h] : aa[h];
-					float hv = hi[i], lv = lo[i];
-					fold_twosum(hv, lv, e == 0 ? v.x : v.y);
-					hi[i] = hv; lo[i] = lv;
-				}
+			for (int e = 0; e < 2; ++e) {
+				const int i = (2 * h + e) * NT + tid;
+				float hv = hi[i], lv = lo[i];
+				fold_twosum(hv, lv, e == 0 ? acc[h].x : acc[h].y);
+				hi[i] = hv; lo[i] = lv;
+			}
 	};
 	if (!Stream1::run(smem, p.src, s_begin, n_s, err, tile_fn)) return;
 #pragma unroll
 	for (int k = 0; k < TPT; ++k) {
 		const int t = tbase + k * NT + tid;
 		if (t >= p.n_tgt) continue;
-		double sum[NC];
-#pragma unroll
-		for (int c = 0; c < NC; ++c) {
-			const int i = (c * TPT + k) * NT + tid;
-			sum[c] = double(hi[i]) + double(lo[i]);
-		}
-		if (gridDim.y == 1) {
-			write_visc2d(p, t, scale, sum[0], sum[1]);
-		} else {
-#pragma unroll
-			for (int c = 0; c < NC; ++c) partial[(size_t(blockIdx.y) * NC + c) * p.n_tgt + t] = sum[c];
-		}
+		const int i = k * NT + tid;
+		const double sum = double(hi[i]) + double(lo[i]);
+		if (gridDim.y == 1) p.out[t] = float(scale * sum);
+		else partial[size_t(blockIdx.y) * p.n_tgt + t] = sum;
 	}
-}
-
-// Split partials of the viscous exchange, added in split order.
-__global__ void p2d_visc_finalize(const P2DViscProblem p, const double* __restrict__ partial,
-	int n_split, double scale)
-{
-	const int t = blockIdx.x * blockDim.x + threadIdx.x;
-	if (t >= p.n_tgt) return;
-	double sg = 0.0, sa = 0.0;
-	for (int sp = 0; sp < n_split; ++sp) {
-		sg += partial[(size_t(sp) * kViscNC + 0) * p.n_tgt + t];
-		sa += partial[(size_t(sp) * kViscNC + 1) * p.n_tgt + t];
-	}
-	write_visc2d(p, t, scale, sg, sa);
 }
 
 template <int NC>
@@ -466,15 +417,15 @@ auto visc_kernel() {
 
 template <Reg R, int TPT, int NT, bool PK>
 Plan plan_visc(int n_src, int n_tgt, int num_sms, int max_split = 64) {
-	constexpr size_t smem = smem_bytes<TPT, NT, kViscNC>();
+	constexpr size_t smem = smem_bytes<TPT, NT, 1>();
 	static const int occ = resident_ctas(visc_kernel<R, TPT, NT, PK>(), NT, smem);
-	return make_plan(n_src, n_tgt, TPT * NT, kTile, kViscNC, num_sms * occ, smem, max_split);
+	return make_plan(n_src, n_tgt, TPT * NT, kTile, 1, num_sms * occ, smem, max_split);
 }
 
 template <Reg R, int TPT, int NT, bool PK>
 cudaError_t launch_visc(const P2DViscProblem& p, const LaunchEnv& env) {
 	const Plan pl = plan_visc<R, TPT, NT, PK>(p.n_src, p.n_tgt, env.num_sms,
-		env.cap_to_ws ? split_cap_for(env.ws_bytes, kViscNC, p.n_tgt) : 64);
+		env.cap_to_ws ? split_cap_for(env.ws_bytes, 1, p.n_tgt) : 64);
 	if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
 	const RegConsts rc = make_reg_consts_host(p.sigma);
 	const double scale = 2.0 * double(p.nu) / (double(p.sigma) * double(p.sigma));
@@ -483,8 +434,8 @@ cudaError_t launch_visc(const P2DViscProblem& p, const LaunchEnv& env) {
 		p, rc, scale, partial, pl.src_per_split, env.err);
 	count_launch();
 	if (pl.n_split > 1) {
-		p2d_visc_finalize<<<(p.n_tgt + 255) / 256, 256, 0, env.stream>>>(
-			p, partial, pl.n_split, scale);
+		finalize_scaled<1><<<(p.n_tgt + 255) / 256, 256, 0, env.stream>>>(
+			p.out, p.n_tgt, partial, pl.n_split, scale);
 		count_launch();
 	}
 	return cudaGetLastError();

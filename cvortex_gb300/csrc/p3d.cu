@@ -310,32 +310,15 @@ struct P3DInduceOp {
 // ---------------------------------------------------------------------------
 // Viscous vorticity exchange (PSE), reference src/P3D.cpp:116-144:
 //   out_t = (2 nu / sigma^2) sum_s (alpha_s V_t - alpha_t V_s) eta(rho)
-//         = (2 nu / sigma^2) (V_t sum_s eta alpha_s - alpha_t sum_s eta V_s).
-// The kernels accumulate the four sums (sum eta alpha_s, sum eta V_s) per
-// target, compensated across tiles, and combine them once per target in
-// FP64: four multiply-adds per pair instead of nine, and the two parts
-// cancel once, in FP64, rather than in every FP32 term.
 // ---------------------------------------------------------------------------
 struct ViscConsts { RegConsts rc; double scale; };
-constexpr int kViscNC = 4;
-
-__device__ __forceinline__ void write_visc3d(const P3DViscProblem& p, double scale, int t,
-	const double* s)
-{
-	const float4 tp = p.tgt[size_t(t) * p.tstride];
-	const float4 tw = p.tgt[size_t(t) * p.tstride + 1];
-	float* o = p.out + 3 * size_t(t);
-	o[0] = float(scale * (double(tp.w) * s[0] - double(tw.x) * s[3]));
-	o[1] = float(scale * (double(tp.w) * s[1] - double(tw.y) * s[3]));
-	o[2] = float(scale * (double(tp.w) * s[2] - double(tw.z) * s[3]));
-}
 
 template <Reg R, int TPT, int NT>
 __global__ void __launch_bounds__(NT)
 p3d_visc_kernel(const P3DViscProblem p, const ViscConsts vc,
 	double* __restrict__ partial, int src_per_split, unsigned* err)
 {
-	constexpr int NC = kViscNC;
+	constexpr int NC = 3;
 	extern __shared__ __align__(16) unsigned char smem[];
 	float* hi = reinterpret_cast<float*>(smem + Stream2::kSmemBytes);
 	float* lo = hi + NC * TPT * NT;
@@ -346,13 +329,15 @@ p3d_visc_kernel(const P3DViscProblem p, const ViscConsts vc,
 	n_s = n_s < src_per_split ? n_s : src_per_split;
 	n_s = n_s > 0 ? n_s : 0;
 
-	float tx[TPT], ty[TPT], tz[TPT];
+	float tx[TPT], ty[TPT], tz[TPT], tv_[TPT], ax[TPT], ay[TPT], az[TPT];
 #pragma unroll
 	for (int k = 0; k < TPT; ++k) {
 		int t = tbase + k * NT + tid;
 		t = t < p.n_tgt ? t : p.n_tgt - 1;
 		const float4 tp = p.tgt[size_t(t) * p.tstride];
-		tx[k] = tp.x; ty[k] = tp.y; tz[k] = tp.z;
+		const float4 tw = p.tgt[size_t(t) * p.tstride + 1];
+		tx[k] = tp.x; ty[k] = tp.y; tz[k] = tp.z; tv_[k] = tp.w;
+		ax[k] = tw.x; ay[k] = tw.y; az[k] = tw.z;
 	}
 #pragma unroll
 	for (int i = 0; i < NC * TPT; ++i) { hi[i * NT + tid] = 0.f; lo[i * NT + tid] = 0.f; }
@@ -374,10 +359,13 @@ p3d_visc_kernel(const P3DViscProblem p, const ViscConsts vc,
 				const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
 				float e = RegP3D<R>::eta(r2, vc.rc);
 				e = r2 > 0.f ? e : 0.f;
-				acc[0][k] = fmaf(e, sv.x, acc[0][k]);
-				acc[1][k] = fmaf(e, sv.y, acc[1][k]);
-				acc[2][k] = fmaf(e, sv.z, acc[2][k]);
-				acc[3][k] = fmaf(e, sp.w, acc[3][k]);
+				// alpha_s V_t - alpha_t V_s, as the reference forms it per pair
+				const float wx = fmaf(sv.x, tv_[k], -ax[k] * sp.w);
+				const float wy = fmaf(sv.y, tv_[k], -ay[k] * sp.w);
+				const float wz = fmaf(sv.z, tv_[k], -az[k] * sp.w);
+				acc[0][k] = fmaf(e, wx, acc[0][k]);
+				acc[1][k] = fmaf(e, wy, acc[1][k]);
+				acc[2][k] = fmaf(e, wz, acc[2][k]);
 			}
 		};
 		if (cnt == kTile) {
@@ -403,17 +391,12 @@ p3d_visc_kernel(const P3DViscProblem p, const ViscConsts vc,
 	for (int k = 0; k < TPT; ++k) {
 		const int t = tbase + k * NT + tid;
 		if (t >= p.n_tgt) continue;
-		double s[NC];
 #pragma unroll
 		for (int c = 0; c < NC; ++c) {
 			const int i = (c * TPT + k) * NT + tid;
-			s[c] = double(hi[i]) + double(lo[i]);
-		}
-		if (gridDim.y == 1) {
-			write_visc3d(p, vc.scale, t, s);
-		} else {
-#pragma unroll
-			for (int c = 0; c < NC; ++c) partial[(size_t(blockIdx.y) * NC + c) * p.n_tgt + t] = s[c];
+			const double s = double(hi[i]) + double(lo[i]);
+			if (gridDim.y == 1) p.out[3 * size_t(t) + c] = float(vc.scale * s);
+			else partial[(size_t(blockIdx.y) * NC + c) * p.n_tgt + t] = s;
 		}
 	}
 }
@@ -425,7 +408,7 @@ p3d_visc2_kernel(const P3DViscProblem p, const ViscConsts vc,
 	double* __restrict__ partial, int src_per_split, unsigned* err)
 {
 	static_assert(TPT % 2 == 0, "packed kernel: even TPT");
-	constexpr int NC = kViscNC, H = TPT / 2;
+	constexpr int NC = 3, H = TPT / 2;
 	extern __shared__ __align__(16) unsigned char smem[];
 	float* hi = reinterpret_cast<float*>(smem + Stream2::kSmemBytes);
 	float* lo = hi + NC * TPT * NT;
@@ -435,18 +418,21 @@ p3d_visc2_kernel(const P3DViscProblem p, const ViscConsts vc,
 	int n_s = p.n_src - s_begin;
 	n_s = n_s < src_per_split ? n_s : src_per_split;
 	n_s = n_s > 0 ? n_s : 0;
-	float2 ntx[H], nty[H], ntz[H];
+	float2 tx[H], ty[H], tz[H], tv[H], nax[H], nay[H], naz[H];
 #pragma unroll
 	for (int h = 0; h < H; ++h) {
-		float4 q[2];
+		float4 q[2], w[2];
 #pragma unroll
 		for (int e = 0; e < 2; ++e) {
 			int t = tbase + (2 * h + e) * NT + tid;
 			t = t < p.n_tgt ? t : p.n_tgt - 1;
 			q[e] = p.tgt[size_t(t) * p.tstride];
+			w[e] = p.tgt[size_t(t) * p.tstride + 1];
 		}
-		ntx[h] = make_float2(-q[0].x, -q[1].x); nty[h] = make_float2(-q[0].y, -q[1].y);
-		ntz[h] = make_float2(-q[0].z, -q[1].z);
+		tx[h] = make_float2(q[0].x, q[1].x); ty[h] = make_float2(q[0].y, q[1].y);
+		tz[h] = make_float2(q[0].z, q[1].z); tv[h] = make_float2(q[0].w, q[1].w);
+		nax[h] = make_float2(-w[0].x, -w[1].x); nay[h] = make_float2(-w[0].y, -w[1].y);
+		naz[h] = make_float2(-w[0].z, -w[1].z);
 	}
 #pragma unroll
 	for (int i = 0; i < NC * TPT; ++i) { hi[i * NT + tid] = 0.f; lo[i * NT + tid] = 0.f; }
@@ -460,20 +446,22 @@ p3d_visc2_kernel(const P3DViscProblem p, const ViscConsts vc,
 			const float4 sp = st[2 * j];
 			const float4 sv = st[2 * j + 1];
 			const float2 sx = bc2(sp.x), sy = bc2(sp.y), sz = bc2(sp.z), vs = bc2(sp.w);
-			const float2 wx = bc2(sv.x), wy = bc2(sv.y), wz = bc2(sv.z);
 #pragma unroll
 			for (int h = 0; h < H; ++h) {
-				const float2 dx = __fadd2_rn(sx, ntx[h]);
-				const float2 dy = __fadd2_rn(sy, nty[h]);
-				const float2 dz = __fadd2_rn(sz, ntz[h]);
+				const float2 dx = __fadd2_rn(sx, make_float2(-tx[h].x, -tx[h].y));
+				const float2 dy = __fadd2_rn(sy, make_float2(-ty[h].x, -ty[h].y));
+				const float2 dz = __fadd2_rn(sz, make_float2(-tz[h].x, -tz[h].y));
 				const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
 				float2 e = RegEta2<R>::eta2(r2, vc.rc);
 				e.x = r2.x > 0.f ? e.x : 0.f;
 				e.y = r2.y > 0.f ? e.y : 0.f;
+				// alpha_s V_t - alpha_t V_s
+				const float2 wx = __ffma2_rn(bc2(sv.x), tv[h], __fmul2_rn(nax[h], vs));
+				const float2 wy = __ffma2_rn(bc2(sv.y), tv[h], __fmul2_rn(nay[h], vs));
+				const float2 wz = __ffma2_rn(bc2(sv.z), tv[h], __fmul2_rn(naz[h], vs));
 				acc[0][h] = __ffma2_rn(e, wx, acc[0][h]);
 				acc[1][h] = __ffma2_rn(e, wy, acc[1][h]);
 				acc[2][h] = __ffma2_rn(e, wz, acc[2][h]);
-				acc[3][h] = __ffma2_rn(e, vs, acc[3][h]);
 			}
 		};
 		if (cnt == kTile) {
@@ -500,32 +488,14 @@ p3d_visc2_kernel(const P3DViscProblem p, const ViscConsts vc,
 	for (int k = 0; k < TPT; ++k) {
 		const int t = tbase + k * NT + tid;
 		if (t >= p.n_tgt) continue;
-		double s[NC];
 #pragma unroll
 		for (int c = 0; c < NC; ++c) {
 			const int i = (c * TPT + k) * NT + tid;
-			s[c] = double(hi[i]) + double(lo[i]);
-		}
-		if (gridDim.y == 1) {
-			write_visc3d(p, vc.scale, t, s);
-		} else {
-#pragma unroll
-			for (int c = 0; c < NC; ++c) partial[(size_t(blockIdx.y) * NC + c) * p.n_tgt + t] = s[c];
+			const double s = double(hi[i]) + double(lo[i]);
+			if (gridDim.y == 1) p.out[3 * size_t(t) + c] = float(vc.scale * s);
+			else partial[(size_t(blockIdx.y) * NC + c) * p.n_tgt + t] = s;
 		}
 	}
-}
-
-// Split partials of the viscous exchange, added in split order.
-__global__ void p3d_visc_finalize(const P3DViscProblem p, const double* __restrict__ partial,
-	int n_split, double scale)
-{
-	const int t = blockIdx.x * blockDim.x + threadIdx.x;
-	if (t >= p.n_tgt) return;
-	double s[kViscNC] = {0.0, 0.0, 0.0, 0.0};
-	for (int sp = 0; sp < n_split; ++sp)
-#pragma unroll
-		for (int c = 0; c < kViscNC; ++c) s[c] += partial[(size_t(sp) * kViscNC + c) * p.n_tgt + t];
-	write_visc3d(p, scale, t, s);
 }
 
 __global__ void p3_finalize_scaled(float* __restrict__ out, int n_tgt,
@@ -952,15 +922,15 @@ auto visc_kernel() {
 
 template <Reg R, int TPT, int NT, bool PK>
 Plan plan_visc(int n_src, int n_tgt, int num_sms, int max_split = 64) {
-	constexpr size_t smem = smem_bytes<TPT, NT, kViscNC>();
+	constexpr size_t smem = smem_bytes<TPT, NT, 3>();
 	static const int occ = resident_ctas(visc_kernel<R, TPT, NT, PK>(), NT, smem);
-	return make_plan(n_src, n_tgt, TPT * NT, kTile, kViscNC, num_sms * occ, smem, max_split);
+	return make_plan(n_src, n_tgt, TPT * NT, kTile, 3, num_sms * occ, smem, max_split);
 }
 
 template <Reg R, int TPT, int NT, bool PK>
 cudaError_t launch_visc(const P3DViscProblem& p, const LaunchEnv& env) {
 	const Plan pl = plan_visc<R, TPT, NT, PK>(p.n_src, p.n_tgt, env.num_sms,
-		env.cap_to_ws ? split_cap_for(env.ws_bytes, kViscNC, p.n_tgt) : 64);
+		env.cap_to_ws ? split_cap_for(env.ws_bytes, 3, p.n_tgt) : 64);
 	if (pl.ws_bytes > env.ws_bytes) return cudaErrorInvalidValue;
 	ViscConsts vc;
 	vc.rc = make_reg_consts(p.sigma);
@@ -972,8 +942,8 @@ cudaError_t launch_visc(const P3DViscProblem& p, const LaunchEnv& env) {
 		p, vc, partial, pl.src_per_split, env.err);
 	count_launch();
 	if (pl.n_split > 1) {
-		p3d_visc_finalize<<<(p.n_tgt + 255) / 256, 256, 0, env.stream>>>(
-			p, partial, pl.n_split, vc.scale);
+		p3_finalize_scaled<<<(p.n_tgt + 255) / 256, 256, 0, env.stream>>>(
+			p.out, p.n_tgt, partial, pl.n_split, vc.scale);
 		count_launch();
 	}
 	return cudaGetLastError();

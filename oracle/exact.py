@@ -257,6 +257,74 @@ def f3d_dvort(fil, ind):
     return out
 
 
+def term_magnitude(op, reg, sigma, nu, src, tgt=None, pts=None):
+    """Per target, the sum of the magnitudes of its terms, sum_s |term_s|
+    (vector norms for vector outputs), with the same scaling as the op's
+    result: the condition number of a target's sum is this over |result|.
+    op: p3d_vel (src, pts), p3d_dvort (src, tgt), p3d_visc (src, tgt),
+    p2d_vel (src, pts), p2d_visc (src, tgt), f3d_vel (fil=src, pts),
+    f3d_dvort (fil=src, tgt)."""
+    s = float(sigma)
+    if op in ("p3d_vel", "p3d_dvort"):
+        xs, a_s = src["coord"].astype(F64), src["vorticity"].astype(F64)
+        xt = np.asarray(pts if op == "p3d_vel" else tgt["coord"], F64)
+        d = xt[:, None, :] - xs[None, :, :]
+        r2 = np.einsum("ijk,ijk->ij", d, d)
+        G, K = G_K(np.sqrt(r2) / abs(s), reg)
+        G = np.where(r2 > 0, G, 0.0)
+        K = np.where(r2 > 0, K, 0.0)
+        if op == "p3d_vel":
+            c = np.cross(d, a_s[None])
+            return (np.abs(G) * np.linalg.norm(c, axis=-1)).sum(1) / (4 * math.pi * abs(s) ** 3)
+        co = np.cross(tgt["vorticity"].astype(F64)[:, None, :], a_s[None])
+        dco = np.einsum("ijk,ijk->ij", d, co)
+        t = G[..., None] * co - (K * dco / s ** 2)[..., None] * d
+        return np.linalg.norm(t, axis=-1).sum(1) / (4 * math.pi * abs(s) ** 3)
+    if op in ("p3d_visc", "p2d_visc"):
+        two_d = op == "p2d_visc"
+        xs, xt = src["coord"].astype(F64), tgt["coord"].astype(F64)
+        d = xs[None] - xt[:, None]
+        r2 = np.einsum("ijk,ijk->ij", d, d)
+        e = np.where(r2 > 0, (eta2 if two_d else eta3)(np.sqrt(r2) / abs(s), reg), 0.0)
+        if two_d:
+            w = (src["vorticity"].astype(F64)[None] * tgt["area"].astype(F64)[:, None]
+                 - tgt["vorticity"].astype(F64)[:, None] * src["area"].astype(F64)[None])
+            return np.abs(e * w).sum(1) * (2.0 * nu / s ** 2)
+        w = (src["vorticity"].astype(F64)[None] * tgt["volume"].astype(F64)[:, None, None]
+             - tgt["vorticity"].astype(F64)[:, None] * src["volume"].astype(F64)[None, :, None])
+        return (np.abs(e) * np.linalg.norm(w, axis=-1)).sum(1) * (2.0 * nu / s ** 2)
+    if op == "p2d_vel":
+        xs, gs = src["coord"].astype(F64), src["vorticity"].astype(F64)
+        d = np.asarray(pts, F64)[:, None] - xs[None]
+        r2 = d[..., 0] ** 2 + d[..., 1] ** 2
+        h = np.where(r2 > 0, g2_over_r2(np.where(r2 > 0, r2, 1.0), sigma, reg), 0.0) * gs[None]
+        return (np.abs(h) * np.sqrt(r2)).sum(1) / (2 * math.pi)
+    if op in ("f3d_vel", "f3d_dvort"):
+        a, b = src["start"].astype(F64), src["end"].astype(F64)
+        g = src["strength"].astype(F64)
+        x = np.asarray(pts if op == "f3d_vel" else tgt["coord"], F64)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            r1, r2 = x[:, None] - a[None], x[:, None] - b[None]
+            r0 = r1 - r2
+            l1, l2 = np.linalg.norm(r1, axis=-1), np.linalg.norm(r2, axis=-1)
+            t212 = np.einsum("ijk,ijk->ij", r0, r1) / l1 - np.einsum("ijk,ijk->ij", r0, r2) / l2
+            if op == "f3d_vel":
+                c = np.cross(r1, r2)
+                cc = np.einsum("ijk,ijk->ij", c, c)
+                v = (g[None] / (4 * math.pi * cc) * t212)[..., None] * c
+            else:
+                X = np.cross(r1, r0)
+                X2 = np.einsum("ijk,ijk->ij", X, X)
+                t1 = g[None] / (4 * math.pi)
+                A = (-r0 / X2[..., None]) * (t1 * t212)[..., None]
+                B = (3.0 / np.linalg.norm(r0, axis=-1)) * t1 * (np.sqrt(X2) / l1 - np.sqrt(X2) / l2)
+                w = np.broadcast_to(tgt["vorticity"].astype(F64)[:, None], A.shape)
+                v = w * B[..., None] + np.cross(A, w)
+            m = np.linalg.norm(v, axis=-1)
+            return np.where(np.isfinite(m), m, 0.0).sum(1)
+    raise ValueError(op)
+
+
 def rel_l2(a, b):
     """||a - b||_2 / ||b||_2 over a whole output array."""
     a = np.asarray(a, F64).ravel()

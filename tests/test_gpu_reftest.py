@@ -23,6 +23,7 @@ import pytest
 import oracle
 import reftest_inputs as rt
 from conftest import golden
+from oracle import exact
 
 pytestmark = pytest.mark.gpu
 
@@ -74,6 +75,18 @@ def _fp64(op, reg, a, rows):
     raise ValueError(op)
 
 
+def _kappa(op, reg, a, rows, ex):
+    """Condition number of the rows' sums: sum of term magnitudes over the
+    magnitude of the FP64 result."""
+    src = a["fil"] if op.startswith("f3d") else a["p2"] if op.startswith("p2d") else a["p3"]
+    tgt = (a["t2"] if op.startswith("p2d") else a["t3"])[rows]
+    pts = (a["p2"] if op.startswith("p2d") else a["p3"])["coord"][rows]
+    mag = exact.term_magnitude(op, reg, rt.SIGMA, rt.NU, src, tgt=tgt, pts=pts)
+    ex = np.asarray(ex, np.float64)
+    nrm = np.abs(ex) if ex.ndim == 1 else np.linalg.norm(ex, axis=1)
+    return mag / np.maximum(nrm, 1e-300)
+
+
 def _row_err(x, ref):
     x, ref = np.asarray(x, np.float64), np.asarray(ref, np.float64)
     if x.ndim == 1:
@@ -86,10 +99,12 @@ def _row_err(x, ref):
 def test_reference_comparison(gpu, test, repeat):
     """Per element: |gpu - ref| / |gpu + ref| <= 1e-5, the reference's bar.
     An element that misses it passes only if the GPU is within 1e-5 of the
-    FP64 result or at least as close to it as the reference is: there the
-    two FP32 formulations disagree because the element is ill-conditioned
-    (terms that cancel, a point near a filament's line, the reference's
-    Gaussian closed forms at small rho), not because either is wrong."""
+    FP64 result, or at least as close to it as the reference is, or within
+    the accuracy FP32 terms can give its sum (8 u kappa, kappa the sum's
+    condition number): there the two FP32 formulations disagree because the
+    element is ill-conditioned (terms that cancel, a point near a
+    filament's line, the reference's Gaussian closed forms at small rho),
+    not because either is wrong."""
     g = _golden()
     a = _inputs()[(test, repeat)]
     rho_c = float(gpu.lib.cvtx_gb300_gaussian_rho_c())
@@ -117,6 +132,13 @@ def test_reference_comparison(gpu, test, repeat):
         e_gpu = _row_err(np.asarray(got)[rows], ex)
         e_ref = _row_err(np.asarray(want)[rows], ex)
         bad = e_gpu > np.maximum(e_ref, rt.REL_ACC)
+        if bad.any():
+            # FP32 terms resolve a sum only to about u * kappa, with kappa =
+            # sum |terms| / |sum| its condition number (u = 2^-24; 8 u allows
+            # for the few roundings inside one term)
+            kappa = _kappa(op, reg, a, rows[bad], ex[bad])
+            ok = e_gpu[bad] <= 8 * 2.0 ** -24 * kappa
+            bad[np.nonzero(bad)[0][ok]] = False
         fallback[key] = int(len(rows))
         if bad.any():
             i = int(np.argmax(e_gpu - np.maximum(e_ref, rt.REL_ACC)))
