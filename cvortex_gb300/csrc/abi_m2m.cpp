@@ -255,16 +255,16 @@ CVTX_EXPORT void cvtx_P3D_M2M_visc_dvort(const cvtx_P3D** src, const int n,
 		float4* ht = (!alias && hs) ? job.stage(c->h_tgt, c->tgt, tb) : nullptr;
 		if (ht) gather_p3d_host(ind, m, ht);
 		job.ensure_out(c->out0, c->h_out0, ob);
-		job.check(c->ensure_ws(p3d_visc_ws_bytes(reg, n, m, c->num_sms)), "workspace");
+		P3DViscProblem p;
+		p.src = static_cast<const float4*>(c->src.ptr); p.n_src = n;
+		p.tgt = static_cast<const float4*>(alias ? c->src.ptr : c->tgt.ptr);
+		p.tstride = 2; p.n_tgt = m;
+		p.out = static_cast<float*>(c->out0.ptr);
+		p.sigma = sigma; p.nu = nu;
+		job.check(c->ensure_ws(p3d_visc_ws_bytes_for(reg, p, c->num_sms)), "workspace");
 		if (job.begin()) {
 			job.upload(c->h_src, c->src, sb);
 			if (!alias) job.upload(c->h_tgt, c->tgt, tb);
-			P3DViscProblem p;
-			p.src = static_cast<const float4*>(c->src.ptr); p.n_src = n;
-			p.tgt = static_cast<const float4*>(alias ? c->src.ptr : c->tgt.ptr);
-			p.tstride = 2; p.n_tgt = m;
-			p.out = static_cast<float*>(c->out0.ptr);
-			p.sigma = sigma; p.nu = nu;
 			job.check(p3d_visc(reg, p, c->env()), "kernel launch");
 			if (job.finish(c->out0, c->h_out0, ob)) std::memcpy(out, c->h_out0.ptr, ob);
 		}

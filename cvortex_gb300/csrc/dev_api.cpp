@@ -113,13 +113,13 @@ CVTX_EXPORT int cvtx_gb300_dev_P3D_M2M_visc(const void* src, int n_src, const vo
 		const cudaError_t e = cudaMemsetAsync(out, 0, sizeof(float) * 3 * size_t(n_tgt), c.stream);
 		return e == cudaSuccess ? 0 : -2;
 	}
-	int st = c.prepare(p3d_visc_ws_bytes(reg, n_src, n_tgt, c.ctx ? c.ctx->num_sms : 1),
-		"cvtx_gb300_dev_P3D_M2M_visc");
-	if (st) return st;
 	P3DViscProblem p;
 	p.src = static_cast<const float4*>(src); p.n_src = n_src;
 	p.tgt = static_cast<const float4*>(tgt); p.tstride = tgt_stride; p.n_tgt = n_tgt;
 	p.out = out; p.sigma = sigma; p.nu = nu;
+	int st = c.prepare(p3d_visc_ws_bytes_for(reg, p, c.ctx ? c.ctx->num_sms : 1),
+		"cvtx_gb300_dev_P3D_M2M_visc");
+	if (st) return st;
 	return c.done(p3d_visc(reg, p, c.env()), "cvtx_gb300_dev_P3D_M2M_visc");
 }
 

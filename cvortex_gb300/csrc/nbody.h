@@ -157,7 +157,16 @@ bool p3d_induce_set_tuned(int reg, unsigned ops, int bucket, int cfg);
 int p3d_induce_current_config(int reg, unsigned ops, int n_tgt);
 
 size_t p3d_visc_ws_bytes(int reg, int n_src, int n_tgt, int num_sms);
+// Workspace for p3d_visc on this problem (the self-interaction form's when
+// it applies).
+size_t p3d_visc_ws_bytes_for(int reg, const P3DViscProblem& p, int num_sms);
 cudaError_t p3d_visc(int reg, const P3DViscProblem& p, const LaunchEnv& env);
+// Self-interaction form of the viscous exchange (p3d_sym.cu), on the same
+// conditions as p3d_self_form_applies; p3d_visc takes it when it applies and
+// the workspace suffices.
+bool p3d_visc_self_form_applies(int reg, const P3DViscProblem& p);
+size_t p3d_visc_self_ws_bytes(int reg, int n, int num_sms, size_t ws_cap = 0);
+cudaError_t p3d_visc_self(int reg, const P3DViscProblem& p, const LaunchEnv& env);
 
 size_t p3d_vort_ws_bytes(int reg, int n_src, int n_tgt, int num_sms);
 cudaError_t p3d_vort(int reg, const P3DVortProblem& p, const LaunchEnv& env);

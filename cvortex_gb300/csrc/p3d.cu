@@ -1083,8 +1083,19 @@ size_t p3d_visc_ws_bytes(int reg, int n_src, int n_tgt, int num_sms) {
 
 // Only Winckelmans and Gaussian have an eta function; the runtime handles the
 // other regularisations (zeros and a warning) without launching anything.
+size_t p3d_visc_ws_bytes_for(int reg, const P3DViscProblem& p, int num_sms) {
+	if (p.n_tgt <= 0) return 0;
+	const size_t base = p3d_visc_ws_bytes(reg, p.n_src, p.n_tgt, num_sms);
+	if (!p3d_visc_self_form_applies(reg, p)) return base;
+	return std::max(base, p3d_visc_self_ws_bytes(reg, p.n_tgt, num_sms));
+}
+
 cudaError_t p3d_visc(int reg, const P3DViscProblem& p, const LaunchEnv& env) {
 	if (p.n_tgt <= 0) return cudaSuccess;
+	if (env.cta_src_cap == 0 && p3d_visc_self_form_applies(reg, p) &&
+		p3d_visc_self_ws_bytes(reg, p.n_tgt, env.num_sms, env.cap_to_ws ? env.ws_bytes : 0) <=
+			env.ws_bytes)
+		return p3d_visc_self(reg, p, env);
 	const bool small = p.n_tgt < kSmallTargets;
 	if (reg == int(Reg::Winckelmans))
 		return small ? launch_visc<Reg::Winckelmans, 1, 128, false>(p, env)

@@ -90,3 +90,37 @@ def test_self_form_coincident_particles(gpu):
     sub = p[idx].copy()
     check(vel[idx], oracle.p3d_vel(p, sub["coord"], "singular", 0.05))
     check(dv[idx], oracle.p3d_dvort(p, sub, "singular", 0.05))
+
+
+def _dev_visc(gpu, torch, rec, tgt, n, reg, nu):
+    out = torch.full((n, 3), float("nan"), dtype=torch.float32, device="cuda")
+    sh = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert gpu.lib.cvtx_gb300_dev_P3D_M2M_visc(rec.data_ptr(), n, tgt.data_ptr(), 2, n,
+                                               out.data_ptr(), abi.REG_IDS[reg], 0.05,
+                                               C.c_float(nu), sh) == 0
+    assert gpu.lib.cvtx_gb300_dev_status(sh) == 0
+    return out.cpu().numpy()
+
+
+@pytest.mark.parametrize("reg", ["winckelmans", "gaussian"])
+@pytest.mark.parametrize("n", [33_001, 70_000])
+def test_viscous_self_form_vs_oracle_and_ordered_pairs(gpu, reg, n):
+    """The viscous exchange of the particles with themselves in the
+    self-interaction form, against the oracle on sampled targets and against
+    the ordered-pair kernel (targets passed as a separate copy of the
+    records) on every target."""
+    import torch
+    nu = 1e-3
+    p = workloads.vortex_ring(n, seed=76) if n == 70_000 else workloads.uniform_cube(n, seed=77)
+    rec = torch.from_numpy(_records(p)).cuda()
+    self_out = _dev_visc(gpu, torch, rec, rec, n, reg, nu)
+    ordered = _dev_visc(gpu, torch, rec, rec.clone(), n, reg, nu)
+    assert np.all(np.isfinite(self_out))
+    assert exact.rel_l2(self_out, ordered) <= TOL, exact.rel_l2(self_out, ordered)
+    idx = np.sort(np.random.Generator(np.random.PCG64(78)).choice(n, 1024, replace=False))
+    sub = p[idx].copy()
+    ref = oracle.p3d_visc(p, sub, reg, 0.05, nu)
+    check(self_out[idx], ref, reg, sub["coord"], p["coord"], 0.05)
+    # the cvtx_ ABI with the pointer array as its own targets takes the same form
+    via_abi = gpu.p3d_visc(p, p, reg, 0.05, nu, same=True)
+    assert exact.rel_l2(via_abi, self_out) <= 1e-6
