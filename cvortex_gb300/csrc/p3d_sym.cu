@@ -59,7 +59,9 @@ namespace {
 
 constexpr int kSymNT = 128;                    // threads per CTA
 constexpr int kSymTPT = 4;                     // particles per thread and pass
+constexpr int kSymH = kSymTPT / 2;             // f32x2 lane pairs per thread
 constexpr int kSymPass = kSymNT * kSymTPT;     // particles of block bi per pass
+constexpr int kSymUnroll = 2;                  // rotation steps unrolled
 constexpr int kSymWarps = kSymNT / 32;
 // Resident CTAs per SM the registers are sized for (167 registers for the
 // fused pair). Sizing for two (217 registers) measured 5-7 % slower.
@@ -80,14 +82,16 @@ struct InduceSym {
 	using Problem = P3DInduceProblem;
 	using Consts = InduceConsts;
 	static constexpr int NC = InduceNC<VEL, DV>::value;
-	static constexpr bool kBlockDiagonal = true;   // diagonal items by induce2_block
-	struct Tgt { float2 tx[2], ty[2], tz[2], ax[2], ay[2], az[2], nax[2], nay[2], naz[2]; };
+	struct Tgt {
+		float2 tx[kSymH], ty[kSymH], tz[kSymH], ax[kSymH], ay[kSymH], az[kSymH];
+		float2 nax[kSymH], nay[kSymH], naz[kSymH];
+	};
 
 	__device__ __forceinline__ static void load(const Problem& p, int tb, int tid, int lim,
 		Tgt& g)
 	{
 #pragma unroll
-		for (int h = 0; h < 2; ++h) {
+		for (int h = 0; h < kSymH; ++h) {
 			const int t0 = min(tb + (2 * h) * kSymNT + tid, lim - 1);
 			const int t1 = min(tb + (2 * h + 1) * kSymNT + tid, lim - 1);
 			const float4 q0 = p.tgt[2 * size_t(t0)], q1 = p.tgt[2 * size_t(t1)];
@@ -103,7 +107,7 @@ struct InduceSym {
 
 	template <bool FULL, bool SYM>
 	__device__ __forceinline__ static void step(const Consts& kc, float4 sp, float4 sv,
-		bool valid, const Tgt& g, float2 (&acc)[NC][2], float (&js)[NC])
+		bool valid, const Tgt& g, float2 (&acc)[NC][kSymH], float (&js)[NC])
 	{
 		constexpr bool kFinite = FiniteAtZero<R>::value;
 		const RegConsts& rc = kc.rc;
@@ -115,7 +119,7 @@ struct InduceSym {
 		const float2 wx = bc2(sv.x), wy = bc2(sv.y), wz = bc2(sv.z);
 		const float2 nwx = bc2(-sv.x), nwy = bc2(-sv.y), nwz = bc2(-sv.z);
 #pragma unroll
-		for (int h = 0; h < 2; ++h) {
+		for (int h = 0; h < kSymH; ++h) {
 			const float2 dx = __ffma2_rn(sx, bc2(-1.f), g.tx[h]);
 			const float2 dy = __ffma2_rn(sy, bc2(-1.f), g.ty[h]);
 			const float2 dz = __ffma2_rn(sz, bc2(-1.f), g.tz[h]);
@@ -200,14 +204,15 @@ struct ViscSym {
 	using Problem = P3DViscProblem;
 	using Consts = SymViscConsts;
 	static constexpr int NC = 3;
-	static constexpr bool kBlockDiagonal = false;
-	struct Tgt { float2 ntx[2], nty[2], ntz[2], tv[2], nax[2], nay[2], naz[2]; };
+	struct Tgt {
+		float2 ntx[kSymH], nty[kSymH], ntz[kSymH], tv[kSymH], nax[kSymH], nay[kSymH], naz[kSymH];
+	};
 
 	__device__ __forceinline__ static void load(const Problem& p, int tb, int tid, int lim,
 		Tgt& g)
 	{
 #pragma unroll
-		for (int h = 0; h < 2; ++h) {
+		for (int h = 0; h < kSymH; ++h) {
 			const int t0 = min(tb + (2 * h) * kSymNT + tid, lim - 1);
 			const int t1 = min(tb + (2 * h + 1) * kSymNT + tid, lim - 1);
 			const float4 q0 = p.tgt[2 * size_t(t0)], q1 = p.tgt[2 * size_t(t1)];
@@ -221,7 +226,7 @@ struct ViscSym {
 
 	template <bool FULL, bool SYM>
 	__device__ __forceinline__ static void step(const Consts& vc, float4 sp, float4 sv,
-		bool valid, const Tgt& g, float2 (&acc)[NC][2], float (&js)[NC])
+		bool valid, const Tgt& g, float2 (&acc)[NC][kSymH], float (&js)[NC])
 	{
 		if (!FULL && !valid) {
 			sp = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -229,7 +234,7 @@ struct ViscSym {
 		}
 		const float2 sx = bc2(sp.x), sy = bc2(sp.y), sz = bc2(sp.z), vs = bc2(sp.w);
 #pragma unroll
-		for (int h = 0; h < 2; ++h) {
+		for (int h = 0; h < kSymH; ++h) {
 			// source - target, rounded once as in the per-call kernels
 			const float2 dx = __fadd2_rn(sx, g.ntx[h]);
 			const float2 dy = __fadd2_rn(sy, g.nty[h]);
@@ -286,10 +291,10 @@ __device__ __forceinline__ void red_add_f32(float* p, float v) {
 template <class Op, bool FULL, bool SYM>
 __device__ __forceinline__ void sym_group(const typename Op::Consts& kc,
 	const float4* __restrict__ grp, int gcnt, int lane, const typename Op::Tgt& g,
-	float2 (&acc)[Op::NC][2], float (&js)[Op::NC])
+	float2 (&acc)[Op::NC][kSymH], float (&js)[Op::NC])
 {
 	const int from = (lane + 1) & 31;
-#pragma unroll 2
+#pragma unroll kSymUnroll
 	for (int k = 0; k < 32; ++k) {
 		const int jl = (lane + k) & 31;
 		const float4 sp = grp[2 * jl];
@@ -336,9 +341,11 @@ __device__ __forceinline__ bool sym_item(const typename Op::Problem& p,
 		int toff = 0;   // first record of the current tile within block bj
 
 		auto tile_fn = [&](const float4* __restrict__ st, int cnt) {
-			float2 acc[NC][2];
+			float2 acc[NC][kSymH];
 #pragma unroll
-			for (int c = 0; c < NC; ++c) { acc[c][0] = make_float2(0.f, 0.f); acc[c][1] = acc[c][0]; }
+			for (int c = 0; c < NC; ++c)
+#pragma unroll
+				for (int h = 0; h < kSymH; ++h) acc[c][h] = make_float2(0.f, 0.f);
 			const int ng = (cnt + 31) >> 5;
 			for (int gi = 0; gi < ng; ++gi) {
 				const int gcnt = min(32, cnt - 32 * gi);
@@ -374,7 +381,7 @@ __device__ __forceinline__ bool sym_item(const typename Op::Problem& p,
 #pragma unroll
 			for (int c = 0; c < NC; ++c) {
 #pragma unroll
-				for (int h = 0; h < 2; ++h)
+				for (int h = 0; h < kSymH; ++h)
 #pragma unroll
 					for (int e = 0; e < 2; ++e) {
 						const int i = (c * kSymTPT + 2 * h + e) * kSymNT + tid;
