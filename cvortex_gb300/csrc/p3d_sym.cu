@@ -61,7 +61,6 @@ constexpr int kSymNT = 128;                    // threads per CTA
 constexpr int kSymTPT = 4;                     // particles per thread and pass
 constexpr int kSymH = kSymTPT / 2;             // f32x2 lane pairs per thread
 constexpr int kSymPass = kSymNT * kSymTPT;     // particles of block bi per pass
-constexpr int kSymUnroll = 2;                  // rotation steps unrolled
 constexpr int kSymWarps = kSymNT / 32;
 // Resident CTAs per SM the registers are sized for (167 registers for the
 // fused pair). Sizing for two (217 registers) measured 5-7 % slower.
@@ -73,7 +72,9 @@ constexpr int kSymMinBlocks = 3;
 // clamped below `lim`); step<FULL, SYM>, one lane's particles against one
 // record, adding to the particles' packed sums `acc` and (SYM) to the
 // record's running sums `js`; write, the output of a particle from its FP64
-// sums. FULL = false zeroes the pair for a lane whose record lies past the
+// sums; kUnroll, the rotation steps unrolled (timed on a GB300 per op; two
+// particles per thread instead of four measured 5-9 % slower).
+// FULL = false zeroes the pair for a lane whose record lies past the
 // end of the block (`valid` false).
 
 // Induced velocity and/or stretching (reference src/P3D.cpp:51-114).
@@ -82,6 +83,8 @@ struct InduceSym {
 	using Problem = P3DInduceProblem;
 	using Consts = InduceConsts;
 	static constexpr int NC = InduceNC<VEL, DV>::value;
+	// fused, 1M cube: 4 -> 967, 8 -> 947, 2 -> 937 G/s; one output alone: 8
+	static constexpr int kUnroll = (VEL && DV) ? 4 : 8;
 	struct Tgt {
 		float2 tx[kSymH], ty[kSymH], tz[kSymH], ax[kSymH], ay[kSymH], az[kSymH];
 		float2 nax[kSymH], nay[kSymH], naz[kSymH];
@@ -204,6 +207,8 @@ struct ViscSym {
 	using Problem = P3DViscProblem;
 	using Consts = SymViscConsts;
 	static constexpr int NC = 3;
+	// 100k ring: 16 -> 1,966, 8 -> 1,943, 4 -> 1,925, 2 -> 1,821 G/s
+	static constexpr int kUnroll = 16;
 	struct Tgt {
 		float2 ntx[kSymH], nty[kSymH], ntz[kSymH], tv[kSymH], nax[kSymH], nay[kSymH], naz[kSymH];
 	};
@@ -294,7 +299,7 @@ __device__ __forceinline__ void sym_group(const typename Op::Consts& kc,
 	float2 (&acc)[Op::NC][kSymH], float (&js)[Op::NC])
 {
 	const int from = (lane + 1) & 31;
-#pragma unroll kSymUnroll
+#pragma unroll Op::kUnroll
 	for (int k = 0; k < 32; ++k) {
 		const int jl = (lane + k) & 31;
 		const float4 sp = grp[2 * jl];
@@ -607,13 +612,12 @@ bool self_shape(const float4* src, int n_src, const float4* tgt, int tstride, in
 
 }  // namespace
 
-// Stretching (alone or with the velocity) only: measured on a GB300, the
-// velocity alone runs faster in the ordered-pair kernel (1,722 against
-// 1,643 G interactions/s on the 100,000-particle ring), the stretching alone
-// 1.42x faster in this form and the fused pair 1.07-1.08x.
+// Measured on a GB300 against the ordered-pair kernel (G interactions/s):
+// fused 967 against 866 (1M cube), stretching alone 1,464 against 1,010 and
+// velocity alone 1,770 against 1,698 (100,000-particle ring).
 bool p3d_self_form_applies(int reg, unsigned ops, const P3DInduceProblem& p) {
 	(void)reg;
-	if (!(ops & kOpDvort)) return false;
+	(void)ops;
 	return self_shape(p.src, p.n_src, p.tgt, p.tstride, p.n_tgt);
 }
 
