@@ -185,14 +185,35 @@ def test_every_configuration_on_every_target_ring_100k(gpu, reg):
             if cfg == few_cfg:
                 continue
             v, d = run(ops, cfg)
-            for got, base in ((v, base_v), (d, base_d)):
-                if got is None:
-                    continue
-                assert np.all(np.isfinite(got)), (ops, cfg)
-                # per target: |got - base| within 1e-5 of the target's own
-                # result or of the array's RMS, whichever is larger
-                err = np.linalg.norm(got - base, axis=1)
-                scale = np.maximum(np.linalg.norm(base, axis=1),
-                                   np.sqrt(np.mean(np.sum(base ** 2, axis=1))))
-                worst = float(np.max(err / scale))
-                assert worst <= 1e-5, (ops, cfg, worst, int(np.argmax(err / scale)))
+            for name, got, base in (("vel", v, base_v), ("dvort", d, base_d)):
+                if got is not None:
+                    _same_up_to_rounding(p, reg, name, got, base, (ops, cfg))
+
+
+def _same_up_to_rounding(p, reg, name, got, base, what):
+    """Two FP32 evaluations of the same sums: equal within 1e-5 relative on
+    every target except targets whose sums cancel (a few per thousand at
+    most); those must lie within the FP32 bound 8 u sum_s |term_s| of the
+    FP64 value in both evaluations. A fault confined to one packed lane or
+    one target slot would show on a fixed fraction (1/2 .. 1/6) of all
+    targets."""
+    n = len(base)
+    assert np.all(np.isfinite(got)), what
+    assert exact.rel_l2(got, base) <= TOL, (what, exact.rel_l2(got, base))
+    err = np.linalg.norm(got - base, axis=1)
+    scale = np.maximum(np.linalg.norm(base, axis=1), np.sqrt(np.mean(np.sum(base ** 2, axis=1))))
+    rel = err / scale
+    bad = np.flatnonzero(rel > 1e-5)
+    assert len(bad) <= n // 1000, (what, len(bad))
+    if len(bad) == 0:
+        return
+    worst = bad[np.argsort(rel[bad])[-16:]]
+    sub = p[worst].copy()
+    ev, ed = oracle.exact_p3d_vel_dvort(p, sub["coord"], sub["vorticity"], reg, SIG,
+                                        want_vel=name == "vel", want_dvort=name == "dvort")
+    ex = ev if name == "vel" else ed
+    mag = exact.term_magnitude("p3d_" + name, reg, SIG, 0.0, p, tgt=sub, pts=sub["coord"])
+    bound = np.maximum(1e-5 * np.linalg.norm(ex, axis=1), 8 * 2.0 ** -24 * mag)
+    for arr in (got, base):
+        e = np.linalg.norm(arr[worst].astype(np.float64) - ex, axis=1)
+        assert np.all(e <= bound), (what, worst[e > bound], e[e > bound], bound[e > bound])
