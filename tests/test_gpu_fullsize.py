@@ -192,14 +192,13 @@ def test_every_configuration_on_every_target_ring_100k(gpu, reg):
 
 def _same_up_to_rounding(p, reg, name, got, base, what):
     """Two FP32 evaluations of the same sums: equal within 1e-5 relative on
-    every target except targets whose sums cancel (a few per thousand at
-    most); those must lie within the FP32 bound 8 u sum_s |term_s| of the
-    FP64 value in both evaluations. A fault confined to one packed lane or
+    every target except targets whose sums cancel (one per thousand at
+    most); the 32 worst of those must lie within the FP32 bound
+    8 u sum_s |term_s| of the FP64 value in both evaluations. A fault confined to one packed lane or
     one target slot would show on a fixed fraction (1/2 .. 1/6) of all
     targets."""
     n = len(base)
     assert np.all(np.isfinite(got)), what
-    assert exact.rel_l2(got, base) <= TOL, (what, exact.rel_l2(got, base))
     err = np.linalg.norm(got - base, axis=1)
     scale = np.maximum(np.linalg.norm(base, axis=1), np.sqrt(np.mean(np.sum(base ** 2, axis=1))))
     rel = err / scale
@@ -207,7 +206,7 @@ def _same_up_to_rounding(p, reg, name, got, base, what):
     assert len(bad) <= n // 1000, (what, len(bad))
     if len(bad) == 0:
         return
-    worst = bad[np.argsort(rel[bad])[-16:]]
+    worst = bad[np.argsort(rel[bad])[-32:]]
     sub = p[worst].copy()
     ev, ed = oracle.exact_p3d_vel_dvort(p, sub["coord"], sub["vorticity"], reg, SIG,
                                         want_vel=name == "vel", want_dvort=name == "dvort")
