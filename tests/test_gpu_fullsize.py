@@ -192,8 +192,8 @@ def test_every_configuration_on_every_target_ring_100k(gpu, reg):
 
 def _same_up_to_rounding(p, reg, name, got, base, what):
     """Two FP32 evaluations of the same sums: equal within 1e-5 relative on
-    every target except targets whose sums cancel (one per thousand at
-    most); the 32 worst of those must lie within the FP32 bound
+    every target except targets whose sums cancel (one per hundred at
+    most; the singular stretching of the ring has 0.3 %); the 32 worst of those must lie within the FP32 bound
     8 u sum_s |term_s| of the FP64 value in both evaluations. A fault confined to one packed lane or
     one target slot would show on a fixed fraction (1/2 .. 1/6) of all
     targets."""
@@ -203,7 +203,7 @@ def _same_up_to_rounding(p, reg, name, got, base, what):
     scale = np.maximum(np.linalg.norm(base, axis=1), np.sqrt(np.mean(np.sum(base ** 2, axis=1))))
     rel = err / scale
     bad = np.flatnonzero(rel > 1e-5)
-    assert len(bad) <= n // 1000, (what, len(bad))
+    assert len(bad) <= n // 100, (what, len(bad))
     if len(bad) == 0:
         return
     worst = bad[np.argsort(rel[bad])[-32:]]
