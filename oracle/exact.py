@@ -257,13 +257,17 @@ def f3d_dvort(fil, ind):
     return out
 
 
-def term_magnitude(op, reg, sigma, nu, src, tgt=None, pts=None):
+def term_magnitude(op, reg, sigma, nu, src, tgt=None, pts=None, co_bound=False):
     """Per target, the sum of the magnitudes of its terms, sum_s |term_s|
     (vector norms for vector outputs), with the same scaling as the op's
     result: the condition number of a target's sum is this over |result|.
     op: p3d_vel (src, pts), p3d_dvort (src, tgt), p3d_visc (src, tgt),
     p2d_vel (src, pts), p2d_visc (src, tgt), f3d_vel (fil=src, pts),
-    f3d_dvort (fil=src, tgt)."""
+    f3d_dvort (fil=src, tgt).
+    co_bound (p3d_dvort): bound each term's parts by |alpha_t| |alpha_s| in
+    place of |alpha_t x alpha_s| (reference src/P3D.cpp:86-114 forms the
+    cross product in FP32; for nearly parallel vorticities its rounding error
+    is of order u |alpha_t| |alpha_s|, not u |alpha_t x alpha_s|)."""
     s = float(sigma)
     if op in ("p3d_vel", "p3d_dvort"):
         xs, a_s = src["coord"].astype(F64), src["vorticity"].astype(F64)
@@ -276,7 +280,12 @@ def term_magnitude(op, reg, sigma, nu, src, tgt=None, pts=None):
         if op == "p3d_vel":
             c = np.cross(d, a_s[None])
             return (np.abs(G) * np.linalg.norm(c, axis=-1)).sum(1) / (4 * math.pi * abs(s) ** 3)
-        co = np.cross(tgt["vorticity"].astype(F64)[:, None, :], a_s[None])
+        a_t = tgt["vorticity"].astype(F64)
+        if co_bound:
+            aa = np.linalg.norm(a_t, axis=1)[:, None] * np.linalg.norm(a_s, axis=1)[None]
+            t = (np.abs(G) + np.abs(K) * r2 / s ** 2) * aa
+            return t.sum(1) / (4 * math.pi * abs(s) ** 3)
+        co = np.cross(a_t[:, None, :], a_s[None])
         dco = np.einsum("ijk,ijk->ij", d, co)
         t = G[..., None] * co - (K * dco / s ** 2)[..., None] * d
         return np.linalg.norm(t, axis=-1).sum(1) / (4 * math.pi * abs(s) ** 3)

@@ -211,7 +211,10 @@ def _same_up_to_rounding(p, reg, name, got, base, what):
     ev, ed = oracle.exact_p3d_vel_dvort(p, sub["coord"], sub["vorticity"], reg, SIG,
                                         want_vel=name == "vel", want_dvort=name == "dvort")
     ex = ev if name == "vel" else ed
-    mag = exact.term_magnitude("p3d_" + name, reg, SIG, 0.0, p, tgt=sub, pts=sub["coord"])
+    # the pair terms' own FP32 rounding (the stretching's alpha_t x alpha_s)
+    # counts at its parts' magnitude
+    mag = exact.term_magnitude("p3d_" + name, reg, SIG, 0.0, p, tgt=sub, pts=sub["coord"],
+                               co_bound=True)
     bound = np.maximum(1e-5 * np.linalg.norm(ex, axis=1), 8 * 2.0 ** -24 * mag)
     for arr in (got, base):
         e = np.linalg.norm(arr[worst].astype(np.float64) - ex, axis=1)
