@@ -85,22 +85,6 @@ struct InduceSym {
 	static constexpr int NC = InduceNC<VEL, DV>::value;
 	// fused, 1M cube: 4 -> 967, 8 -> 947, 2 -> 937 G/s; one output alone: 8
 	static constexpr int kUnroll = (VEL && DV) ? 4 : 8;
-	// Records as streamed (expand): -x, -y, -z and the vorticity each as an
-	// f32x2 pair, the vorticity also negated, so that the rotation builds no
-	// operand pair; five float4 (80 B) per particle.
-	static constexpr int kRec = 5;
-	static constexpr int kTile = 128;
-	__device__ __forceinline__ static void expand(const float4* __restrict__ src,
-		float4* __restrict__ ex, int i)
-	{
-		const float4 q = src[2 * size_t(i)], v = src[2 * size_t(i) + 1];
-		float4* o = ex + kRec * size_t(i);
-		o[0] = make_float4(-q.x, -q.x, -q.y, -q.y);
-		o[1] = make_float4(-q.z, -q.z, v.x, v.x);
-		o[2] = make_float4(v.y, v.y, v.z, v.z);
-		o[3] = make_float4(-v.x, -v.x, -v.y, -v.y);
-		o[4] = make_float4(-v.z, -v.z, 0.f, 0.f);
-	}
 	struct Tgt {
 		float2 tx[kSymH], ty[kSymH], tz[kSymH], ax[kSymH], ay[kSymH], az[kSymH];
 		float2 nax[kSymH], nay[kSymH], naz[kSymH];
@@ -125,27 +109,23 @@ struct InduceSym {
 	}
 
 	template <bool FULL, bool SYM>
-	__device__ __forceinline__ static void step(const Consts& kc, const float4* __restrict__ r,
+	__device__ __forceinline__ static void step(const Consts& kc, float4 sp, float4 sv,
 		bool valid, const Tgt& g, float2 (&acc)[NC][kSymH], float (&js)[NC])
 	{
 		constexpr bool kFinite = FiniteAtZero<R>::value;
 		const RegConsts& rc = kc.rc;
-		float4 f0 = r[0], f1 = r[1], f2 = r[2], f3 = r[3], f4 = r[4];
 		if (!FULL && !valid) {
-			f0 = f1 = f2 = f3 = f4 = make_float4(0.f, 0.f, 0.f, 0.f);
+			sp = make_float4(0.f, 0.f, 0.f, 0.f);
+			sv = make_float4(0.f, 0.f, 0.f, 0.f);
 		}
-		const float2 nsx = make_float2(f0.x, f0.y), nsy = make_float2(f0.z, f0.w);
-		const float2 nsz = make_float2(f1.x, f1.y);
-		const float2 wx = make_float2(f1.z, f1.w), wy = make_float2(f2.x, f2.y);
-		const float2 wz = make_float2(f2.z, f2.w);
-		const float2 nwx = make_float2(f3.x, f3.y), nwy = make_float2(f3.z, f3.w);
-		const float2 nwz = make_float2(f4.x, f4.y);
+		const float2 sx = bc2(sp.x), sy = bc2(sp.y), sz = bc2(sp.z);
+		const float2 wx = bc2(sv.x), wy = bc2(sv.y), wz = bc2(sv.z);
+		const float2 nwx = bc2(-sv.x), nwy = bc2(-sv.y), nwz = bc2(-sv.z);
 #pragma unroll
 		for (int h = 0; h < kSymH; ++h) {
-			// t - s, rounded once as the per-call kernel rounds it
-			const float2 dx = __fadd2_rn(g.tx[h], nsx);
-			const float2 dy = __fadd2_rn(g.ty[h], nsy);
-			const float2 dz = __fadd2_rn(g.tz[h], nsz);
+			const float2 dx = __ffma2_rn(sx, bc2(-1.f), g.tx[h]);
+			const float2 dy = __ffma2_rn(sy, bc2(-1.f), g.ty[h]);
+			const float2 dz = __ffma2_rn(sz, bc2(-1.f), g.tz[h]);
 			const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
 			float2 G, K;
 			if (DV) {
@@ -229,22 +209,6 @@ struct ViscSym {
 	static constexpr int NC = 3;
 	// 100k ring: 16 -> 1,966, 8 -> 1,943, 4 -> 1,925, 2 -> 1,821 G/s
 	static constexpr int kUnroll = 16;
-	// Records as streamed (expand): position, volume and vorticity as f32x2
-	// pairs, padded to five float4 (80 B, a stride without shared-memory bank
-	// conflicts in the rotation).
-	static constexpr int kRec = 5;
-	static constexpr int kTile = 128;
-	__device__ __forceinline__ static void expand(const float4* __restrict__ src,
-		float4* __restrict__ ex, int i)
-	{
-		const float4 q = src[2 * size_t(i)], v = src[2 * size_t(i) + 1];
-		float4* o = ex + kRec * size_t(i);
-		o[0] = make_float4(q.x, q.x, q.y, q.y);
-		o[1] = make_float4(q.z, q.z, q.w, q.w);
-		o[2] = make_float4(v.x, v.x, v.y, v.y);
-		o[3] = make_float4(v.z, v.z, 0.f, 0.f);
-		o[4] = make_float4(0.f, 0.f, 0.f, 0.f);
-	}
 	struct Tgt {
 		float2 ntx[kSymH], nty[kSymH], ntz[kSymH], tv[kSymH], nax[kSymH], nay[kSymH], naz[kSymH];
 	};
@@ -266,17 +230,14 @@ struct ViscSym {
 	}
 
 	template <bool FULL, bool SYM>
-	__device__ __forceinline__ static void step(const Consts& vc, const float4* __restrict__ r,
+	__device__ __forceinline__ static void step(const Consts& vc, float4 sp, float4 sv,
 		bool valid, const Tgt& g, float2 (&acc)[NC][kSymH], float (&js)[NC])
 	{
-		float4 f0 = r[0], f1 = r[1], f2 = r[2], f3 = r[3];
 		if (!FULL && !valid) {
-			f0 = f1 = f2 = f3 = make_float4(0.f, 0.f, 0.f, 0.f);
+			sp = make_float4(0.f, 0.f, 0.f, 0.f);
+			sv = make_float4(0.f, 0.f, 0.f, 0.f);
 		}
-		const float2 sx = make_float2(f0.x, f0.y), sy = make_float2(f0.z, f0.w);
-		const float2 sz = make_float2(f1.x, f1.y), vs = make_float2(f1.z, f1.w);
-		const float2 ax = make_float2(f2.x, f2.y), ay = make_float2(f2.z, f2.w);
-		const float2 az = make_float2(f3.x, f3.y);
+		const float2 sx = bc2(sp.x), sy = bc2(sp.y), sz = bc2(sp.z), vs = bc2(sp.w);
 #pragma unroll
 		for (int h = 0; h < kSymH; ++h) {
 			// source - target, rounded once as in the per-call kernels
@@ -289,9 +250,9 @@ struct ViscSym {
 			e.y = r2.y > 0.f ? e.y : 0.f;
 			if (!FULL && !valid) e = make_float2(0.f, 0.f);
 			// alpha_s V_t - alpha_t V_s
-			const float2 wx = __ffma2_rn(ax, g.tv[h], __fmul2_rn(g.nax[h], vs));
-			const float2 wy = __ffma2_rn(ay, g.tv[h], __fmul2_rn(g.nay[h], vs));
-			const float2 wz = __ffma2_rn(az, g.tv[h], __fmul2_rn(g.naz[h], vs));
+			const float2 wx = __ffma2_rn(bc2(sv.x), g.tv[h], __fmul2_rn(g.nax[h], vs));
+			const float2 wy = __ffma2_rn(bc2(sv.y), g.tv[h], __fmul2_rn(g.nay[h], vs));
+			const float2 wz = __ffma2_rn(bc2(sv.z), g.tv[h], __fmul2_rn(g.naz[h], vs));
 			acc[0][h] = __ffma2_rn(e, wx, acc[0][h]);
 			acc[1][h] = __ffma2_rn(e, wy, acc[1][h]);
 			acc[2][h] = __ffma2_rn(e, wz, acc[2][h]);
@@ -314,14 +275,12 @@ struct ViscSym {
 };
 
 // ---- the rotation ------------------------------------------------------------
-template <class Op> using SymStream = TileStream<Op::kRec, Op::kTile, 2>;
-
-template <class Op>
+template <int NC>
 constexpr size_t sym_smem_bytes() {
 	// tile stages, (hi, lo) per pass particle and sum, and two buffers of
 	// per-warp record sums [2][warps][NC][32]
-	return SymStream<Op>::kSmemBytes + size_t(2) * Op::NC * kSymPass * sizeof(float) +
-		size_t(2) * kSymWarps * Op::NC * 32 * sizeof(float);
+	return P3DStream::kSmemBytes + size_t(2) * NC * kSymPass * sizeof(float) +
+		size_t(2) * kSymWarps * NC * 32 * sizeof(float);
 }
 
 // Fire-and-forget add to global memory (no value returned, so the thread
@@ -343,7 +302,9 @@ __device__ __forceinline__ void sym_group(const typename Op::Consts& kc,
 #pragma unroll Op::kUnroll
 	for (int k = 0; k < 32; ++k) {
 		const int jl = (lane + k) & 31;
-		Op::template step<FULL, SYM>(kc, grp + Op::kRec * jl, jl < gcnt, g, acc, js);
+		const float4 sp = grp[2 * jl];
+		const float4 sv = grp[2 * jl + 1];
+		Op::template step<FULL, SYM>(kc, sp, sv, jl < gcnt, g, acc, js);
 		if (SYM) {
 #pragma unroll
 			for (int c = 0; c < Op::NC; ++c) js[c] = __shfl_sync(0xffffffffu, js[c], from);
@@ -352,10 +313,9 @@ __device__ __forceinline__ void sym_group(const typename Op::Consts& kc,
 }
 
 struct SymArgs {
-	int S;                 // block length (multiple of kSymPass)
-	int nb;                // blocks
-	float* slots;          // [nb][NC][n] partial sums
-	const float4* rec;     // the particles as streamed (Op::kRec float4 each)
+	int S;            // block length (multiple of kSymPass)
+	int nb;           // blocks
+	float* slots;     // [nb][NC][n] partial sums
 };
 
 // Item (bi, bj): all passes of block bi against block bj. SYM (bi < bj)
@@ -369,8 +329,7 @@ __device__ __forceinline__ bool sym_item(const typename Op::Problem& p,
 {
 	constexpr int NC = Op::NC;
 	const int n = p.n_tgt;
-	using Stream = SymStream<Op>;
-	float* hi = reinterpret_cast<float*>(smem + Stream::kSmemBytes);
+	float* hi = reinterpret_cast<float*>(smem + P3DStream::kSmemBytes);
 	float* lo = hi + NC * kSymPass;
 	float* jbuf = lo + NC * kSymPass;            // [2][warps][NC][32]
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -395,7 +354,7 @@ __device__ __forceinline__ bool sym_item(const typename Op::Problem& p,
 			const int ng = (cnt + 31) >> 5;
 			for (int gi = 0; gi < ng; ++gi) {
 				const int gcnt = min(32, cnt - 32 * gi);
-				const float4* grp = st + Op::kRec * 32 * gi;
+				const float4* grp = st + 2 * 32 * gi;
 				float js[NC];
 #pragma unroll
 				for (int c = 0; c < NC; ++c) js[c] = 0.f;
@@ -438,7 +397,7 @@ __device__ __forceinline__ bool sym_item(const typename Op::Problem& p,
 			}
 			toff += cnt;
 		};
-		if (!Stream::run_continue(smem, a.rec, j0, nj, err, tcount, tile_fn)) return false;
+		if (!P3DStream::run_continue(smem, p.src, j0, nj, err, tcount, tile_fn)) return false;
 #pragma unroll
 		for (int k = 0; k < kSymTPT; ++k) {
 			const int t = tb + k * kSymNT + tid;
@@ -451,6 +410,37 @@ __device__ __forceinline__ bool sym_item(const typename Op::Problem& p,
 		}
 	}
 	return true;
+}
+
+// The diagonal item (b, b) of the induced velocity / stretching: the per-call
+// CTA body over the block's ordered pairs.
+template <Reg R, bool VEL, bool DV>
+__device__ __forceinline__ bool sym_diagonal(const P3DInduceProblem& p, const InduceConsts& kc,
+	const SymArgs& a, int b, unsigned char* smem, unsigned* err, unsigned& tcount,
+	InduceSym<R, VEL, DV>*)
+{
+	constexpr int NC = InduceNC<VEL, DV>::value;
+	const int n = p.n_tgt;
+	const int b0 = b * a.S;
+	const int b1 = min(n, b0 + a.S);
+	P3DInduceProblem q = p;
+	q.n_tgt = b1;      // targets of this block only; loads clamp below b1
+	for (int tb = b0; tb < b1; tb += kSymPass) {
+		const bool ok = induce2_block<R, VEL, DV, kSymTPT, kSymNT, 2>(q, kc, tb, b0, b1 - b0,
+			smem, err, tcount, [&](int t, const double* s) {
+#pragma unroll
+				for (int c = 0; c < NC; ++c) a.slots[(size_t(b) * NC + c) * n + t] = float(s[c]);
+			});
+		if (!ok) return false;
+	}
+	return true;
+}
+
+template <Reg R>
+__device__ __forceinline__ bool sym_diagonal(const P3DViscProblem& p, const SymViscConsts& vc,
+	const SymArgs& a, int b, unsigned char* smem, unsigned* err, unsigned& tcount, ViscSym<R>*)
+{
+	return sym_item<ViscSym<R>, false>(p, vc, a, b, b, smem, err, tcount);
 }
 
 // Item `it` of nb blocks, largest first: the full off-diagonal pairs column
@@ -481,7 +471,7 @@ p3d_sym_kernel(const typename Op::Problem p, const typename Op::Consts kc, const
 		if (threadIdx.x == 0) atomicOr(err, kErrBadLaunch);
 		return;
 	}
-	if (!SymStream<Op>::init(smem, err)) return;
+	if (!P3DStream::init(smem, err)) return;
 	unsigned tcount = 0;
 	const int n = p.n_tgt;
 	for (;;) {
@@ -496,9 +486,9 @@ p3d_sym_kernel(const typename Op::Problem p, const typename Op::Consts kc, const
 			if (threadIdx.x == 0) atomicOr(err, kErrBadWork);
 			continue;
 		}
-		// a diagonal item pairs the block with itself from the particle side
-		const bool ok = bi == bj ? sym_item<Op, false>(p, kc, a, bi, bj, smem, err, tcount)
-		                         : sym_item<Op, true>(p, kc, a, bi, bj, smem, err, tcount);
+		const bool ok = bi == bj
+			? sym_diagonal(p, kc, a, bi, smem, err, tcount, static_cast<Op*>(nullptr))
+			: sym_item<Op, true>(p, kc, a, bi, bj, smem, err, tcount);
 		if (!ok) return;
 	}
 }
@@ -522,32 +512,22 @@ __global__ void p3d_sym_finalize(const typename Op::Problem p, const typename Op
 	Op::write(p, kc, t, s);
 }
 
-// The particles' records rewritten as the rotation streams them.
-template <class Op>
-__global__ void p3d_sym_expand(const float4* __restrict__ src, float4* __restrict__ ex, int n)
-{
-	const int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i < n) Op::expand(src, ex, i);
-}
-
 template <class Op>
 int sym_occupancy() {
-	static const int occ = resident_ctas(p3d_sym_kernel<Op>, kSymNT, sym_smem_bytes<Op>());
+	static const int occ = resident_ctas(p3d_sym_kernel<Op>, kSymNT, sym_smem_bytes<Op::NC>());
 	return occ;
 }
 
 // Block plan: about eight items per resident CTA (so that the last items
 // leave little of the GPU idle), blocks a multiple of the 512-particle pass,
 // and a workspace within `ws_cap` bytes (fewer, longer blocks otherwise).
-// Workspace: the slots, the item counter, the streamed records.
 struct SymPlan {
 	int S = 0, nb = 0, n_items = 0;
-	size_t slots_bytes = 0, counter_off = 0, rec_off = 0, ws_bytes = 0;
+	size_t slots_bytes = 0, counter_off = 0, ws_bytes = 0;
 };
 
-SymPlan sym_plan(int n, int nc, int rec_f4, int capacity, size_t ws_cap) {
+SymPlan sym_plan(int n, int nc, int capacity, size_t ws_cap) {
 	SymPlan pl;
-	const size_t rec_bytes = (size_t(n) * rec_f4 * 16 + 255) & ~size_t(255);
 	int nb = int(std::ceil(std::sqrt(16.0 * capacity)));
 	for (;; nb = nb * 7 / 8) {
 		nb = std::max(nb, 2);
@@ -560,8 +540,7 @@ SymPlan sym_plan(int n, int nc, int rec_f4, int capacity, size_t ws_cap) {
 		pl.slots_bytes = size_t(nbr) * nc * size_t(n) * sizeof(float);
 		pl.slots_bytes = (pl.slots_bytes + 255) & ~size_t(255);
 		pl.counter_off = pl.slots_bytes;
-		pl.rec_off = pl.counter_off + 256;
-		pl.ws_bytes = pl.rec_off + rec_bytes;
+		pl.ws_bytes = pl.counter_off + 256;
 		if (pl.ws_bytes <= ws_cap || nb == 2) break;
 	}
 	return pl;
@@ -572,8 +551,7 @@ constexpr size_t kSymWsCap = size_t(4) << 30;
 
 template <class Op>
 size_t sym_ws_bytes(int n, int num_sms, size_t ws_cap) {
-	return sym_plan(n, Op::NC, Op::kRec, num_sms * sym_occupancy<Op>(),
-		ws_cap ? ws_cap : kSymWsCap).ws_bytes;
+	return sym_plan(n, Op::NC, num_sms * sym_occupancy<Op>(), ws_cap ? ws_cap : kSymWsCap).ws_bytes;
 }
 
 template <class Op>
@@ -581,24 +559,20 @@ cudaError_t sym_launch(const typename Op::Problem& p, const typename Op::Consts&
 	const LaunchEnv& env)
 {
 	const int occ = sym_occupancy<Op>();
-	const SymPlan pl = sym_plan(p.n_tgt, Op::NC, Op::kRec, env.num_sms * occ,
+	const SymPlan pl = sym_plan(p.n_tgt, Op::NC, env.num_sms * occ,
 		env.cap_to_ws ? env.ws_bytes : std::min(env.ws_bytes, kSymWsCap));
 	if (pl.ws_bytes > env.ws_bytes || !env.ws) return cudaErrorInvalidValue;
 	unsigned char* ws = static_cast<unsigned char*>(env.ws);
 	unsigned* d_next = reinterpret_cast<unsigned*>(ws + pl.counter_off);
-	float4* rec = reinterpret_cast<float4*>(ws + pl.rec_off);
 	// the slots and the item counter start at zero
-	const cudaError_t e = cudaMemsetAsync(ws, 0, pl.rec_off, env.stream);
+	const cudaError_t e = cudaMemsetAsync(ws, 0, pl.ws_bytes, env.stream);
 	if (e != cudaSuccess) return e;
-	p3d_sym_expand<Op><<<(p.n_tgt + 255) / 256, 256, 0, env.stream>>>(p.src, rec, p.n_tgt);
-	count_launch();
 	SymArgs a;
 	a.S = pl.S;
 	a.nb = pl.nb;
 	a.slots = reinterpret_cast<float*>(ws);
-	a.rec = rec;
 	const int grid = std::max(1, std::min(pl.n_items, env.num_sms * occ));
-	p3d_sym_kernel<Op><<<grid, kSymNT, sym_smem_bytes<Op>(), env.stream>>>(
+	p3d_sym_kernel<Op><<<grid, kSymNT, sym_smem_bytes<Op::NC>(), env.stream>>>(
 		p, kc, a, pl.n_items, d_next, env.err);
 	count_launch();
 	p3d_sym_finalize<Op><<<(p.n_tgt + 255) / 256, 256, 0, env.stream>>>(p, kc, a.slots, pl.nb);
