@@ -183,7 +183,8 @@ int gpu_p3d_induce(const char* what, const cvtx_P3D** src, int n, const bsv_V3f*
 	p.out_vel = vel ? static_cast<float*>(c->out0.ptr) : nullptr;
 	p.out_dvort = dvort ? static_cast<float*>(c->out1.ptr) : nullptr;
 	p.sigma = sigma;
-	if (!job.check(c->ensure_ws(p3d_induce_ws_bytes_for(reg, ops, p, c->num_sms)), "workspace"))
+	if (!job.check(c->ensure_ws_or(p3d_induce_ws_bytes_for(reg, ops, p, c->num_sms),
+			p3d_induce_ws_bytes(reg, ops, p.n_src, p.n_tgt, c->num_sms)), "workspace"))
 		return job.status();
 	if (!job.begin()) return job.status();
 	job.upload(c->h_src, c->src, sb);
@@ -261,7 +262,8 @@ CVTX_EXPORT void cvtx_P3D_M2M_visc_dvort(const cvtx_P3D** src, const int n,
 		p.tstride = 2; p.n_tgt = m;
 		p.out = static_cast<float*>(c->out0.ptr);
 		p.sigma = sigma; p.nu = nu;
-		job.check(c->ensure_ws(p3d_visc_ws_bytes_for(reg, p, c->num_sms)), "workspace");
+		job.check(c->ensure_ws_or(p3d_visc_ws_bytes_for(reg, p, c->num_sms),
+			p3d_visc_ws_bytes(reg, n, m, c->num_sms)), "workspace");
 		if (job.begin()) {
 			job.upload(c->h_src, c->src, sb);
 			if (!alias) job.upload(c->h_tgt, c->tgt, tb);

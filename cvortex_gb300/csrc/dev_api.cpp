@@ -9,6 +9,7 @@
 // overlap on the workspace whatever streams they use. Device-side errors of
 // these calls go to their own error word (cvtx_gb300_dev_status), which the
 // host-pointer calls never reset.
+#include <cstdint>
 #include <string>
 
 #include "cvortex/cvtx_gb300.h"
@@ -26,10 +27,12 @@ struct DevCall {
 		: lock(Runtime::get().lock()), ctx(Runtime::get().active_context()),
 		  stream(static_cast<cudaStream_t>(s)) {}
 
-	// Serialise workspace users across streams.
-	int prepare(size_t ws_bytes, const char* what) {
+	// Serialise workspace users across streams. A call whose preferred form
+	// needs more workspace than can be allocated runs in the form that fits
+	// `fallback_bytes`.
+	int prepare(size_t ws_bytes, const char* what, size_t fallback_bytes = SIZE_MAX) {
 		if (!ctx) return -3;
-		cudaError_t e = ctx->ensure_ws(ws_bytes);
+		cudaError_t e = ctx->ensure_ws_or(ws_bytes, fallback_bytes);
 		if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, ctx->ws_ev, 0);
 		if (e != cudaSuccess) {
 			set_error(std::string(what) + ": " + cudaGetErrorString(e));
@@ -76,8 +79,9 @@ CVTX_EXPORT int cvtx_gb300_dev_P3D_M2M(const void* src, int n_src, const void* t
 	p.src = static_cast<const float4*>(src); p.n_src = n_src;
 	p.tgt = static_cast<const float4*>(tgt); p.tstride = tgt_stride; p.n_tgt = n_tgt;
 	p.out_vel = vel_out; p.out_dvort = dvort_out; p.sigma = sigma;
-	int st = c.prepare(p3d_induce_ws_bytes_for(reg, ops, p, c.ctx ? c.ctx->num_sms : 1),
-		"cvtx_gb300_dev_P3D_M2M");
+	const int sms = c.ctx ? c.ctx->num_sms : 1;
+	int st = c.prepare(p3d_induce_ws_bytes_for(reg, ops, p, sms), "cvtx_gb300_dev_P3D_M2M",
+		p3d_induce_ws_bytes(reg, ops, n_src, n_tgt, sms));
 	if (st) return st;
 	return c.done(p3d_induce(reg, ops, p, c.env()), "cvtx_gb300_dev_P3D_M2M");
 }
@@ -94,8 +98,9 @@ CVTX_EXPORT int cvtx_gb300_dev_P3D_step(void* rec, int n, float* vel, float* dvo
 	p.src = r; p.n_src = n;
 	p.tgt = r; p.tstride = 2; p.n_tgt = n;
 	p.out_vel = vel; p.out_dvort = dvort; p.sigma = sigma;
-	int st = c.prepare(p3d_induce_ws_bytes_for(reg, ops, p, c.ctx ? c.ctx->num_sms : 1),
-		"cvtx_gb300_dev_P3D_step");
+	const int sms = c.ctx ? c.ctx->num_sms : 1;
+	int st = c.prepare(p3d_induce_ws_bytes_for(reg, ops, p, sms), "cvtx_gb300_dev_P3D_step",
+		p3d_induce_ws_bytes(reg, ops, n, n, sms));
 	if (st) return st;
 	cudaError_t e = p3d_induce(reg, ops, p, c.env());
 	if (e == cudaSuccess) e = advance_p3d(r, n, vel, dvort, dt, c.stream);
@@ -117,8 +122,9 @@ CVTX_EXPORT int cvtx_gb300_dev_P3D_M2M_visc(const void* src, int n_src, const vo
 	p.src = static_cast<const float4*>(src); p.n_src = n_src;
 	p.tgt = static_cast<const float4*>(tgt); p.tstride = tgt_stride; p.n_tgt = n_tgt;
 	p.out = out; p.sigma = sigma; p.nu = nu;
-	int st = c.prepare(p3d_visc_ws_bytes_for(reg, p, c.ctx ? c.ctx->num_sms : 1),
-		"cvtx_gb300_dev_P3D_M2M_visc");
+	const int sms = c.ctx ? c.ctx->num_sms : 1;
+	int st = c.prepare(p3d_visc_ws_bytes_for(reg, p, sms), "cvtx_gb300_dev_P3D_M2M_visc",
+		p3d_visc_ws_bytes(reg, n_src, n_tgt, sms));
 	if (st) return st;
 	return c.done(p3d_visc(reg, p, c.env()), "cvtx_gb300_dev_P3D_M2M_visc");
 }

@@ -14,6 +14,7 @@
 // memory. With one source split the CTA writes results directly; otherwise
 // it writes FP64 partials that a finalize kernel combines in split order.
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <atomic>
@@ -1030,7 +1031,8 @@ size_t p3d_induce_ws_bytes_for(int reg, unsigned ops, const P3DInduceProblem& p,
 	if (p.n_tgt <= 0) return 0;
 	const size_t base = p3d_induce_ws_bytes(reg, ops, p.n_src, p.n_tgt, num_sms);
 	if (!use_self_form(reg, ops, p, 0)) return base;
-	return std::max(base, p3d_self_ws_bytes(reg, ops, p.n_tgt, num_sms));
+	const size_t self = p3d_self_ws_bytes(reg, ops, p.n_tgt, num_sms);
+	return self == SIZE_MAX ? base : std::max(base, self);
 }
 
 cudaError_t p3d_induce(int reg, unsigned ops, const P3DInduceProblem& p, const LaunchEnv& env) {
@@ -1087,7 +1089,8 @@ size_t p3d_visc_ws_bytes_for(int reg, const P3DViscProblem& p, int num_sms) {
 	if (p.n_tgt <= 0) return 0;
 	const size_t base = p3d_visc_ws_bytes(reg, p.n_src, p.n_tgt, num_sms);
 	if (!p3d_visc_self_form_applies(reg, p)) return base;
-	return std::max(base, p3d_visc_self_ws_bytes(reg, p.n_tgt, num_sms));
+	const size_t self = p3d_visc_self_ws_bytes(reg, p.n_tgt, num_sms);
+	return self == SIZE_MAX ? base : std::max(base, self);
 }
 
 cudaError_t p3d_visc(int reg, const P3DViscProblem& p, const LaunchEnv& env) {

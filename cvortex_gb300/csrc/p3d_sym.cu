@@ -43,6 +43,7 @@
 // reference; every wait on a tile is bounded (tile_stream.cuh).
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdlib>
 #include <type_traits>
 
@@ -546,12 +547,18 @@ SymPlan sym_plan(int n, int nc, int capacity, size_t ws_cap) {
 	return pl;
 }
 
-// Largest workspace the self-interaction form asks of its caller.
-constexpr size_t kSymWsCap = size_t(4) << 30;
+// Largest workspace the self-interaction form asks of its caller (the slots
+// grow as blocks x particles: 1M particles, fused: 3.1 GB; 4M: 14 GB).
+constexpr size_t kSymWsCap = size_t(16) << 30;
 
+// The workspace of the form, or SIZE_MAX where the cap leaves fewer than two
+// items per resident CTA (blocks so long that the GPU would idle; the
+// ordered-pair kernels then serve the call).
 template <class Op>
 size_t sym_ws_bytes(int n, int num_sms, size_t ws_cap) {
-	return sym_plan(n, Op::NC, num_sms * sym_occupancy<Op>(), ws_cap ? ws_cap : kSymWsCap).ws_bytes;
+	const int capacity = num_sms * sym_occupancy<Op>();
+	const SymPlan pl = sym_plan(n, Op::NC, capacity, ws_cap ? ws_cap : kSymWsCap);
+	return pl.n_items < 2 * capacity ? SIZE_MAX : pl.ws_bytes;
 }
 
 template <class Op>

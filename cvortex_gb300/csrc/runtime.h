@@ -70,6 +70,14 @@ struct DeviceContext {
 	LaunchEnv env() const;
 	// Make sure the workspace holds `bytes`.
 	cudaError_t ensure_ws(size_t bytes) { return ws.ensure(bytes); }
+	// The workspace for `want` bytes or, if that cannot be allocated, for
+	// `fallback` bytes (the launchers then take a form that fits it).
+	cudaError_t ensure_ws_or(size_t want, size_t fallback) {
+		const cudaError_t e = ws.ensure(want);
+		if (e == cudaSuccess || fallback >= want) return e;
+		(void)cudaGetLastError();   // the failed allocation is not the call's error
+		return ws.ensure(fallback);
+	}
 };
 
 class Runtime {
