@@ -69,6 +69,17 @@ void gather_f3d_host(const cvtx_F3D* const* src, int n, float4* out) {
 
 // True when the measurement points are the gathered particles' coordinates,
 // bit for bit: the velocity call is then the particles acting on themselves.
+bool points2_are_coords(const bsv_V2f* mes, const float4* rec, int n) {
+	int differ = 0;
+#pragma omp parallel for schedule(static) reduction(|: differ) if (n >= kParallelGather)
+	for (int i = 0; i < n; ++i) {
+		const float4 q = rec[i];
+		const float c[2] = {q.x, q.y};
+		differ |= std::memcmp(c, mes[i].x, sizeof c) != 0;
+	}
+	return !differ;
+}
+
 bool points_are_coords(const bsv_V3f* mes, const float4* rec, int n) {
 	int differ = 0;
 #pragma omp parallel for schedule(static) reduction(|: differ) if (n >= kParallelGather)
@@ -345,18 +356,22 @@ CVTX_EXPORT void cvtx_P2D_M2M_vel(const cvtx_P2D** src, const int n, const bsv_V
 		const size_t sb = size_t(n) * 16, tb = size_t(m) * 16, ob = size_t(m) * 8;
 		float4* hs = job.stage(c->h_src, c->src, sb);
 		if (hs) gather_p2d_host(src, n, hs);
-		float4* ht = hs ? job.stage(c->h_tgt, c->tgt, tb) : nullptr;
+		// points that are the particles' own positions bit for bit: the
+		// particle records serve as targets (no upload, self-interaction form)
+		const bool alias = hs && m == n && n >= kSelfCheckMin && points2_are_coords(mes, hs, n);
+		float4* ht = (hs && !alias) ? job.stage(c->h_tgt, c->tgt, tb) : nullptr;
 		if (ht) pack_v2_host(mes, m, ht);
 		job.ensure_out(c->out0, c->h_out0, ob);
-		job.check(c->ensure_ws(p2d_vel_ws_bytes(reg, n, m, c->num_sms)), "workspace");
+		P2DVelProblem p;
+		p.src = static_cast<const float4*>(c->src.ptr); p.n_src = n;
+		p.tgt = static_cast<const float4*>(alias ? c->src.ptr : c->tgt.ptr); p.n_tgt = m;
+		p.out = static_cast<float*>(c->out0.ptr);
+		p.sigma = sigma;
+		job.check(c->ensure_ws_or(p2d_vel_ws_bytes_for(reg, p, c->num_sms),
+			p2d_vel_ws_bytes(reg, n, m, c->num_sms)), "workspace");
 		if (job.begin()) {
 			job.upload(c->h_src, c->src, sb);
-			job.upload(c->h_tgt, c->tgt, tb);
-			P2DVelProblem p;
-			p.src = static_cast<const float4*>(c->src.ptr); p.n_src = n;
-			p.tgt = static_cast<const float4*>(c->tgt.ptr); p.n_tgt = m;
-			p.out = static_cast<float*>(c->out0.ptr);
-			p.sigma = sigma;
+			if (!alias) job.upload(c->h_tgt, c->tgt, tb);
 			job.check(p2d_vel(reg, p, c->env()), "kernel launch");
 			if (job.finish(c->out0, c->h_out0, ob)) std::memcpy(out, c->h_out0.ptr, ob);
 		}
@@ -391,15 +406,16 @@ CVTX_EXPORT void cvtx_P2D_M2M_visc_dvort(const cvtx_P2D** src, const int n,
 		float4* ht = (!alias && hs) ? job.stage(c->h_tgt, c->tgt, tb) : nullptr;
 		if (ht) gather_p2d_host(ind, m, ht);
 		job.ensure_out(c->out0, c->h_out0, ob);
-		job.check(c->ensure_ws(p2d_visc_ws_bytes(reg, n, m, c->num_sms)), "workspace");
+		P2DViscProblem p;
+		p.src = static_cast<const float4*>(c->src.ptr); p.n_src = n;
+		p.tgt = static_cast<const float4*>(alias ? c->src.ptr : c->tgt.ptr); p.n_tgt = m;
+		p.out = static_cast<float*>(c->out0.ptr);
+		p.sigma = sigma; p.nu = nu;
+		job.check(c->ensure_ws_or(p2d_visc_ws_bytes_for(reg, p, c->num_sms),
+			p2d_visc_ws_bytes(reg, n, m, c->num_sms)), "workspace");
 		if (job.begin()) {
 			job.upload(c->h_src, c->src, sb);
 			if (!alias) job.upload(c->h_tgt, c->tgt, tb);
-			P2DViscProblem p;
-			p.src = static_cast<const float4*>(c->src.ptr); p.n_src = n;
-			p.tgt = static_cast<const float4*>(alias ? c->src.ptr : c->tgt.ptr); p.n_tgt = m;
-			p.out = static_cast<float*>(c->out0.ptr);
-			p.sigma = sigma; p.nu = nu;
 			job.check(p2d_visc(reg, p, c->env()), "kernel launch");
 			if (job.finish(c->out0, c->h_out0, ob)) std::memcpy(out, c->h_out0.ptr, ob);
 		}

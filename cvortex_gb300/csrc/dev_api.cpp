@@ -151,13 +151,14 @@ CVTX_EXPORT int cvtx_gb300_dev_P2D_M2M_vel(const void* src, int n_src, const voi
 	if (n_tgt <= 0) return 0;
 	if (n_src < 0 || !tgt || !out || bad_reg(reg)) return -1;
 	DevCall c(stream);
-	int st = c.prepare(p2d_vel_ws_bytes(reg, n_src, n_tgt, c.ctx ? c.ctx->num_sms : 1),
-		"cvtx_gb300_dev_P2D_M2M_vel");
-	if (st) return st;
 	P2DVelProblem p;
 	p.src = static_cast<const float4*>(src); p.n_src = n_src;
 	p.tgt = static_cast<const float4*>(tgt); p.n_tgt = n_tgt;
 	p.out = out; p.sigma = sigma;
+	const int sms = c.ctx ? c.ctx->num_sms : 1;
+	int st = c.prepare(p2d_vel_ws_bytes_for(reg, p, sms), "cvtx_gb300_dev_P2D_M2M_vel",
+		p2d_vel_ws_bytes(reg, n_src, n_tgt, sms));
+	if (st) return st;
 	return c.done(p2d_vel(reg, p, c.env()), "cvtx_gb300_dev_P2D_M2M_vel");
 }
 
@@ -172,13 +173,14 @@ CVTX_EXPORT int cvtx_gb300_dev_P2D_M2M_visc(const void* src, int n_src, const vo
 		const cudaError_t e = cudaMemsetAsync(out, 0, sizeof(float) * size_t(n_tgt), c.stream);
 		return e == cudaSuccess ? 0 : -2;
 	}
-	int st = c.prepare(p2d_visc_ws_bytes(reg, n_src, n_tgt, c.ctx ? c.ctx->num_sms : 1),
-		"cvtx_gb300_dev_P2D_M2M_visc");
-	if (st) return st;
 	P2DViscProblem p;
 	p.src = static_cast<const float4*>(src); p.n_src = n_src;
 	p.tgt = static_cast<const float4*>(tgt); p.n_tgt = n_tgt;
 	p.out = out; p.sigma = sigma; p.nu = nu;
+	const int sms = c.ctx ? c.ctx->num_sms : 1;
+	int st = c.prepare(p2d_visc_ws_bytes_for(reg, p, sms), "cvtx_gb300_dev_P2D_M2M_visc",
+		p2d_visc_ws_bytes(reg, n_src, n_tgt, sms));
+	if (st) return st;
 	return c.done(p2d_visc(reg, p, c.env()), "cvtx_gb300_dev_P2D_M2M_visc");
 }
 

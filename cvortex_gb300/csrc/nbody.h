@@ -173,10 +173,30 @@ size_t p3d_vort_ws_bytes(int reg, int n_src, int n_tgt, int num_sms);
 cudaError_t p3d_vort(int reg, const P3DVortProblem& p, const LaunchEnv& env);
 
 size_t p2d_vel_ws_bytes(int reg, int n_src, int n_tgt, int num_sms);
+// As above, or the larger workspace of the self-interaction form when that
+// form applies to the problem (the same rule for the viscous exchange).
+size_t p2d_vel_ws_bytes_for(int reg, const P2DVelProblem& p, int num_sms);
 cudaError_t p2d_vel(int reg, const P2DVelProblem& p, const LaunchEnv& env);
+// The velocity scale of the reference (1/(2 pi), with 1/sigma^2 for the
+// rho-normalised regularisations).
+double p2d_vel_scale(int reg, float sigma);
 
 size_t p2d_visc_ws_bytes(int reg, int n_src, int n_tgt, int num_sms);
+size_t p2d_visc_ws_bytes_for(int reg, const P2DViscProblem& p, int num_sms);
 cudaError_t p2d_visc(int reg, const P2DViscProblem& p, const LaunchEnv& env);
+
+// P2D self-interaction form (p2d_sym.cu): the records are their own targets
+// (tgt == src, n_tgt == n_src, at least CVTX_GB300_SYM_MIN particles), each
+// unordered pair evaluated once. p2d_vel / p2d_visc take it under the same
+// conditions as p3d_induce takes the P3D form (and, for the velocity, no
+// launch configuration forced by CVTX_GB300_P2D_CFG); *_self_ws_bytes is
+// SIZE_MAX where the workspace cap would leave too few work items.
+bool p2d_vel_self_form_applies(const P2DVelProblem& p);
+size_t p2d_vel_self_ws_bytes(int reg, int n, int num_sms, size_t ws_cap = 0);
+cudaError_t p2d_vel_self(int reg, const P2DVelProblem& p, const LaunchEnv& env);
+bool p2d_visc_self_form_applies(int reg, const P2DViscProblem& p);
+size_t p2d_visc_self_ws_bytes(int reg, int n, int num_sms, size_t ws_cap = 0);
+cudaError_t p2d_visc_self(int reg, const P2DViscProblem& p, const LaunchEnv& env);
 
 size_t f3d_vel_ws_bytes(int n_fil, int n_tgt, int num_sms);
 cudaError_t f3d_vel(const F3DVelProblem& p, const LaunchEnv& env);

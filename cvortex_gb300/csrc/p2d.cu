@@ -5,6 +5,7 @@
 // reference CPU path src/P2D.cpp:49-69 (velocity) and :167-194 (viscous
 // exchange). Same CTA shape as p3d.cu; a P2D source record is one float4
 // (x, y, Gamma, area), so a 512-record tile is 8 KB.
+#include <cstdint>
 #include <cmath>
 #include <cstdlib>
 #include <type_traits>
@@ -541,6 +542,28 @@ cudaError_t visc_r(const P2DViscProblem& p, const LaunchEnv& env) {
 
 }  // namespace
 
+double p2d_vel_scale(int reg, float sigma) { return vel_scale(reg, sigma); }
+
+static bool use_vel_self(const P2DVelProblem& p, int cta_src_cap) {
+	return cta_src_cap == 0 && p2d_env_cfg() < 0 && p2d_vel_self_form_applies(p);
+}
+
+size_t p2d_vel_ws_bytes_for(int reg, const P2DVelProblem& p, int num_sms) {
+	if (p.n_tgt <= 0) return 0;
+	const size_t base = p2d_vel_ws_bytes(reg, p.n_src, p.n_tgt, num_sms);
+	if (!use_vel_self(p, 0)) return base;
+	const size_t self = p2d_vel_self_ws_bytes(reg, p.n_tgt, num_sms);
+	return self == SIZE_MAX ? base : std::max(base, self);
+}
+
+size_t p2d_visc_ws_bytes_for(int reg, const P2DViscProblem& p, int num_sms) {
+	if (p.n_tgt <= 0) return 0;
+	const size_t base = p2d_visc_ws_bytes(reg, p.n_src, p.n_tgt, num_sms);
+	if (!p2d_visc_self_form_applies(reg, p)) return base;
+	const size_t self = p2d_visc_self_ws_bytes(reg, p.n_tgt, num_sms);
+	return self == SIZE_MAX ? base : std::max(base, self);
+}
+
 size_t p2d_vel_ws_bytes(int reg, int n_src, int n_tgt, int num_sms) {
 	if (n_tgt <= 0) return 0;
 	switch (reg) {
@@ -553,6 +576,10 @@ size_t p2d_vel_ws_bytes(int reg, int n_src, int n_tgt, int num_sms) {
 
 cudaError_t p2d_vel(int reg, const P2DVelProblem& p, const LaunchEnv& env) {
 	if (p.n_tgt <= 0) return cudaSuccess;
+	if (reg >= 0 && reg <= 3 && use_vel_self(p, env.cta_src_cap) &&
+		p2d_vel_self_ws_bytes(reg, p.n_tgt, env.num_sms, env.cap_to_ws ? env.ws_bytes : 0) <=
+			env.ws_bytes)
+		return p2d_vel_self(reg, p, env);
 	switch (reg) {
 	case 0: return vel_r<Reg::Singular>(p, env);
 	case 1: return vel_r<Reg::Winckelmans>(p, env);
@@ -571,6 +598,10 @@ size_t p2d_visc_ws_bytes(int reg, int n_src, int n_tgt, int num_sms) {
 
 cudaError_t p2d_visc(int reg, const P2DViscProblem& p, const LaunchEnv& env) {
 	if (p.n_tgt <= 0) return cudaSuccess;
+	if (env.cta_src_cap == 0 && p2d_visc_self_form_applies(reg, p) &&
+		p2d_visc_self_ws_bytes(reg, p.n_tgt, env.num_sms, env.cap_to_ws ? env.ws_bytes : 0) <=
+			env.ws_bytes)
+		return p2d_visc_self(reg, p, env);
 	if (reg == int(Reg::Winckelmans)) return visc_r<Reg::Winckelmans>(p, env);
 	if (reg == int(Reg::Gaussian)) return visc_r<Reg::Gaussian>(p, env);
 	return cudaErrorInvalidValue;

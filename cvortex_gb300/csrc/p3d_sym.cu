@@ -16,40 +16,16 @@
 // One evaluation of the pair's weights (and of co, d.co, the viscous
 // difference) thus serves both particles.
 //
-// Work decomposition (deterministic, no floating-point atomics):
-// * The particles are cut into nb blocks of S (a multiple of the 512-target
-//   pass of a CTA; the last block may be shorter). A work item is a block
-//   pair (bi, bj), bi <= bj; a persistent grid claims items through an atomic
-//   counter, largest first.
-// * Item (bi, bj), bi < bj: for each pass of 512 particles of block bi (held
-//   in registers, two per f32x2 lane pair), the records of block bj stream
-//   through shared memory in 256-record tiles (bulk copies). Within a warp
-//   the 32 records of a group are visited in a rotation: at step k lane l
-//   pairs its four particles with record (l + k) mod 32, whose running sums
-//   travel with it from lane to lane by shuffles and are back at their home
-//   lane after 32 steps. The four warps' sums per record are added in warp
-//   order in shared memory and added into the workspace slot (bi, record).
-//   The bi particles' own sums are folded per tile into compensated
-//   (hi, lo) pairs and written to slot (bj, particle) after the pass.
-// * Item (b, b): every ordered pair of the block, into slot (b, particle):
-//   the per-call CTA body (induce2_block) for the induced velocity and
-//   stretching, the same rotation with the record side left out for the
-//   viscous exchange.
-// * Every particle thus has exactly nb slot partials (one per partner
-//   block); a finalize kernel adds them in block order in FP64 and applies
-//   the output transforms. The result does not depend on scheduling.
-//
-// Coincident distinct particles contribute nothing to each other, as in the
-// reference; every wait on a tile is bounded (tile_stream.cuh).
-#include <algorithm>
-#include <cmath>
+// The rotation that evaluates each unordered pair once is in sym.cuh; the
+// diagonal blocks of the induced velocity / stretching run the per-call CTA
+// body (p3d_induce.cuh). Coincident distinct particles contribute nothing to
+// each other, as in the reference.
 #include <cstdint>
-#include <cstdlib>
 #include <type_traits>
 
 #include "nbody.h"
 #include "p3d_induce.cuh"
-#include "plan.cuh"
+#include "sym.cuh"
 
 namespace cvtx {
 
@@ -58,25 +34,11 @@ RegConsts make_reg_consts_host(float sigma);
 
 namespace {
 
-constexpr int kSymNT = 128;                    // threads per CTA
-constexpr int kSymTPT = 4;                     // particles per thread and pass
-constexpr int kSymH = kSymTPT / 2;             // f32x2 lane pairs per thread
-constexpr int kSymPass = kSymNT * kSymTPT;     // particles of block bi per pass
-constexpr int kSymWarps = kSymNT / 32;
 // Resident CTAs per SM the registers are sized for (167 registers for the
 // fused pair). Sizing for two (217 registers) measured 5-7 % slower.
-constexpr int kSymMinBlocks = 3;
+constexpr int kP3DSymMinBlocks = 3;
 
-// ---- pair operations -------------------------------------------------------
-// An operation supplies: NC sums per particle; the per-lane particle data
-// (Tgt: four particles as two f32x2 lane pairs) and its loader (indices
-// clamped below `lim`); step<FULL, SYM>, one lane's particles against one
-// record, adding to the particles' packed sums `acc` and (SYM) to the
-// record's running sums `js`; write, the output of a particle from its FP64
-// sums; kUnroll, the rotation steps unrolled (timed on a GB300 per op; two
-// particles per thread instead of four measured 5-9 % slower).
-// FULL = false zeroes the pair for a lane whose record lies past the
-// end of the block (`valid` false).
+// ---- pair operations (the interface is described in sym.cuh) --------------
 
 // Induced velocity and/or stretching (reference src/P3D.cpp:51-114).
 template <Reg R, bool VEL, bool DV>
@@ -86,6 +48,8 @@ struct InduceSym {
 	static constexpr int NC = InduceNC<VEL, DV>::value;
 	// fused, 1M cube: 4 -> 967, 8 -> 947, 2 -> 937 G/s; one output alone: 8
 	static constexpr int kUnroll = (VEL && DV) ? 4 : 8;
+	static constexpr int kRec = 2, kTile = kP3DTile, kMinBlocks = kP3DSymMinBlocks;
+	static constexpr bool kOwnDiagonal = true;
 	struct Tgt {
 		float2 tx[kSymH], ty[kSymH], tz[kSymH], ax[kSymH], ay[kSymH], az[kSymH];
 		float2 nax[kSymH], nay[kSymH], naz[kSymH];
@@ -110,11 +74,12 @@ struct InduceSym {
 	}
 
 	template <bool FULL, bool SYM>
-	__device__ __forceinline__ static void step(const Consts& kc, float4 sp, float4 sv,
+	__device__ __forceinline__ static void step(const Consts& kc, const float4* __restrict__ r,
 		bool valid, const Tgt& g, float2 (&acc)[NC][kSymH], float (&js)[NC])
 	{
 		constexpr bool kFinite = FiniteAtZero<R>::value;
 		const RegConsts& rc = kc.rc;
+		float4 sp = r[0], sv = r[1];
 		if (!FULL && !valid) {
 			sp = make_float4(0.f, 0.f, 0.f, 0.f);
 			sv = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -195,6 +160,26 @@ struct InduceSym {
 	{
 		write_induce<VEL, DV>(p, kc, t, s);
 	}
+
+	// A diagonal item: the per-call CTA body over the block's ordered pairs.
+	__device__ __forceinline__ static bool diagonal(const Problem& p, const Consts& kc,
+		const SymArgs& a, int b, unsigned char* smem, unsigned* err, unsigned& tcount)
+	{
+		const int n = p.n_tgt;
+		const int b0 = b * a.S;
+		const int b1 = min(n, b0 + a.S);
+		Problem q = p;
+		q.n_tgt = b1;      // targets of this block only; loads clamp below b1
+		for (int tb = b0; tb < b1; tb += kSymPass) {
+			const bool ok = induce2_block<R, VEL, DV, kSymTPT, kSymNT, 2>(q, kc, tb, b0, b1 - b0,
+				smem, err, tcount, [&](int t, const double* s) {
+#pragma unroll
+					for (int c = 0; c < NC; ++c) a.slots[(size_t(b) * NC + c) * n + t] = float(s[c]);
+				});
+			if (!ok) return false;
+		}
+		return true;
+	}
 };
 
 // Viscous vorticity exchange (PSE, reference src/P3D.cpp:116-144): the
@@ -210,6 +195,8 @@ struct ViscSym {
 	static constexpr int NC = 3;
 	// 100k ring: 16 -> 1,966, 8 -> 1,943, 4 -> 1,925, 2 -> 1,821 G/s
 	static constexpr int kUnroll = 16;
+	static constexpr int kRec = 2, kTile = kP3DTile, kMinBlocks = kP3DSymMinBlocks;
+	static constexpr bool kOwnDiagonal = false;
 	struct Tgt {
 		float2 ntx[kSymH], nty[kSymH], ntz[kSymH], tv[kSymH], nax[kSymH], nay[kSymH], naz[kSymH];
 	};
@@ -231,9 +218,10 @@ struct ViscSym {
 	}
 
 	template <bool FULL, bool SYM>
-	__device__ __forceinline__ static void step(const Consts& vc, float4 sp, float4 sv,
+	__device__ __forceinline__ static void step(const Consts& vc, const float4* __restrict__ r,
 		bool valid, const Tgt& g, float2 (&acc)[NC][kSymH], float (&js)[NC])
 	{
+		float4 sp = r[0], sv = r[1];
 		if (!FULL && !valid) {
 			sp = make_float4(0.f, 0.f, 0.f, 0.f);
 			sv = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -275,318 +263,6 @@ struct ViscSym {
 	}
 };
 
-// ---- the rotation ------------------------------------------------------------
-template <int NC>
-constexpr size_t sym_smem_bytes() {
-	// tile stages, (hi, lo) per pass particle and sum, and two buffers of
-	// per-warp record sums [2][warps][NC][32]
-	return P3DStream::kSmemBytes + size_t(2) * NC * kSymPass * sizeof(float) +
-		size_t(2) * kSymWarps * NC * 32 * sizeof(float);
-}
-
-// Fire-and-forget add to global memory (no value returned, so the thread
-// does not wait for it).
-__device__ __forceinline__ void red_add_f32(float* p, float v) {
-	asm volatile("red.global.add.f32 [%0], %1;" :: "l"(p), "f"(v) : "memory");
-}
-
-// One 32-record group: 32 rotation steps; with SYM the group records' sums
-// come back at their home lanes in js. (Passing the records' data along
-// with their sums by shuffles, instead of reading them from shared memory at
-// every step, measured no faster on a GB300.)
-template <class Op, bool FULL, bool SYM>
-__device__ __forceinline__ void sym_group(const typename Op::Consts& kc,
-	const float4* __restrict__ grp, int gcnt, int lane, const typename Op::Tgt& g,
-	float2 (&acc)[Op::NC][kSymH], float (&js)[Op::NC])
-{
-	const int from = (lane + 1) & 31;
-#pragma unroll Op::kUnroll
-	for (int k = 0; k < 32; ++k) {
-		const int jl = (lane + k) & 31;
-		const float4 sp = grp[2 * jl];
-		const float4 sv = grp[2 * jl + 1];
-		Op::template step<FULL, SYM>(kc, sp, sv, jl < gcnt, g, acc, js);
-		if (SYM) {
-#pragma unroll
-			for (int c = 0; c < Op::NC; ++c) js[c] = __shfl_sync(0xffffffffu, js[c], from);
-		}
-	}
-}
-
-struct SymArgs {
-	int S;            // block length (multiple of kSymPass)
-	int nb;           // blocks
-	float* slots;     // [nb][NC][n] partial sums
-};
-
-// Item (bi, bj): all passes of block bi against block bj. SYM (bi < bj)
-// also adds the bj records' sums into their slots (bi, record); without it
-// (a diagonal item) only the bi particles' sums are formed. Returns false if
-// a tile wait timed out.
-template <class Op, bool SYM>
-__device__ __forceinline__ bool sym_item(const typename Op::Problem& p,
-	const typename Op::Consts& kc, const SymArgs& a, int bi, int bj, unsigned char* smem,
-	unsigned* err, unsigned& tcount)
-{
-	constexpr int NC = Op::NC;
-	const int n = p.n_tgt;
-	float* hi = reinterpret_cast<float*>(smem + P3DStream::kSmemBytes);
-	float* lo = hi + NC * kSymPass;
-	float* jbuf = lo + NC * kSymPass;            // [2][warps][NC][32]
-	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-	const int i0 = bi * a.S;
-	const int i1 = min(n, i0 + a.S);              // whole passes when bi < bj
-	const int j0 = bj * a.S;
-	const int nj = min(n, j0 + a.S) - j0;
-	int par = 0;
-	for (int tb = i0; tb < i1; tb += kSymPass) {
-		typename Op::Tgt g;
-		Op::load(p, tb, tid, i1, g);
-#pragma unroll
-		for (int i = 0; i < NC * kSymTPT; ++i) { hi[i * kSymNT + tid] = 0.f; lo[i * kSymNT + tid] = 0.f; }
-		int toff = 0;   // first record of the current tile within block bj
-
-		auto tile_fn = [&](const float4* __restrict__ st, int cnt) {
-			float2 acc[NC][kSymH];
-#pragma unroll
-			for (int c = 0; c < NC; ++c)
-#pragma unroll
-				for (int h = 0; h < kSymH; ++h) acc[c][h] = make_float2(0.f, 0.f);
-			const int ng = (cnt + 31) >> 5;
-			for (int gi = 0; gi < ng; ++gi) {
-				const int gcnt = min(32, cnt - 32 * gi);
-				const float4* grp = st + 2 * 32 * gi;
-				float js[NC];
-#pragma unroll
-				for (int c = 0; c < NC; ++c) js[c] = 0.f;
-				if (gcnt == 32) sym_group<Op, true, SYM>(kc, grp, gcnt, lane, g, acc, js);
-				else sym_group<Op, false, SYM>(kc, grp, gcnt, lane, g, acc, js);
-				if (SYM) {
-					// the group's record sums are back at their home lanes
-					float* wb = jbuf + ((par * kSymWarps + warp) * NC) * 32;
-#pragma unroll
-					for (int c = 0; c < NC; ++c) wb[c * 32 + lane] = js[c];
-					__syncthreads();
-					// warp-ordered sum per record, added to its slot (zeroed
-					// before the launch). A slot element is only ever added to
-					// by this thread of this CTA, in pass order, so the sum is
-					// deterministic; the reduction does not wait for the memory.
-					const float* rb = jbuf + (par * kSymWarps * NC) * 32;
-					for (int v = tid; v < NC * 32; v += kSymNT) {
-						const int c = v >> 5, l = v & 31;
-						if (l >= gcnt) continue;
-						float s = rb[v];
-#pragma unroll
-						for (int w = 1; w < kSymWarps; ++w) s += rb[w * NC * 32 + v];
-						red_add_f32(a.slots + (size_t(bi) * NC + c) * n +
-							(j0 + toff + 32 * gi + l), s);
-					}
-					par ^= 1;
-				}
-			}
-#pragma unroll
-			for (int c = 0; c < NC; ++c) {
-#pragma unroll
-				for (int h = 0; h < kSymH; ++h)
-#pragma unroll
-					for (int e = 0; e < 2; ++e) {
-						const int i = (c * kSymTPT + 2 * h + e) * kSymNT + tid;
-						float hh = hi[i], ll = lo[i];
-						fold_twosum(hh, ll, e == 0 ? acc[c][h].x : acc[c][h].y);
-						hi[i] = hh; lo[i] = ll;
-					}
-			}
-			toff += cnt;
-		};
-		if (!P3DStream::run_continue(smem, p.src, j0, nj, err, tcount, tile_fn)) return false;
-#pragma unroll
-		for (int k = 0; k < kSymTPT; ++k) {
-			const int t = tb + k * kSymNT + tid;
-			if (t >= i1) continue;
-#pragma unroll
-			for (int c = 0; c < NC; ++c) {
-				const int i = (c * kSymTPT + k) * kSymNT + tid;
-				a.slots[(size_t(bj) * NC + c) * n + t] = float(double(hi[i]) + double(lo[i]));
-			}
-		}
-	}
-	return true;
-}
-
-// The diagonal item (b, b) of the induced velocity / stretching: the per-call
-// CTA body over the block's ordered pairs.
-template <Reg R, bool VEL, bool DV>
-__device__ __forceinline__ bool sym_diagonal(const P3DInduceProblem& p, const InduceConsts& kc,
-	const SymArgs& a, int b, unsigned char* smem, unsigned* err, unsigned& tcount,
-	InduceSym<R, VEL, DV>*)
-{
-	constexpr int NC = InduceNC<VEL, DV>::value;
-	const int n = p.n_tgt;
-	const int b0 = b * a.S;
-	const int b1 = min(n, b0 + a.S);
-	P3DInduceProblem q = p;
-	q.n_tgt = b1;      // targets of this block only; loads clamp below b1
-	for (int tb = b0; tb < b1; tb += kSymPass) {
-		const bool ok = induce2_block<R, VEL, DV, kSymTPT, kSymNT, 2>(q, kc, tb, b0, b1 - b0,
-			smem, err, tcount, [&](int t, const double* s) {
-#pragma unroll
-				for (int c = 0; c < NC; ++c) a.slots[(size_t(b) * NC + c) * n + t] = float(s[c]);
-			});
-		if (!ok) return false;
-	}
-	return true;
-}
-
-template <Reg R>
-__device__ __forceinline__ bool sym_diagonal(const P3DViscProblem& p, const SymViscConsts& vc,
-	const SymArgs& a, int b, unsigned char* smem, unsigned* err, unsigned& tcount, ViscSym<R>*)
-{
-	return sym_item<ViscSym<R>, false>(p, vc, a, b, b, smem, err, tcount);
-}
-
-// Item `it` of nb blocks, largest first: the full off-diagonal pairs column
-// by column (bj = 1 .. nb-2, bi < bj; items running at the same time share
-// their bj block in L2), then the pairs with the short last block, then the
-// diagonal blocks (about 2/3 of an off-diagonal pair's time).
-__device__ __forceinline__ int2 sym_item_at(int it, int nb) {
-	const long long a = (long long)(nb - 1) * (nb - 2) / 2;
-	if (it < a) {
-		long long j = (long long)((1.0 + sqrt(1.0 + 8.0 * double(it))) * 0.5);
-		while (j * (j - 1) / 2 > it) --j;
-		while ((j + 1) * j / 2 <= it) ++j;
-		return make_int2(int(it - j * (j - 1) / 2), int(j));
-	}
-	if (it < a + nb - 1) return make_int2(int(it - a), nb - 1);
-	const int b = int(it - a - (nb - 1));
-	return make_int2(b, b);
-}
-
-template <class Op>
-__global__ void __launch_bounds__(kSymNT, kSymMinBlocks)
-p3d_sym_kernel(const typename Op::Problem p, const typename Op::Consts kc, const SymArgs a,
-	int n_items, unsigned* next, unsigned* err)
-{
-	extern __shared__ __align__(16) unsigned char smem[];
-	__shared__ int item_s;
-	if (blockDim.x != kSymNT) {
-		if (threadIdx.x == 0) atomicOr(err, kErrBadLaunch);
-		return;
-	}
-	if (!P3DStream::init(smem, err)) return;
-	unsigned tcount = 0;
-	const int n = p.n_tgt;
-	for (;;) {
-		if (threadIdx.x == 0) item_s = int(atomicAdd(next, 1u));
-		__syncthreads();
-		const int it = item_s;
-		__syncthreads();
-		if (it >= n_items) return;
-		const int2 w = sym_item_at(it, a.nb);
-		const int bi = w.x, bj = w.y;
-		if (bi < 0 || bj < bi || bj >= a.nb || bi * a.S >= n) {
-			if (threadIdx.x == 0) atomicOr(err, kErrBadWork);
-			continue;
-		}
-		const bool ok = bi == bj
-			? sym_diagonal(p, kc, a, bi, smem, err, tcount, static_cast<Op*>(nullptr))
-			: sym_item<Op, true>(p, kc, a, bi, bj, smem, err, tcount);
-		if (!ok) return;
-	}
-}
-
-// Sum of every particle's nb slot partials in block order (FP64), then the
-// output transforms.
-template <class Op>
-__global__ void p3d_sym_finalize(const typename Op::Problem p, const typename Op::Consts kc,
-	const float* __restrict__ slots, int nb)
-{
-	constexpr int NC = Op::NC;
-	const int t = blockIdx.x * blockDim.x + threadIdx.x;
-	const int n = p.n_tgt;
-	if (t >= n) return;
-	double s[NC];
-#pragma unroll
-	for (int c = 0; c < NC; ++c) s[c] = 0.0;
-	for (int b = 0; b < nb; ++b)
-#pragma unroll
-		for (int c = 0; c < NC; ++c) s[c] += double(slots[(size_t(b) * NC + c) * n + t]);
-	Op::write(p, kc, t, s);
-}
-
-template <class Op>
-int sym_occupancy() {
-	static const int occ = resident_ctas(p3d_sym_kernel<Op>, kSymNT, sym_smem_bytes<Op::NC>());
-	return occ;
-}
-
-// Block plan: about eight items per resident CTA (so that the last items
-// leave little of the GPU idle), blocks a multiple of the 512-particle pass,
-// and a workspace within `ws_cap` bytes (fewer, longer blocks otherwise).
-struct SymPlan {
-	int S = 0, nb = 0, n_items = 0;
-	size_t slots_bytes = 0, counter_off = 0, ws_bytes = 0;
-};
-
-SymPlan sym_plan(int n, int nc, int capacity, size_t ws_cap) {
-	SymPlan pl;
-	int nb = int(std::ceil(std::sqrt(16.0 * capacity)));
-	for (;; nb = nb * 7 / 8) {
-		nb = std::max(nb, 2);
-		int S = (n + nb - 1) / nb;
-		S = ((S + kSymPass - 1) / kSymPass) * kSymPass;
-		const int nbr = (n + S - 1) / S;
-		pl.S = S;
-		pl.nb = nbr;
-		pl.n_items = nbr * (nbr + 1) / 2;
-		pl.slots_bytes = size_t(nbr) * nc * size_t(n) * sizeof(float);
-		pl.slots_bytes = (pl.slots_bytes + 255) & ~size_t(255);
-		pl.counter_off = pl.slots_bytes;
-		pl.ws_bytes = pl.counter_off + 256;
-		if (pl.ws_bytes <= ws_cap || nb == 2) break;
-	}
-	return pl;
-}
-
-// Largest workspace the self-interaction form asks of its caller (the slots
-// grow as blocks x particles: 1M particles, fused: 3.1 GB; 4M: 14 GB).
-constexpr size_t kSymWsCap = size_t(16) << 30;
-
-// The workspace of the form, or SIZE_MAX where the cap leaves fewer than two
-// items per resident CTA (blocks so long that the GPU would idle; the
-// ordered-pair kernels then serve the call).
-template <class Op>
-size_t sym_ws_bytes(int n, int num_sms, size_t ws_cap) {
-	const int capacity = num_sms * sym_occupancy<Op>();
-	const SymPlan pl = sym_plan(n, Op::NC, capacity, ws_cap ? ws_cap : kSymWsCap);
-	return pl.n_items < 2 * capacity ? SIZE_MAX : pl.ws_bytes;
-}
-
-template <class Op>
-cudaError_t sym_launch(const typename Op::Problem& p, const typename Op::Consts& kc,
-	const LaunchEnv& env)
-{
-	const int occ = sym_occupancy<Op>();
-	const SymPlan pl = sym_plan(p.n_tgt, Op::NC, env.num_sms * occ,
-		env.cap_to_ws ? env.ws_bytes : std::min(env.ws_bytes, kSymWsCap));
-	if (pl.ws_bytes > env.ws_bytes || !env.ws) return cudaErrorInvalidValue;
-	unsigned char* ws = static_cast<unsigned char*>(env.ws);
-	unsigned* d_next = reinterpret_cast<unsigned*>(ws + pl.counter_off);
-	// the slots and the item counter start at zero
-	const cudaError_t e = cudaMemsetAsync(ws, 0, pl.ws_bytes, env.stream);
-	if (e != cudaSuccess) return e;
-	SymArgs a;
-	a.S = pl.S;
-	a.nb = pl.nb;
-	a.slots = reinterpret_cast<float*>(ws);
-	const int grid = std::max(1, std::min(pl.n_items, env.num_sms * occ));
-	p3d_sym_kernel<Op><<<grid, kSymNT, sym_smem_bytes<Op::NC>(), env.stream>>>(
-		p, kc, a, pl.n_items, d_next, env.err);
-	count_launch();
-	p3d_sym_finalize<Op><<<(p.n_tgt + 255) / 256, 256, 0, env.stream>>>(p, kc, a.slots, pl.nb);
-	count_launch();
-	return cudaGetLastError();
-}
-
 template <class F>
 auto with_reg_ops_sym(int reg, unsigned ops, F&& f) {
 	auto by_ops = [&](auto rt) {
@@ -603,18 +279,8 @@ auto with_reg_ops_sym(int reg, unsigned ops, F&& f) {
 	}
 }
 
-int sym_min_particles() {
-	static const int min_n = [] {
-		const char* e = std::getenv("CVTX_GB300_SYM_MIN");
-		return (e && *e) ? std::atoi(e) : 32768;
-	}();
-	return min_n;
-}
-
 bool self_shape(const float4* src, int n_src, const float4* tgt, int tstride, int n_tgt) {
-	const int min_n = sym_min_particles();
-	return min_n > 0 && tgt == src && tstride == 2 && n_tgt == n_src && n_tgt >= min_n &&
-		n_tgt >= 2 * kSymPass;
+	return tgt == src && tstride == 2 && n_tgt == n_src && sym_size_ok(n_tgt);
 }
 
 }  // namespace

@@ -1,9 +1,11 @@
-"""Self-interaction form (each unordered pair once; csrc/p3d_sym.cu): the
-particles acting on themselves through the device API and through the cvtx_
-ABI (velocity at the particles' own coordinates, stretching with the pointer
-array as its own target array), for every regularisation and op, on ragged
-sizes, against the oracle on sampled targets and against the ordered-pair
-kernels (forced through the tuning table) on every target."""
+"""Self-interaction form (each unordered pair once; csrc/sym.cuh with the
+operations of csrc/p3d_sym.cu and csrc/p2d_sym.cu): the particles acting on
+themselves through the device API and through the cvtx_ ABI (velocity at the
+particles' own coordinates, stretching and viscous exchange with the pointer
+array as its own target array), P3D and P2D, for every regularisation and
+op, on ragged sizes, against the oracle on sampled targets and against the
+ordered-pair kernels (forced through the tuning table, or given the targets
+as a separate copy) on every target."""
 import ctypes as C
 
 import numpy as np
@@ -124,3 +126,76 @@ def test_viscous_self_form_vs_oracle_and_ordered_pairs(gpu, reg, n):
     # the cvtx_ ABI with the pointer array as its own targets takes the same form
     via_abi = gpu.p3d_visc(p, p, reg, 0.05, nu, same=True)
     assert exact.rel_l2(via_abi, self_out) <= 1e-6
+
+
+def _records2d(q):
+    return np.ascontiguousarray(
+        np.stack([q["coord"][:, 0], q["coord"][:, 1], q["vorticity"], q["area"]], 1), np.float32)
+
+
+def _dev_p2d(gpu, torch, rec, tgt, n, reg, nu=None):
+    sh = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    if nu is None:
+        out = torch.full((n, 2), float("nan"), dtype=torch.float32, device="cuda")
+        assert gpu.lib.cvtx_gb300_dev_P2D_M2M_vel(rec.data_ptr(), n, tgt.data_ptr(), n,
+                                                  out.data_ptr(), abi.REG_IDS[reg], 0.05, sh) == 0
+    else:
+        out = torch.full((n,), float("nan"), dtype=torch.float32, device="cuda")
+        assert gpu.lib.cvtx_gb300_dev_P2D_M2M_visc(rec.data_ptr(), n, tgt.data_ptr(), n,
+                                                   out.data_ptr(), abi.REG_IDS[reg], 0.05,
+                                                   C.c_float(nu), sh) == 0
+    assert gpu.lib.cvtx_gb300_dev_status(sh) == 0
+    return out.cpu().numpy()
+
+
+@pytest.mark.parametrize("reg", REGS)
+@pytest.mark.parametrize("n", [33_001, 70_000])
+def test_p2d_velocity_self_form(gpu, reg, n):
+    """P2D velocity at the particles' own positions in the self-interaction
+    form, against the ordered-pair kernel (the points passed as a separate
+    copy of the records) on every particle and the oracle on sampled ones."""
+    import torch
+    q = workloads.gaussian_patch_2d(n, seed=91 + n % 7)
+    rec = torch.from_numpy(_records2d(q)).cuda()
+    got = _dev_p2d(gpu, torch, rec, rec, n, reg)
+    ordered = _dev_p2d(gpu, torch, rec, rec.clone(), n, reg)
+    assert np.all(np.isfinite(got))
+    assert exact.rel_l2(got, ordered) <= TOL, exact.rel_l2(got, ordered)
+    idx = np.sort(np.random.Generator(np.random.PCG64(92)).choice(n, 1024, replace=False))
+    ref = oracle.p2d_vel(q, q["coord"][idx], reg, 0.05)
+    check(got[idx], ref, reg, q["coord"][idx], q["coord"], 0.05)
+
+
+@pytest.mark.parametrize("reg", ["winckelmans", "gaussian"])
+@pytest.mark.parametrize("n", [33_001, 70_000])
+def test_p2d_viscous_self_form(gpu, reg, n):
+    """P2D viscous exchange of the particles with themselves in the
+    self-interaction form, against the ordered-pair kernel on every particle
+    and the oracle on sampled ones."""
+    import torch
+    nu = 1e-3
+    q = workloads.gaussian_patch_2d(n, seed=93 + n % 7)
+    rec = torch.from_numpy(_records2d(q)).cuda()
+    got = _dev_p2d(gpu, torch, rec, rec, n, reg, nu)
+    ordered = _dev_p2d(gpu, torch, rec, rec.clone(), n, reg, nu)
+    assert np.all(np.isfinite(got))
+    assert exact.rel_l2(got, ordered) <= TOL, exact.rel_l2(got, ordered)
+    idx = np.sort(np.random.Generator(np.random.PCG64(94)).choice(n, 1024, replace=False))
+    ref = oracle.p2d_visc(q, q[idx], reg, 0.05, nu)
+    check(got[idx], ref, reg, q["coord"][idx], q["coord"], 0.05)
+
+
+def test_p2d_self_form_through_the_abi(gpu):
+    """cvtx_P2D_M2M_vel at the particles' own coordinates and
+    cvtx_P2D_M2M_visc_dvort with the pointer array as its own targets take
+    the self-interaction form: equal to the device calls in that form."""
+    import torch
+    n = 50_000
+    q = workloads.gaussian_patch_2d(n, seed=95)
+    rec = torch.from_numpy(_records2d(q)).cuda()
+    vel = gpu.p2d_vel(q, q["coord"].copy(), "winckelmans", 0.05)
+    visc = gpu.p2d_visc(q, q, "winckelmans", 0.05, 1e-3, same=True)
+    assert exact.rel_l2(vel, _dev_p2d(gpu, torch, rec, rec, n, "winckelmans")) <= 1e-6
+    assert exact.rel_l2(visc, _dev_p2d(gpu, torch, rec, rec, n, "winckelmans", 1e-3)) <= 1e-6
+    idx = np.arange(0, n, 53)
+    check(vel[idx], oracle.p2d_vel(q, q["coord"][idx], "winckelmans", 0.05))
