@@ -26,9 +26,12 @@ RegConsts make_reg_consts_host(float sigma);
 namespace {
 
 // Records of one float4 (x, y, Gamma, area), the per-call kernels' 512-record
-// tiles; the registers are sized for four resident CTAs per SM.
+// tiles. Unroll and resident CTAs per SM timed on a GB300 (200,000-particle
+// patch, G interactions/s): Gaussian velocity 6 CTAs, unroll 8: 2,822
+// (4 CTAs: 2,714; unroll 16: 2,658); Winckelmans velocity 4 CTAs, unroll
+// 16: 3,551 (unroll 8: 3,496; 6 CTAs: 3,323); viscous exchange 4 CTAs,
+// unroll 16: Gaussian 4,403, Winckelmans 3,114 (unroll 8: 4,335 / 3,036).
 constexpr int kP2DSymTile = 512;
-constexpr int kP2DSymMinBlocks = 4;
 
 template <Reg R> struct HFinite2 { static constexpr bool value = true; };
 template <> struct HFinite2<Reg::Singular> { static constexpr bool value = false; };
@@ -39,8 +42,8 @@ struct VelSym2D {
 	using Problem = P2DVelProblem;
 	struct Consts { RegConsts rc; double scale; };
 	static constexpr int NC = 2;
-	static constexpr int kUnroll = 8;
-	static constexpr int kRec = 1, kTile = kP2DSymTile, kMinBlocks = kP2DSymMinBlocks;
+	static constexpr int kUnroll = R == Reg::Gaussian ? 8 : 16;
+	static constexpr int kRec = 1, kTile = kP2DSymTile, kMinBlocks = R == Reg::Gaussian ? 6 : 4;
 	static constexpr bool kOwnDiagonal = false;
 	struct Tgt { float2 tx[kSymH], ty[kSymH], tg[kSymH]; };
 
@@ -103,8 +106,8 @@ struct ViscSym2D {
 	using Problem = P2DViscProblem;
 	struct Consts { RegConsts rc; double scale; };
 	static constexpr int NC = 1;
-	static constexpr int kUnroll = 8;
-	static constexpr int kRec = 1, kTile = kP2DSymTile, kMinBlocks = kP2DSymMinBlocks;
+	static constexpr int kUnroll = 16;
+	static constexpr int kRec = 1, kTile = kP2DSymTile, kMinBlocks = 4;
 	static constexpr bool kOwnDiagonal = false;
 	struct Tgt { float2 ntx[kSymH], nty[kSymH], ntg[kSymH], ta[kSymH]; };
 
