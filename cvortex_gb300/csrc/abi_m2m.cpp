@@ -299,18 +299,23 @@ CVTX_EXPORT void cvtx_P3D_M2M_vort(const cvtx_P3D** src, const int n, const bsv_
 		const size_t sb = size_t(n) * 32, tb = size_t(m) * 16, ob = size_t(m) * 12;
 		float4* hs = job.stage(c->h_src, c->src, sb);
 		if (hs) gather_p3d_host(src, n, hs);
-		float4* ht = hs ? job.stage(c->h_tgt, c->tgt, tb) : nullptr;
+		// points that are the particles' own positions bit for bit (the
+		// Pedrizzetti relaxation): the records serve as targets
+		const bool alias = hs && m == n && n >= kSelfCheckMin && points_are_coords(mes, hs, n);
+		float4* ht = (hs && !alias) ? job.stage(c->h_tgt, c->tgt, tb) : nullptr;
 		if (ht) pack_v3_host(mes, m, ht);
 		job.ensure_out(c->out0, c->h_out0, ob);
-		job.check(c->ensure_ws(p3d_vort_ws_bytes(reg, n, m, c->num_sms)), "workspace");
+		P3DVortProblem p;
+		p.src = static_cast<const float4*>(c->src.ptr); p.n_src = n;
+		p.tgt = static_cast<const float4*>(alias ? c->src.ptr : c->tgt.ptr);
+		p.tstride = alias ? 2 : 1; p.n_tgt = m;
+		p.out = static_cast<float*>(c->out0.ptr);
+		p.sigma = sigma;
+		job.check(c->ensure_ws_or(p3d_vort_ws_bytes_for(reg, p, c->num_sms),
+			p3d_vort_ws_bytes(reg, n, m, c->num_sms)), "workspace");
 		if (job.begin()) {
 			job.upload(c->h_src, c->src, sb);
-			job.upload(c->h_tgt, c->tgt, tb);
-			P3DVortProblem p;
-			p.src = static_cast<const float4*>(c->src.ptr); p.n_src = n;
-			p.tgt = static_cast<const float4*>(c->tgt.ptr); p.tstride = 1; p.n_tgt = m;
-			p.out = static_cast<float*>(c->out0.ptr);
-			p.sigma = sigma;
+			if (!alias) job.upload(c->h_tgt, c->tgt, tb);
 			job.check(p3d_vort(reg, p, c->env()), "kernel launch");
 			if (job.finish(c->out0, c->h_out0, ob)) std::memcpy(out, c->h_out0.ptr, ob);
 		}

@@ -135,13 +135,14 @@ CVTX_EXPORT int cvtx_gb300_dev_P3D_M2M_vort(const void* src, int n_src, const vo
 	if (n_tgt <= 0) return 0;
 	if (n_src < 0 || !tgt || !out || bad_reg(reg) || tgt_stride < 1) return -1;
 	DevCall c(stream);
-	int st = c.prepare(p3d_vort_ws_bytes(reg, n_src, n_tgt, c.ctx ? c.ctx->num_sms : 1),
-		"cvtx_gb300_dev_P3D_M2M_vort");
-	if (st) return st;
 	P3DVortProblem p;
 	p.src = static_cast<const float4*>(src); p.n_src = n_src;
 	p.tgt = static_cast<const float4*>(tgt); p.tstride = tgt_stride; p.n_tgt = n_tgt;
 	p.out = out; p.sigma = sigma;
+	const int sms = c.ctx ? c.ctx->num_sms : 1;
+	int st = c.prepare(p3d_vort_ws_bytes_for(reg, p, sms), "cvtx_gb300_dev_P3D_M2M_vort",
+		p3d_vort_ws_bytes(reg, n_src, n_tgt, sms));
+	if (st) return st;
 	return c.done(p3d_vort(reg, p, c.env()), "cvtx_gb300_dev_P3D_M2M_vort");
 }
 

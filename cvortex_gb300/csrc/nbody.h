@@ -170,7 +170,14 @@ size_t p3d_visc_self_ws_bytes(int reg, int n, int num_sms, size_t ws_cap = 0);
 cudaError_t p3d_visc_self(int reg, const P3DViscProblem& p, const LaunchEnv& env);
 
 size_t p3d_vort_ws_bytes(int reg, int n_src, int n_tgt, int num_sms);
+size_t p3d_vort_ws_bytes_for(int reg, const P3DVortProblem& p, int num_sms);
 cudaError_t p3d_vort(int reg, const P3DVortProblem& p, const LaunchEnv& env);
+// The vorticity field at the particles' own positions (p3d_sym.cu), under
+// the conditions of p3d_self_form_applies (Winckelmans, planetary,
+// Gaussian; no configuration forced by CVTX_GB300_VORT_CFG).
+bool p3d_vort_self_form_applies(int reg, const P3DVortProblem& p);
+size_t p3d_vort_self_ws_bytes(int reg, int n, int num_sms, size_t ws_cap = 0);
+cudaError_t p3d_vort_self(int reg, const P3DVortProblem& p, const LaunchEnv& env);
 
 size_t p2d_vel_ws_bytes(int reg, int n_src, int n_tgt, int num_sms);
 // As above, or the larger workspace of the self-interaction form when that

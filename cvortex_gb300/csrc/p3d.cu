@@ -618,30 +618,8 @@ p3d_vort_kernel(const P3DVortProblem p, const RegConsts rc, float cutoff,
 	}
 }
 
-// Packed form (two targets per f32x2 lane pair). zeta's constant factor
-// (7.5 Winckelmans, 3 planetary, sqrt(2/pi) Gaussian) is left to the FP64
-// output scale, so each pair evaluates only the shape of zeta.
-template <Reg R> struct ZetaShape2;
-template <> struct ZetaShape2<Reg::Winckelmans> {
-	static constexpr double kFactor = 7.5;
-	__device__ __forceinline__ static float2 z(float2 r2, const RegConsts& c) {
-		const float2 q = __ffma2_rn(r2, bc2(c.inv_s2), bc2(1.f));
-		const float2 s = make_float2(rsqrt_approx(q.x), rsqrt_approx(q.y));
-		const float2 s2 = __fmul2_rn(s, s);
-		return __fmul2_rn(__fmul2_rn(s2, s2), __fmul2_rn(s2, s));   // (1 + rho^2)^-3.5
-	} };
-template <> struct ZetaShape2<Reg::Planetary> {
-	static constexpr double kFactor = 3.0;
-	__device__ __forceinline__ static float2 z(float2 r2, const RegConsts& c) {
-		return make_float2(r2.x < c.s2 ? 1.f : 0.f, r2.y < c.s2 ? 1.f : 0.f);
-	} };
-template <> struct ZetaShape2<Reg::Gaussian> {
-	static constexpr double kFactor = 0.7978845608028654;   // sqrt(2/pi)
-	__device__ __forceinline__ static float2 z(float2 r2, const RegConsts& c) {
-		const float2 a = __fmul2_rn(r2, bc2(c.exp2_half));
-		return make_float2(ex2_approx(a.x), ex2_approx(a.y));       // exp(-rho^2/2)
-	} };
-
+// Packed form (two targets per f32x2 lane pair); zeta's shape is
+// ZetaShape2 (p3d_induce.cuh), its constant factor in the FP64 output scale.
 template <Reg R, int TPT, int NT>
 __global__ void __launch_bounds__(NT)
 p3d_vort2_kernel(const P3DVortProblem p, const RegConsts rc, float cutoff,
@@ -1116,13 +1094,17 @@ cudaError_t p3d_visc(int reg, const P3DViscProblem& p, const LaunchEnv& env) {
 // one.
 // The singular regularisation's zeta is identically zero (reference
 // src/VortFunc.cpp:68-70), so its field is zero without evaluating any pair.
-int vort_cfg(int n_tgt) {
+int vort_forced_cfg() {
 	static const int forced = [] {
 		const char* e = std::getenv("CVTX_GB300_VORT_CFG");
 		if (!e || !*e) return -1;
 		const int c = std::atoi(e);
 		return (c >= 0 && c <= 3) ? c : -1;
 	}();
+	return forced;
+}
+int vort_cfg(int n_tgt) {
+	const int forced = vort_forced_cfg();
 	if (forced >= 0) return forced;
 	return n_tgt < kSmallTargets ? 0 : n_tgt < 65536 ? 3 : 2;
 }
@@ -1159,10 +1141,25 @@ size_t p3d_vort_ws_bytes(int reg, int n_src, int n_tgt, int num_sms) {
 	return ws;
 }
 
+static bool use_vort_self(int reg, const P3DVortProblem& p, int cta_src_cap) {
+	return cta_src_cap == 0 && vort_forced_cfg() < 0 && p3d_vort_self_form_applies(reg, p);
+}
+
+size_t p3d_vort_ws_bytes_for(int reg, const P3DVortProblem& p, int num_sms) {
+	const size_t base = p3d_vort_ws_bytes(reg, p.n_src, p.n_tgt, num_sms);
+	if (p.n_tgt <= 0 || !use_vort_self(reg, p, 0)) return base;
+	const size_t self = p3d_vort_self_ws_bytes(reg, p.n_tgt, num_sms);
+	return self == SIZE_MAX ? base : std::max(base, self);
+}
+
 cudaError_t p3d_vort(int reg, const P3DVortProblem& p, const LaunchEnv& env) {
 	if (p.n_tgt <= 0) return cudaSuccess;
 	if (reg == int(Reg::Singular))
 		return cudaMemsetAsync(p.out, 0, sizeof(float) * 3 * size_t(p.n_tgt), env.stream);
+	if (use_vort_self(reg, p, env.cta_src_cap) &&
+		p3d_vort_self_ws_bytes(reg, p.n_tgt, env.num_sms, env.cap_to_ws ? env.ws_bytes : 0) <=
+			env.ws_bytes)
+		return p3d_vort_self(reg, p, env);
 	return with_vort_cfg(reg, p.n_tgt, [&](auto tag) {
 		using T = decltype(tag);
 		return launch_vort<T::R, T::TPT, 128, T::PK>(p, env);

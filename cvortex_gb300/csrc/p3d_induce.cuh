@@ -29,6 +29,31 @@ using P3DStream = P3DStreamT<kP3DTile>;
 template <Reg R> struct FiniteAtZero { static constexpr bool value = true; };
 template <> struct FiniteAtZero<Reg::Singular> { static constexpr bool value = false; };
 
+// The shape of zeta for two pairs at a time (f32x2). zeta's constant factor
+// (7.5 Winckelmans, 3 planetary, sqrt(2/pi) Gaussian) is left to the FP64
+// output scale, so each pair evaluates only the shape of zeta.
+template <Reg R> struct ZetaShape2;
+template <> struct ZetaShape2<Reg::Winckelmans> {
+	static constexpr double kFactor = 7.5;
+	__device__ __forceinline__ static float2 z(float2 r2, const RegConsts& c) {
+		const float2 q = __ffma2_rn(r2, bc2(c.inv_s2), bc2(1.f));
+		const float2 s = make_float2(rsqrt_approx(q.x), rsqrt_approx(q.y));
+		const float2 s2 = __fmul2_rn(s, s);
+		return __fmul2_rn(__fmul2_rn(s2, s2), __fmul2_rn(s2, s));   // (1 + rho^2)^-3.5
+	} };
+template <> struct ZetaShape2<Reg::Planetary> {
+	static constexpr double kFactor = 3.0;
+	__device__ __forceinline__ static float2 z(float2 r2, const RegConsts& c) {
+		return make_float2(r2.x < c.s2 ? 1.f : 0.f, r2.y < c.s2 ? 1.f : 0.f);
+	} };
+template <> struct ZetaShape2<Reg::Gaussian> {
+	static constexpr double kFactor = 0.7978845608028654;   // sqrt(2/pi)
+	__device__ __forceinline__ static float2 z(float2 r2, const RegConsts& c) {
+		const float2 a = __fmul2_rn(r2, bc2(c.exp2_half));
+		return make_float2(ex2_approx(a.x), ex2_approx(a.y));       // exp(-rho^2/2)
+	} };
+
+
 template <bool VEL, bool DV> struct InduceNC { static constexpr int value = (VEL ? 3 : 0) + (DV ? 6 : 0); };
 
 struct InduceConsts {

@@ -1,6 +1,6 @@
 // p3d_sym.cu -- P3D interactions of a particle set on itself, each unordered
-// pair evaluated once: vortex stretching (with or without the velocity) and
-// the viscous vorticity exchange.
+// pair evaluated once: the velocity and / or the vortex stretching, the
+// viscous vorticity exchange and the vorticity field.
 //
 // The all-pairs calls of the reference (src/P3D.cpp:343-366, 387-410,
 // 432-456) are most often made with the particles as their own targets (a
@@ -263,6 +263,95 @@ struct ViscSym {
 	}
 };
 
+// Vorticity field at the particles' own positions (reference
+// src/P3D.cpp:298-322, the CPU path with its 5 sigma box): the pair's weight
+// zeta(r) and its box test (on |d_x|, |d_y|, |d_z|, unchanged when d changes
+// sign) serve both particles: t gets zeta alpha_s, s gets zeta alpha_t. The
+// pair of a particle with itself counts once, as in the reference.
+struct SymVortConsts { RegConsts rc; float cutoff; double scale; };
+
+template <Reg R>
+struct VortSym {
+	using Problem = P3DVortProblem;
+	using Consts = SymVortConsts;
+	static constexpr int NC = 3;
+	static constexpr int kUnroll = 8;
+	static constexpr double kFactor = ZetaShape2<R>::kFactor;   // in the output scale
+	static constexpr int kRec = 2, kTile = kP3DTile, kMinBlocks = kP3DSymMinBlocks;
+	static constexpr bool kOwnDiagonal = false;
+	struct Tgt {
+		float2 ntx[kSymH], nty[kSymH], ntz[kSymH], ax[kSymH], ay[kSymH], az[kSymH];
+	};
+
+	__device__ __forceinline__ static void load(const Problem& p, int tb, int tid, int lim,
+		Tgt& g)
+	{
+#pragma unroll
+		for (int h = 0; h < kSymH; ++h) {
+			const int t0 = min(tb + (2 * h) * kSymNT + tid, lim - 1);
+			const int t1 = min(tb + (2 * h + 1) * kSymNT + tid, lim - 1);
+			const float4 q0 = p.tgt[2 * size_t(t0)], q1 = p.tgt[2 * size_t(t1)];
+			const float4 v0 = p.tgt[2 * size_t(t0) + 1], v1 = p.tgt[2 * size_t(t1) + 1];
+			g.ntx[h] = make_float2(-q0.x, -q1.x); g.nty[h] = make_float2(-q0.y, -q1.y);
+			g.ntz[h] = make_float2(-q0.z, -q1.z);
+			g.ax[h] = make_float2(v0.x, v1.x); g.ay[h] = make_float2(v0.y, v1.y);
+			g.az[h] = make_float2(v0.z, v1.z);
+		}
+	}
+
+	template <bool FULL, bool SYM>
+	__device__ __forceinline__ static void step(const Consts& kc, const float4* __restrict__ r,
+		bool valid, const Tgt& g, float2 (&acc)[NC][kSymH], float (&js)[NC])
+	{
+		float4 sp = r[0], sv = r[1];
+		if (!FULL && !valid) {
+			sp = make_float4(0.f, 0.f, 0.f, 0.f);
+			sv = make_float4(0.f, 0.f, 0.f, 0.f);
+		}
+		const float2 sx = bc2(sp.x), sy = bc2(sp.y), sz = bc2(sp.z);
+#pragma unroll
+		for (int h = 0; h < kSymH; ++h) {
+			// source - target, rounded once as in the per-call kernels
+			const float2 dx = __fadd2_rn(sx, g.ntx[h]);
+			const float2 dy = __fadd2_rn(sy, g.nty[h]);
+			const float2 dz = __fadd2_rn(sz, g.ntz[h]);
+			const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+			float2 z = ZetaShape2<R>::z(r2, kc.rc);
+			const bool in0 = max3_nan(fabsf(dx.x), fabsf(dy.x), fabsf(dz.x)) < kc.cutoff;
+			const bool in1 = max3_nan(fabsf(dx.y), fabsf(dy.y), fabsf(dz.y)) < kc.cutoff;
+			z.x = in0 ? z.x : 0.f;
+			z.y = in1 ? z.y : 0.f;
+			if (!FULL && !valid) z = make_float2(0.f, 0.f);
+			acc[0][h] = __ffma2_rn(z, bc2(sv.x), acc[0][h]);
+			acc[1][h] = __ffma2_rn(z, bc2(sv.y), acc[1][h]);
+			acc[2][h] = __ffma2_rn(z, bc2(sv.z), acc[2][h]);
+			if (SYM) {
+				js[0] = fmaf(z.x, g.ax[h].x, fmaf(z.y, g.ax[h].y, js[0]));
+				js[1] = fmaf(z.x, g.ay[h].x, fmaf(z.y, g.ay[h].y, js[1]));
+				js[2] = fmaf(z.x, g.az[h].x, fmaf(z.y, g.az[h].y, js[2]));
+			}
+		}
+	}
+
+	__device__ __forceinline__ static void write(const Problem& p, const Consts& kc, int t,
+		const double* s)
+	{
+		float* o = p.out + 3 * size_t(t);
+		o[0] = float(kc.scale * s[0]);
+		o[1] = float(kc.scale * s[1]);
+		o[2] = float(kc.scale * s[2]);
+	}
+};
+
+template <class F>
+auto with_reg_vort(int reg, F&& f) {
+	switch (reg) {
+	case 1: return f(static_cast<VortSym<Reg::Winckelmans>*>(nullptr));
+	case 2: return f(static_cast<VortSym<Reg::Planetary>*>(nullptr));
+	default: return f(static_cast<VortSym<Reg::Gaussian>*>(nullptr));
+	}
+}
+
 template <class F>
 auto with_reg_ops_sym(int reg, unsigned ops, F&& f) {
 	auto by_ops = [&](auto rt) {
@@ -331,6 +420,30 @@ cudaError_t p3d_visc_self(int reg, const P3DViscProblem& p, const LaunchEnv& env
 		return sym_launch<ViscSym<Reg::Gaussian>>(p, vc, env);
 	}
 	return cudaErrorInvalidValue;
+}
+
+bool p3d_vort_self_form_applies(int reg, const P3DVortProblem& p) {
+	return reg >= 1 && reg <= 3 && self_shape(p.src, p.n_src, p.tgt, p.tstride, p.n_tgt);
+}
+
+size_t p3d_vort_self_ws_bytes(int reg, int n, int num_sms, size_t ws_cap) {
+	return with_reg_vort(reg, [&](auto* op) {
+		using Op = std::remove_pointer_t<decltype(op)>;
+		return sym_ws_bytes<Op>(n, num_sms, ws_cap);
+	});
+}
+
+cudaError_t p3d_vort_self(int reg, const P3DVortProblem& p, const LaunchEnv& env) {
+	if (reg < 1 || reg > 3) return cudaErrorInvalidValue;
+	return with_reg_vort(reg, [&](auto* op) {
+		using Op = std::remove_pointer_t<decltype(op)>;
+		const double s = p.sigma;
+		SymVortConsts kc;
+		kc.rc = make_reg_consts_host(p.sigma);
+		kc.cutoff = 5.f * p.sigma;
+		kc.scale = Op::kFactor / (4.0 * 3.14159265358979323846 * s * s * s);
+		return sym_launch<Op>(p, kc, env);
+	});
 }
 
 }  // namespace cvtx

@@ -205,3 +205,33 @@ def test_p2d_self_form_through_the_abi(gpu):
     assert exact.rel_l2(visc, _dev_p2d(gpu, torch, rec, rec, n, "winckelmans", 1e-3)) <= 1e-6
     idx = np.arange(0, n, 53)
     check(vel[idx], oracle.p2d_vel(q, q["coord"][idx], "winckelmans", 0.05))
+
+
+def _dev_vort(gpu, torch, rec, tgt, n, reg):
+    out = torch.full((n, 3), float("nan"), dtype=torch.float32, device="cuda")
+    sh = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert gpu.lib.cvtx_gb300_dev_P3D_M2M_vort(rec.data_ptr(), n, tgt.data_ptr(), 2, n,
+                                               out.data_ptr(), abi.REG_IDS[reg], 0.05, sh) == 0
+    assert gpu.lib.cvtx_gb300_dev_status(sh) == 0
+    return out.cpu().numpy()
+
+
+@pytest.mark.parametrize("reg", ["winckelmans", "planetary", "gaussian"])
+@pytest.mark.parametrize("n", [33_001, 70_000])
+def test_vorticity_field_self_form(gpu, reg, n):
+    """The vorticity field at the particles' own positions (5 sigma box) in
+    the self-interaction form, against the ordered-pair kernel on every
+    particle and the oracle on sampled ones; through the cvtx_ ABI (points
+    equal to the particles' coordinates, as the Pedrizzetti relaxation
+    passes them) the same form serves the call."""
+    import torch
+    p = workloads.vortex_ring(n, seed=96) if n == 70_000 else workloads.uniform_cube(n, seed=97)
+    rec = torch.from_numpy(_records(p)).cuda()
+    got = _dev_vort(gpu, torch, rec, rec, n, reg)
+    ordered = _dev_vort(gpu, torch, rec, rec.clone(), n, reg)
+    assert np.all(np.isfinite(got))
+    assert exact.rel_l2(got, ordered) <= TOL, exact.rel_l2(got, ordered)
+    idx = np.sort(np.random.Generator(np.random.PCG64(98)).choice(n, 1024, replace=False))
+    check(got[idx], oracle.p3d_vort(p, p["coord"][idx], reg, 0.05))
+    via_abi = gpu.p3d_vort(p, p["coord"].copy(), reg, 0.05)
+    assert exact.rel_l2(via_abi, got) <= 1e-6
