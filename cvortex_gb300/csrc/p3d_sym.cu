@@ -275,9 +275,11 @@ struct VortSym {
 	using Problem = P3DVortProblem;
 	using Consts = SymVortConsts;
 	static constexpr int NC = 3;
+	// 100k ring, G/s: 4 CTAs per SM (128 registers) 2,629 / 3,091 / 2,976
+	// (Winckelmans / planetary / Gaussian), 3 CTAs 2,545 / 2,876 / 2,852
 	static constexpr int kUnroll = 8;
 	static constexpr double kFactor = ZetaShape2<R>::kFactor;   // in the output scale
-	static constexpr int kRec = 2, kTile = kP3DTile, kMinBlocks = kP3DSymMinBlocks;
+	static constexpr int kRec = 2, kTile = kP3DTile, kMinBlocks = 4;
 	static constexpr bool kOwnDiagonal = false;
 	struct Tgt {
 		float2 ntx[kSymH], nty[kSymH], ntz[kSymH], ax[kSymH], ay[kSymH], az[kSymH];
