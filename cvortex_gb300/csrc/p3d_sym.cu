@@ -193,9 +193,12 @@ struct ViscSym {
 	using Problem = P3DViscProblem;
 	using Consts = SymViscConsts;
 	static constexpr int NC = 3;
-	// 100k ring: 16 -> 1,966, 8 -> 1,943, 4 -> 1,925, 2 -> 1,821 G/s
-	static constexpr int kUnroll = 16;
-	static constexpr int kRec = 2, kTile = kP3DTile, kMinBlocks = kP3DSymMinBlocks;
+	// 100k ring, Winckelmans: unroll 16 -> 1,966, 8 -> 1,943, 4 -> 1,925,
+	// 2 -> 1,821 G/s; Gaussian: 4 CTAs per SM, unroll 8 -> 2,232 (3 CTAs,
+	// unroll 16: 2,155)
+	static constexpr int kUnroll = R == Reg::Gaussian ? 8 : 16;
+	static constexpr int kRec = 2, kTile = kP3DTile;
+	static constexpr int kMinBlocks = R == Reg::Gaussian ? 4 : kP3DSymMinBlocks;
 	static constexpr bool kOwnDiagonal = false;
 	struct Tgt {
 		float2 ntx[kSymH], nty[kSymH], ntz[kSymH], tv[kSymH], nax[kSymH], nay[kSymH], naz[kSymH];
