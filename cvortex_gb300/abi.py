@@ -158,6 +158,7 @@ _EXT_SIGS = {
     "cvtx_gb300_P3D_M2M_vel_dvort": (_i, [_vp, _i, _vp, _vp, _VF, _f]),
     "cvtx_gb300_dev_P3D_M2M": (_i, [_vp, _i, _vp, _i, _i, _vp, _vp, _i, _f, _vp]),
     "cvtx_gb300_dev_P3D_M2M_visc": (_i, [_vp, _i, _vp, _i, _i, _vp, _i, _f, _f, _vp]),
+    "cvtx_gb300_dev_P3D_M2M_ws_bytes": (C.c_longlong, [_i, _i, _i, _i, _i, _i]),
     "cvtx_gb300_dev_P3D_M2M_vort": (_i, [_vp, _i, _vp, _i, _i, _vp, _i, _f, _vp]),
     "cvtx_gb300_dev_P2D_M2M_vel": (_i, [_vp, _i, _vp, _i, _vp, _i, _f, _vp]),
     "cvtx_gb300_dev_P2D_M2M_visc": (_i, [_vp, _i, _vp, _i, _vp, _i, _f, _f, _vp]),

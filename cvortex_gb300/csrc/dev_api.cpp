@@ -86,6 +86,24 @@ CVTX_EXPORT int cvtx_gb300_dev_P3D_M2M(const void* src, int n_src, const void* t
 	return c.done(p3d_induce(reg, ops, p, c.env()), "cvtx_gb300_dev_P3D_M2M");
 }
 
+CVTX_EXPORT long long cvtx_gb300_dev_P3D_M2M_ws_bytes(int n_src, int n_tgt, int self,
+	int reg, int ops, int form)
+{
+	if (n_src < 0 || n_tgt < 0 || bad_reg(reg) || ops < 1 || ops > 3 || (self && n_src != n_tgt))
+		return -1;
+	DevCall c(nullptr);
+	if (!c.ctx) return -1;
+	// only the pointers' equality matters to the choice of form
+	static const float4 dummy[2] = {};
+	P3DInduceProblem p;
+	p.src = dummy; p.n_src = n_src;
+	p.tgt = self ? dummy : dummy + 1; p.tstride = 2; p.n_tgt = n_tgt;
+	p.out_vel = nullptr; p.out_dvort = nullptr; p.sigma = 1.f;
+	const size_t b = form ? p3d_induce_ws_bytes_for(reg, unsigned(ops), p, c.ctx->num_sms)
+	                      : p3d_induce_ws_bytes(reg, unsigned(ops), n_src, n_tgt, c.ctx->num_sms);
+	return static_cast<long long>(b);
+}
+
 CVTX_EXPORT int cvtx_gb300_dev_P3D_step(void* rec, int n, float* vel, float* dvort, int reg,
 	float sigma, float dt, void* stream)
 {

@@ -11,7 +11,9 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 
@@ -21,13 +23,27 @@
 namespace cvtx {
 
 // ---- buffers ---------------------------------------------------------------
+// CVTX_GB300_WS_LIMIT (bytes): device buffers larger than this fail as an
+// out-of-memory cudaMalloc would (host-side fault injection for the tests of
+// the workspace fallbacks; unset, no limit).
+static size_t devbuf_limit() {
+	static const size_t lim = [] {
+		const char* e = std::getenv("CVTX_GB300_WS_LIMIT");
+		const long long v = (e && *e) ? std::atoll(e) : 0;
+		return v > 0 ? size_t(v) : SIZE_MAX;
+	}();
+	return lim;
+}
+
 cudaError_t DevBuf::ensure(size_t need) {
 	if (need <= bytes && ptr) return cudaSuccess;
+	if (need > devbuf_limit()) return cudaErrorMemoryAllocation;
 	if (need == 0) need = 256;
 	release();
 	size_t grow = need + need / 4;
-	cudaError_t e = cudaMalloc(&ptr, grow);
+	cudaError_t e = grow <= devbuf_limit() ? cudaMalloc(&ptr, grow) : cudaErrorMemoryAllocation;
 	if (e != cudaSuccess) {
+		(void)cudaGetLastError();   // retried at the size needed
 		ptr = nullptr;
 		bytes = 0;
 		e = cudaMalloc(&ptr, need);

@@ -315,7 +315,15 @@ SymPlan sym_plan(int n, int nc, int capacity, size_t ws_cap) {
 
 // Largest workspace the self-interaction form asks of its caller (the slots
 // grow as blocks x particles: 1M particles, fused: 3.1 GB; 4M: 14 GB).
-constexpr size_t kSymWsCap = size_t(16) << 30;
+// CVTX_GB300_SYM_WS_CAP (bytes) lowers it, e.g. to test the fallback.
+size_t sym_ws_cap() {
+	static const size_t cap = [] {
+		const char* e = std::getenv("CVTX_GB300_SYM_WS_CAP");
+		const long long v = (e && *e) ? std::atoll(e) : 0;
+		return v > 0 ? size_t(v) : size_t(16) << 30;
+	}();
+	return cap;
+}
 
 // The workspace of the form, or SIZE_MAX where the cap leaves fewer than two
 // items per resident CTA (blocks so long that the GPU would idle; the
@@ -323,7 +331,7 @@ constexpr size_t kSymWsCap = size_t(16) << 30;
 template <class Op>
 size_t sym_ws_bytes(int n, int num_sms, size_t ws_cap) {
 	const int capacity = num_sms * sym_occupancy<Op>();
-	const SymPlan pl = sym_plan(n, Op::NC, capacity, ws_cap ? ws_cap : kSymWsCap);
+	const SymPlan pl = sym_plan(n, Op::NC, capacity, ws_cap ? ws_cap : sym_ws_cap());
 	return pl.n_items < 2 * capacity ? SIZE_MAX : pl.ws_bytes;
 }
 
@@ -333,7 +341,7 @@ cudaError_t sym_launch(const typename Op::Problem& p, const typename Op::Consts&
 {
 	const int occ = sym_occupancy<Op>();
 	const SymPlan pl = sym_plan(p.n_tgt, Op::NC, env.num_sms * occ,
-		env.cap_to_ws ? env.ws_bytes : std::min(env.ws_bytes, kSymWsCap));
+		env.cap_to_ws ? env.ws_bytes : std::min(env.ws_bytes, sym_ws_cap()));
 	if (pl.ws_bytes > env.ws_bytes || !env.ws) return cudaErrorInvalidValue;
 	unsigned char* ws = static_cast<unsigned char*>(env.ws);
 	unsigned* d_next = reinterpret_cast<unsigned*>(ws + pl.counter_off);

@@ -91,6 +91,14 @@ CVTX_EXPORT int cvtx_gb300_P3D_M2M_vel_dvort(const cvtx_P3D** array_start,
 CVTX_EXPORT int cvtx_gb300_dev_P3D_M2M(const void* src, int n_src,
 	const void* tgt, int tgt_stride, int n_tgt, float* vel_out,
 	float* dvort_out, int reg, float regularisation_radius, void* stream);
+/* Workspace in bytes that cvtx_gb300_dev_P3D_M2M allocates (grow-only, per
+ * context) for n_tgt targets against n_src particles: self != 0 when the
+ * targets are the particles themselves (tgt == src, stride 2); ops 1 vel,
+ * 2 dvort, 3 both; form 0 the ordered-pair kernels, form 1 the form the call
+ * takes (the self-interaction form where it applies). -1 without an enabled
+ * GPU or on bad arguments. */
+CVTX_EXPORT long long cvtx_gb300_dev_P3D_M2M_ws_bytes(int n_src, int n_tgt, int self,
+	int reg, int ops, int form);
 CVTX_EXPORT int cvtx_gb300_dev_P3D_M2M_visc(const void* src, int n_src,
 	const void* tgt, int tgt_stride, int n_tgt, float* out, int reg,
 	float regularisation_radius, float kinematic_visc, void* stream);

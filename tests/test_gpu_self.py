@@ -235,3 +235,65 @@ def test_vorticity_field_self_form(gpu, reg, n):
     check(got[idx], oracle.p3d_vort(p, p["coord"][idx], reg, 0.05))
     via_abi = gpu.p3d_vort(p, p["coord"].copy(), reg, 0.05)
     assert exact.rel_l2(via_abi, got) <= 1e-6
+
+
+FALLBACK_CHILD = r"""
+import ctypes as C, sys
+import numpy as np, torch
+sys.path.insert(0, sys.argv[2])
+from cvortex_gb300 import abi, workloads
+cv = abi.Cvtx(); cv.initialise()
+lib = cv.lib
+n = int(sys.argv[3])
+p = workloads.uniform_cube(n, seed=99)
+r = np.zeros((n, 8), np.float32)
+r[:, 0:3], r[:, 3], r[:, 4:7] = p["coord"], p["volume"], p["vorticity"]
+rec = torch.from_numpy(r).cuda()
+sh = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+outs = []
+for tgt in (rec, rec.clone()):          # the particles themselves, then a copy
+    v = torch.full((n, 3), float("nan"), device="cuda")
+    d = torch.full((n, 3), float("nan"), device="cuda")
+    rc = lib.cvtx_gb300_dev_P3D_M2M(rec.data_ptr(), n, tgt.data_ptr(), 2, n, v.data_ptr(),
+                                    d.data_ptr(), 1, 0.05, sh)
+    assert rc == 0 and lib.cvtx_gb300_dev_status(sh) == 0, cv.last_error()
+    outs.append(np.concatenate([v.cpu().numpy(), d.cpu().numpy()], 1))
+np.save(sys.argv[1], np.stack(outs))
+"""
+
+
+def _fallback_child(tmp_path, n, env):
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+    out = tmp_path / "fallback.npy"
+    root = Path(__file__).resolve().parents[1]
+    res = subprocess.run([sys.executable, "-c", FALLBACK_CHILD, str(out), str(root), str(n)],
+                         cwd=root, env=dict(os.environ, **env), capture_output=True, text=True,
+                         timeout=600)
+    assert res.returncode == 0, res.stderr[-2000:]
+    return np.load(out)
+
+
+def test_self_form_workspace_fallbacks(gpu, tmp_path):
+    """The ordered-pair kernels serve a call that would take the
+    self-interaction form (1) when the form's workspace cap leaves too few
+    work items (CVTX_GB300_SYM_WS_CAP lowered), and (2) when its workspace
+    cannot be allocated (CVTX_GB300_WS_LIMIT between the two forms'
+    workspaces: an injected out-of-memory). Either way the call succeeds and
+    equals the ordered-pair kernel on a copy of the particles bit for bit;
+    with neither, the form is taken (results differ in rounding only)."""
+    n = 40_000
+    q = gpu.lib.cvtx_gb300_dev_P3D_M2M_ws_bytes
+    ordered_ws, self_ws = q(n, n, 1, 1, 3, 0), q(n, n, 1, 1, 3, 1)
+    assert 0 < ordered_ws < self_ws, (ordered_ws, self_ws)
+    base = _fallback_child(tmp_path, n, {})
+    assert not np.array_equal(base[0], base[1])
+    assert exact.rel_l2(base[0], base[1]) <= TOL
+    capped = _fallback_child(tmp_path, n, {"CVTX_GB300_SYM_WS_CAP": str(1 << 20)})
+    assert np.array_equal(capped[0], capped[1])
+    limit = (ordered_ws + self_ws) // 2
+    limited = _fallback_child(tmp_path, n, {"CVTX_GB300_WS_LIMIT": str(limit)})
+    assert np.array_equal(limited[0], limited[1])
+    assert exact.rel_l2(limited[0], base[0]) <= TOL
