@@ -153,9 +153,10 @@ __device__ __forceinline__ float2 neg2f(float2 a) { return make_float2(-a.x, -a.
 // f3d_factor for two points at once (per lane). Where no pair of the warp's
 // live lanes lies beside its segment (d >= 0 everywhere: beyond the ends or
 // far away, most pairs of a sheet), only the product form is evaluated; the
-// result is the same as with the per-pair select. (Timed on a GB300, wake
-// sheet 100,000 x 100,000: velocity 673 -> 782, stretching 518 -> 571 G/s;
-// influence matrix 25,000 x 20,000: 0.818 -> 0.783 ms.)
+// result is the same as with the per-pair select. (Timed on a GB300: wake
+// sheet velocity, 50,000 x 50,000, 673 -> 782 G/s; stretching, 100,000 x
+// 100,000, 518 -> 571 G/s; influence matrix 25,000 x 20,000: 0.818 ->
+// 0.783 ms.)
 __device__ __forceinline__ void f3d_factor2(float2 q1, float2 q2, float2 d, float2 il1,
 	float2 il2, float2 cc, float2& num, float2& den)
 {
