@@ -15,13 +15,21 @@
 // The launch shape (targets per thread x threads per CTA) and the source chunk
 // per item are chosen by a built-in autotuner (cvtx_gb300_batch_tune) that
 // times every candidate on the batch itself.
+//
+// Problems whose targets are their own particles (tgt == src, stride 2, from
+// 4,096 particles; CVTX_GB300_SYM_MIN overrides, 0 switches it off) run in
+// the self-interaction form instead (p3d_sym_batch.h): a second persistent
+// launch over the block-pair items of all of them, then one finalize launch;
+// both are part of the captured graph.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
 
 #include "cvortex/cvtx_gb300.h"
 #include "p3d_induce.cuh"
+#include "p3d_sym_batch.h"
 #include "plan.cuh"
 #include "runtime.h"
 
@@ -174,6 +182,11 @@ struct cvtx_gb300_batch {
 	size_t n_counters = 1;          // per-target-block arrival counters in use
 	size_t smem = 0;
 	DevBuf d_probs, d_items, d_partial, d_counters, d_next, d_err;
+	// the self-interaction part
+	std::vector<char> in_sym;       // per problem: served by the self part
+	int n_sym_probs = 0, n_sym_items = 0, sym_grid = 0, sym_total = 0;
+	size_t sym_slot_bytes = 0;
+	DevBuf d_sprobs, d_sitems, d_sprefix, d_slots, d_snext;
 	cudaStream_t stream = nullptr;
 	cudaEvent_t ev_in = nullptr, ev_out = nullptr;
 	cudaGraph_t graph = nullptr;
@@ -218,6 +231,7 @@ int plan_batch(cvtx_gb300_batch* b, int shape, int chunk) {
 		bp.p.out_dvort = (b->ops & kOpDvort) ? q.dvort_out : nullptr;
 		bp.p.sigma = q.sigma;
 		bp.kc = make_induce_consts(b->reg, q.sigma);
+		if (b->in_sym[i]) continue;      // served by the self-interaction part
 		const int n_split = q.n_src > 0 ? std::max(1, (q.n_src + chunk - 1) / chunk) : 1;
 		int per = q.n_src > 0 ? (q.n_src + n_split - 1) / n_split : kP3DTile;
 		per = ((per + kP3DTile - 1) / kP3DTile) * kP3DTile;
@@ -272,19 +286,123 @@ int plan_batch(cvtx_gb300_batch* b, int shape, int chunk) {
 	return 0;
 }
 
+// Smallest problem of the self-interaction part (0: none).
+int batch_sym_min() {
+	static const int v = [] {
+		const char* e = std::getenv("CVTX_GB300_SYM_MIN");
+		return (e && *e) ? std::atoi(e) : 4096;
+	}();
+	return v;
+}
+
+// Select the problems of the self-interaction part, cut each into at most 16
+// blocks (a multiple of 512 particles), list their block-pair items largest
+// first and upload the tables. Independent of the ordered part's plan.
+int plan_sym(cvtx_gb300_batch* b) {
+	const int nc = (b->ops & kOpVel ? 3 : 0) + (b->ops & kOpDvort ? 6 : 0);
+	const int min_n = batch_sym_min();
+	b->in_sym.assign(b->in.size(), 0);
+	std::vector<SymBatchProblem> probs;
+	std::vector<size_t> slot_off;
+	std::vector<int> prefix;
+	struct Item { int4 w; double cost; };
+	std::vector<Item> items;
+	size_t slot_floats = 0;
+	long long total = 0;
+	for (size_t i = 0; i < b->in.size(); ++i) {
+		const cvtx_gb300_p3d_problem& q = b->in[i];
+		const int n = q.n_tgt;
+		if (min_n <= 0 || n < min_n || n < 1024 || q.tgt != q.src || q.tgt_stride != 2 ||
+			q.n_src != n)
+			continue;
+		b->in_sym[i] = 1;
+		const int nb_t = std::min(16, (n + 511) / 512);
+		const int S = 512 * ((n + 512 * nb_t - 1) / (512 * nb_t));
+		const int nb = (n + S - 1) / S;
+		SymBatchProblem r;
+		std::memset(&r, 0, sizeof r);
+		r.p.src = static_cast<const float4*>(q.src); r.p.n_src = n;
+		r.p.tgt = static_cast<const float4*>(q.src); r.p.tstride = 2; r.p.n_tgt = n;
+		r.p.out_vel = (b->ops & kOpVel) ? q.vel_out : nullptr;
+		r.p.out_dvort = (b->ops & kOpDvort) ? q.dvort_out : nullptr;
+		r.p.sigma = q.sigma;
+		r.kc = make_induce_consts(b->reg, q.sigma);
+		r.S = S;
+		r.nb = nb;
+		const int k = int(probs.size());
+		probs.push_back(r);
+		slot_off.push_back(slot_floats);
+		slot_floats += (size_t(nb) * nc * size_t(n) + 63) & ~size_t(63);
+		prefix.push_back(int(total));
+		total += n;
+		for (int bj = 0; bj < nb; ++bj)
+			for (int bi = 0; bi <= bj; ++bi) {
+				const double li = std::min(S, n - bi * S), lj = std::min(S, n - bj * S);
+				items.push_back({make_int4(k, bi, bj, 0), li * lj * (bi == bj ? 0.5 : 1.0)});
+			}
+	}
+	b->n_sym_probs = int(probs.size());
+	b->n_sym_items = int(items.size());
+	if (probs.empty()) return 0;
+	if (total > (long long)(1 << 30)) return fail(b, "self-interaction part too large", -1);
+	prefix.push_back(int(total));
+	b->sym_total = int(total);
+	std::stable_sort(items.begin(), items.end(),
+		[](const Item& a, const Item& c) { return a.cost > c.cost; });
+	b->sym_slot_bytes = slot_floats * sizeof(float);
+	cudaError_t e = b->d_slots.ensure(b->sym_slot_bytes);
+	if (e == cudaSuccess) e = b->d_sprobs.ensure(probs.size() * sizeof(SymBatchProblem));
+	if (e == cudaSuccess) e = b->d_sitems.ensure(items.size() * sizeof(int4));
+	if (e == cudaSuccess) e = b->d_sprefix.ensure(prefix.size() * sizeof(int));
+	if (e == cudaSuccess) e = b->d_snext.ensure(sizeof(unsigned));
+	if (e != cudaSuccess) return fail(b, std::string("allocation: ") + cudaGetErrorString(e), -2);
+	for (size_t k = 0; k < probs.size(); ++k)
+		probs[k].slots = static_cast<float*>(b->d_slots.ptr) + slot_off[k];
+	std::vector<int4> w(items.size());
+	for (size_t i = 0; i < items.size(); ++i) w[i] = items[i].w;
+	e = cudaMemcpy(b->d_sprobs.ptr, probs.data(), probs.size() * sizeof(SymBatchProblem),
+		cudaMemcpyHostToDevice);
+	if (e == cudaSuccess)
+		e = cudaMemcpy(b->d_sitems.ptr, w.data(), w.size() * sizeof(int4), cudaMemcpyHostToDevice);
+	if (e == cudaSuccess)
+		e = cudaMemcpy(b->d_sprefix.ptr, prefix.data(), prefix.size() * sizeof(int),
+			cudaMemcpyHostToDevice);
+	if (e != cudaSuccess) return fail(b, std::string("upload: ") + cudaGetErrorString(e), -2);
+	b->sym_grid = std::max(1, std::min(b->n_sym_items,
+		b->num_sms * p3d_sym_batch_occupancy(b->reg, b->ops)));
+	return 0;
+}
+
 // Enqueue one batch execution on the batch's stream (not via the graph).
 cudaError_t enqueue(cvtx_gb300_batch* b) {
-	cudaError_t e = cudaMemsetAsync(b->d_next.ptr, 0, sizeof(unsigned), b->stream);
-	if (e != cudaSuccess || b->n_items == 0) return e;
-	with_batch_variant(b->reg, b->ops, b->shape, [&](auto var) {
-		using V = decltype(var);
-		V::fn()<<<b->grid, kShapes[b->shape].nt, b->smem, b->stream>>>(
-			static_cast<const BatchProblem*>(b->d_probs.ptr), int(b->in.size()),
-			static_cast<const int4*>(b->d_items.ptr), b->n_items, static_cast<unsigned*>(b->d_next.ptr), static_cast<unsigned*>(b->d_err.ptr));
-		return 0;
-	});
-	count_launch();
-	return cudaGetLastError();
+	cudaError_t e = cudaSuccess;
+	if (b->n_items > 0) {
+		e = cudaMemsetAsync(b->d_next.ptr, 0, sizeof(unsigned), b->stream);
+		if (e != cudaSuccess) return e;
+		with_batch_variant(b->reg, b->ops, b->shape, [&](auto var) {
+			using V = decltype(var);
+			V::fn()<<<b->grid, kShapes[b->shape].nt, b->smem, b->stream>>>(
+				static_cast<const BatchProblem*>(b->d_probs.ptr), int(b->in.size()),
+				static_cast<const int4*>(b->d_items.ptr), b->n_items, static_cast<unsigned*>(b->d_next.ptr), static_cast<unsigned*>(b->d_err.ptr));
+			return 0;
+		});
+		count_launch();
+		e = cudaGetLastError();
+		if (e != cudaSuccess) return e;
+	}
+	if (b->n_sym_items > 0) {
+		// the slots and the item counter start at zero
+		e = cudaMemsetAsync(b->d_slots.ptr, 0, b->sym_slot_bytes, b->stream);
+		if (e == cudaSuccess) e = cudaMemsetAsync(b->d_snext.ptr, 0, sizeof(unsigned), b->stream);
+		if (e == cudaSuccess)
+			e = p3d_sym_batch_enqueue(b->reg, b->ops,
+				static_cast<const SymBatchProblem*>(b->d_sprobs.ptr), b->n_sym_probs,
+				static_cast<const int4*>(b->d_sitems.ptr), b->n_sym_items,
+				static_cast<const int*>(b->d_sprefix.ptr), b->sym_total,
+				static_cast<unsigned*>(b->d_snext.ptr), static_cast<unsigned*>(b->d_err.ptr),
+				b->sym_grid, b->stream);
+	}
+	return e;
 }
 
 // A CTA whose wait expired returns before it counts its arrival at its
@@ -336,7 +454,7 @@ CVTX_EXPORT cvtx_gb300_batch* cvtx_gb300_batch_create(const cvtx_gb300_p3d_probl
 	if (e == cudaSuccess) e = b->d_next.ensure(sizeof(unsigned));
 	if (e == cudaSuccess) e = b->d_err.ensure(sizeof(unsigned));
 	if (e == cudaSuccess) e = cudaMemset(b->d_err.ptr, 0, sizeof(unsigned));
-	if (e != cudaSuccess || plan_batch(b, 0, 8192) != 0) {
+	if (e != cudaSuccess || plan_sym(b) != 0 || plan_batch(b, 0, 8192) != 0) {
 		set_error(std::string("cvtx_gb300_batch_create: ") + cudaGetErrorString(e));
 		cvtx_gb300_batch_destroy(b);
 		return nullptr;
@@ -434,7 +552,7 @@ CVTX_EXPORT int cvtx_gb300_batch_info(const cvtx_gb300_batch* b, int* shape_tpt,
 	if (shape_tpt) *shape_tpt = kShapes[b->shape].tpt;
 	if (shape_nt) *shape_nt = kShapes[b->shape].nt;
 	if (chunk) *chunk = b->chunk;
-	if (n_items) *n_items = b->n_items;
+	if (n_items) *n_items = b->n_items + b->n_sym_items;
 	if (graph) *graph = b->exec ? 1 : 0;
 	if (interactions) *interactions = b->pairs;
 	return 0;
@@ -447,6 +565,8 @@ CVTX_EXPORT void cvtx_gb300_batch_destroy(cvtx_gb300_batch* b) {
 	drop_graph(b);
 	b->d_probs.release(); b->d_items.release(); b->d_partial.release();
 	b->d_counters.release(); b->d_next.release(); b->d_err.release();
+	b->d_sprobs.release(); b->d_sitems.release(); b->d_sprefix.release();
+	b->d_slots.release(); b->d_snext.release();
 	if (b->ev_in) cudaEventDestroy(b->ev_in);
 	if (b->ev_out) cudaEventDestroy(b->ev_out);
 	if (b->stream) cudaStreamDestroy(b->stream);

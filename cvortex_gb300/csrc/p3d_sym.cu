@@ -25,6 +25,7 @@
 
 #include "nbody.h"
 #include "p3d_induce.cuh"
+#include "p3d_sym_batch.h"
 #include "sym.cuh"
 
 namespace cvtx {
@@ -348,6 +349,87 @@ struct VortSym {
 	}
 };
 
+// ---- many problems (the batched form) -----------------------------------------
+// Persistent CTAs claim (problem, bi, bj) items; each item runs exactly as in
+// the single-problem kernel, on its problem's blocks and slots.
+template <class Op>
+__global__ void __launch_bounds__(kSymNT, Op::kMinBlocks)
+sym_batch_kernel(const SymBatchProblem* __restrict__ probs, int n_probs,
+	const int4* __restrict__ items, int n_items, unsigned* next, unsigned* err)
+{
+	extern __shared__ __align__(16) unsigned char smem[];
+	__shared__ SymBatchProblem sp;
+	__shared__ int item_s;
+	if (blockDim.x != kSymNT) {
+		if (threadIdx.x == 0) atomicOr(err, kErrBadLaunch);
+		return;
+	}
+	if (!SymStream<Op>::init(smem, err)) return;
+	unsigned tcount = 0;
+	for (;;) {
+		if (threadIdx.x == 0) item_s = int(atomicAdd(next, 1u));
+		__syncthreads();
+		const int it = item_s;
+		__syncthreads();
+		if (it >= n_items) return;
+		const int4 w = items[it];
+		if (w.x < 0 || w.x >= n_probs) {
+			if (threadIdx.x == 0) atomicOr(err, kErrBadWork);
+			continue;
+		}
+		// every thread finished its reads of the previous problem before
+		// the two barriers above
+		if (threadIdx.x == 0) sp = probs[w.x];
+		__syncthreads();
+		const int bi = w.y, bj = w.z;
+		if (bi < 0 || bj < bi || bj >= sp.nb || bi * sp.S >= sp.p.n_tgt) {
+			if (threadIdx.x == 0) atomicOr(err, kErrBadWork);
+			continue;
+		}
+		SymArgs a;
+		a.S = sp.S;
+		a.nb = sp.nb;
+		a.slots = sp.slots;
+		const bool ok = bi == bj ? sym_diagonal<Op>(sp.p, sp.kc, a, bi, smem, err, tcount)
+		                         : sym_item<Op, true>(sp.p, sp.kc, a, bi, bj, smem, err, tcount);
+		if (!ok) return;
+	}
+}
+
+// Every particle of every problem: its nb slot partials in block order
+// (FP64), then the output transforms.
+template <class Op>
+__global__ void sym_batch_finalize(const SymBatchProblem* __restrict__ probs,
+	const int* __restrict__ prefix, int n_probs, int total)
+{
+	constexpr int NC = Op::NC;
+	const int g = blockIdx.x * blockDim.x + threadIdx.x;
+	if (g >= total) return;
+	int lo = 0, hi = n_probs - 1;      // the problem with prefix[i] <= g
+	while (lo < hi) {
+		const int mid = (lo + hi + 1) >> 1;
+		if (prefix[mid] <= g) lo = mid;
+		else hi = mid - 1;
+	}
+	const SymBatchProblem& q = probs[lo];
+	const int n = q.p.n_tgt;
+	const int t = g - prefix[lo];
+	if (t < 0 || t >= n) return;
+	double s[NC];
+#pragma unroll
+	for (int c = 0; c < NC; ++c) s[c] = 0.0;
+	for (int b = 0; b < q.nb; ++b)
+#pragma unroll
+		for (int c = 0; c < NC; ++c) s[c] += double(q.slots[(size_t(b) * NC + c) * n + t]);
+	Op::write(q.p, q.kc, t, s);
+}
+
+template <class Op>
+int sym_batch_occupancy() {
+	static const int occ = resident_ctas(sym_batch_kernel<Op>, kSymNT, sym_smem_bytes<Op>());
+	return occ;
+}
+
 template <class F>
 auto with_reg_vort(int reg, F&& f) {
 	switch (reg) {
@@ -425,6 +507,29 @@ cudaError_t p3d_visc_self(int reg, const P3DViscProblem& p, const LaunchEnv& env
 		return sym_launch<ViscSym<Reg::Gaussian>>(p, vc, env);
 	}
 	return cudaErrorInvalidValue;
+}
+
+int p3d_sym_batch_occupancy(int reg, unsigned ops) {
+	return with_reg_ops_sym(reg, ops, [&](auto* op) {
+		using Op = std::remove_pointer_t<decltype(op)>;
+		return sym_batch_occupancy<Op>();
+	});
+}
+
+cudaError_t p3d_sym_batch_enqueue(int reg, unsigned ops, const SymBatchProblem* probs,
+	int n_probs, const int4* items, int n_items, const int* prefix, int total, unsigned* next,
+	unsigned* err, int grid, cudaStream_t s)
+{
+	if (n_probs <= 0 || n_items <= 0) return cudaSuccess;
+	return with_reg_ops_sym(reg, ops, [&](auto* op) {
+		using Op = std::remove_pointer_t<decltype(op)>;
+		sym_batch_kernel<Op><<<std::max(grid, 1), kSymNT, sym_smem_bytes<Op>(), s>>>(
+			probs, n_probs, items, n_items, next, err);
+		count_launch();
+		sym_batch_finalize<Op><<<(total + 255) / 256, 256, 0, s>>>(probs, prefix, n_probs, total);
+		count_launch();
+		return cudaGetLastError();
+	});
 }
 
 bool p3d_vort_self_form_applies(int reg, const P3DVortProblem& p) {

@@ -1,6 +1,7 @@
-"""Batched form (many independent P3D problems in one persistent launch):
-each problem's result matches the per-call device API, the captured CUDA
-graph replays deterministically, and tuning keeps results within tolerance."""
+"""Batched form (many independent P3D problems in one persistent launch,
+problems from 4,096 particles in the self-interaction form): each
+problem's result matches the per-call device API, the captured CUDA graph
+replays deterministically, and tuning keeps results within tolerance."""
 import ctypes as C
 
 import numpy as np
@@ -9,7 +10,7 @@ import pytest
 import oracle
 from cvortex_gb300 import abi, workloads
 from oracle import exact
-from parity import TOL
+from parity import TOL, same_up_to_rounding
 
 pytestmark = pytest.mark.gpu
 
@@ -62,10 +63,12 @@ def test_batch_matches_per_call(gpu, reg, ops):
                                             abi.REG_IDS[reg], 0.05, stream)
             assert rc == 0
             torch.cuda.synchronize()
+            # problems from 4,096 particles run in the self-interaction
+            # form in the batch: the two differ in summation order only
             if ops & 1:
-                assert exact.rel_l2(vel.cpu().numpy(), ev.cpu().numpy()) <= 1e-6
+                same_up_to_rounding(p, reg, "vel", vel.cpu().numpy(), ev.cpu().numpy(), n, 0.05)
             if ops & 2:
-                assert exact.rel_l2(dv.cpu().numpy(), ed.cpu().numpy()) <= 1e-6
+                same_up_to_rounding(p, reg, "dvort", dv.cpu().numpy(), ed.cpu().numpy(), n, 0.05)
         # one problem against the oracle directly
         p, rec, vel, dv = keep[6]
         if ops & 1:
