@@ -295,9 +295,14 @@ int batch_sym_min() {
 	return v;
 }
 
+// Slot memory the self-interaction part may hold; problems beyond it (in
+// input order) stay with the ordered-pair items.
+constexpr size_t kBatchSymSlotCap = size_t(8) << 30;
+
 // Select the problems of the self-interaction part, cut each into at most 16
 // blocks (a multiple of 512 particles), list their block-pair items largest
-// first and upload the tables. Independent of the ordered part's plan.
+// first and upload the tables. Independent of the ordered part's plan. If
+// the tables cannot be allocated, every problem stays with the ordered part.
 int plan_sym(cvtx_gb300_batch* b) {
 	const int nc = (b->ops & kOpVel ? 3 : 0) + (b->ops & kOpDvort ? 6 : 0);
 	const int min_n = batch_sym_min();
@@ -315,10 +320,12 @@ int plan_sym(cvtx_gb300_batch* b) {
 		if (min_n <= 0 || n < min_n || n < 1024 || q.tgt != q.src || q.tgt_stride != 2 ||
 			q.n_src != n)
 			continue;
-		b->in_sym[i] = 1;
 		const int nb_t = std::min(16, (n + 511) / 512);
 		const int S = 512 * ((n + 512 * nb_t - 1) / (512 * nb_t));
 		const int nb = (n + S - 1) / S;
+		const size_t floats = (size_t(nb) * nc * size_t(n) + 63) & ~size_t(63);
+		if ((slot_floats + floats) * sizeof(float) > kBatchSymSlotCap) continue;
+		b->in_sym[i] = 1;
 		SymBatchProblem r;
 		std::memset(&r, 0, sizeof r);
 		r.p.src = static_cast<const float4*>(q.src); r.p.n_src = n;
@@ -332,7 +339,7 @@ int plan_sym(cvtx_gb300_batch* b) {
 		const int k = int(probs.size());
 		probs.push_back(r);
 		slot_off.push_back(slot_floats);
-		slot_floats += (size_t(nb) * nc * size_t(n) + 63) & ~size_t(63);
+		slot_floats += floats;
 		prefix.push_back(int(total));
 		total += n;
 		for (int bj = 0; bj < nb; ++bj)
@@ -355,6 +362,14 @@ int plan_sym(cvtx_gb300_batch* b) {
 	if (e == cudaSuccess) e = b->d_sitems.ensure(items.size() * sizeof(int4));
 	if (e == cudaSuccess) e = b->d_sprefix.ensure(prefix.size() * sizeof(int));
 	if (e == cudaSuccess) e = b->d_snext.ensure(sizeof(unsigned));
+	if (e == cudaErrorMemoryAllocation) {
+		// no room for the tables: the ordered part serves every problem
+		(void)cudaGetLastError();
+		b->in_sym.assign(b->in.size(), 0);
+		b->n_sym_probs = b->n_sym_items = 0;
+		b->d_slots.release();
+		return 0;
+	}
 	if (e != cudaSuccess) return fail(b, std::string("allocation: ") + cudaGetErrorString(e), -2);
 	for (size_t k = 0; k < probs.size(); ++k)
 		probs[k].slots = static_cast<float*>(b->d_slots.ptr) + slot_off[k];

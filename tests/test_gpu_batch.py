@@ -113,3 +113,57 @@ def test_batch_graph_replay_and_tuning(gpu):
             assert exact.rel_l2(d.cpu().numpy(), d0) <= 1e-6
     finally:
         lib.cvtx_gb300_batch_destroy(b)
+
+
+BATCH_CHILD = r"""
+import sys
+import numpy as np, torch
+sys.path.insert(0, sys.argv[2])
+sys.path.insert(0, sys.argv[3])
+from cvortex_gb300 import abi
+from test_gpu_batch import _make
+cv = abi.Cvtx(); cv.initialise()
+lib = cv.lib
+sizes = [5000, 12000, 30000, 700]
+arr, keep = _make(torch, sizes, 3, seed0=500)
+b = lib.cvtx_gb300_batch_create(arr, len(sizes), 1, 3)
+assert b, cv.last_error()
+sh = torch.cuda.current_stream().cuda_stream
+import ctypes as C
+assert lib.cvtx_gb300_batch_run(b, C.c_void_p(sh)) == 0
+torch.cuda.synchronize()
+assert lib.cvtx_gb300_batch_status(b) == 0, cv.last_error()
+lib.cvtx_gb300_batch_destroy(b)
+np.savez(sys.argv[1], *[np.concatenate([v.cpu().numpy(), d.cpu().numpy()], 1) for _, _, v, d in keep])
+"""
+
+
+def _batch_child(tmp_path, tag, env):
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+    out = tmp_path / f"batch_{tag}.npz"
+    root = Path(__file__).resolve().parents[1]
+    res = subprocess.run([sys.executable, "-c", BATCH_CHILD, str(out), str(root),
+                          str(root / "tests")], cwd=root, env=dict(os.environ, **env),
+                         capture_output=True, text=True, timeout=600)
+    assert res.returncode == 0, res.stderr[-2000:]
+    z = np.load(out)
+    return [z[f"arr_{i}"] for i in range(len(z.files))]
+
+
+def test_batch_self_part_fallbacks(gpu, tmp_path):
+    """The batch's self-interaction part switched off (CVTX_GB300_SYM_MIN=0)
+    and its tables not allocatable (CVTX_GB300_WS_LIMIT below them: an
+    injected out-of-memory) both leave every problem to the ordered-pair
+    items, bit for bit the same; with the part, the results agree within the
+    FP32 bound."""
+    with_part = _batch_child(tmp_path, "sym", {})
+    ordered = _batch_child(tmp_path, "ordered", {"CVTX_GB300_SYM_MIN": "0"})
+    limited = _batch_child(tmp_path, "limited", {"CVTX_GB300_WS_LIMIT": str(16 << 20)})
+    for a, c in zip(ordered, limited):
+        np.testing.assert_array_equal(a, c)
+    assert any(not np.array_equal(a, c) for a, c in zip(with_part, ordered))
+    for a, c in zip(with_part, ordered):
+        assert exact.rel_l2(a, c) <= 1e-6
