@@ -361,7 +361,6 @@ cudaError_t sym_launch(const typename Op::Problem& p, const typename Op::Consts&
 	return cudaGetLastError();
 }
 
-
 // Smallest particle count that takes the self-interaction form
 // (CVTX_GB300_SYM_MIN; 0 switches the form off).
 int sym_min_particles() {
@@ -371,7 +370,6 @@ int sym_min_particles() {
 	}();
 	return min_n;
 }
-
 
 bool sym_size_ok(int n) {
 	const int min_n = sym_min_particles();
