@@ -439,10 +439,35 @@ def run_ours(args):
         out["serving"] = serve_extra(cv, lib, count=args.serve_requests)
     if rank == 0 and world == 1 and op == "veldvort":
         out["cpu_baseline"] = cpu_baseline(p, args.reg)
+    if rank == 0 and "extras" in out:
+        out["summary"] = summary(out)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def summary(out):
+    """The figures a reader of the line's last characters looks for, in
+    short form (G interactions/s unless named otherwise)."""
+    x, sv = out["extras"], out["serving"]
+    b = x["batch512"]
+    heavy = sv["stream"]["rates"]
+    light = sv["light"]["rates"]
+    return {
+        "value": r4(out["value"]), "fp32_frac": r4(out["roofline"]["frac"]),
+        "e2e": r4(out["e2e"]["value"]),
+        "batch512": [b["batched_ginter_s"], b["speedup"], b["speedup_vs_separate"]],
+        "ring100k_w_vel_dvort_visc_vort": [x["ring100k_winckelmans"][k]["ginter_s"]
+                                           for k in ("vel", "dvort", "visc", "vort")],
+        "p2d200k_vel_visc_w": [x["p2d_patch200k_winckelmans_vel"]["ginter_s"],
+                               x["p2d_patch200k_winckelmans_visc"]["ginter_s"]],
+        "f3d100k_vel_dvort": [x["f3d_sheet100k_vel"]["ginter_s"],
+                              x["f3d_sheet100k_dvort_cube100k"]["ginter_s"]],
+        "serving_light_p50_ms_served_plain": {r: [v["served"][0], v["plain"][0]]
+                                              for r, v in light.items()},
+        "serving_heavy_x": [v["x"] for v in heavy.values()],
+        "cpu_baseline": out.get("cpu_baseline", {}).get("value")}
 
 
 def headline_parity(p, vel, dv, args):
