@@ -33,7 +33,7 @@ namespace {
 constexpr int kParallelGather = 32768;
 // Velocity calls with at least this many points compare the points with the
 // sources' coordinates, to use the source records as the targets.
-constexpr int kSelfCheckMin = 32768;
+constexpr int kSelfCheckMin = 16384;
 
 void gather_p3d_host(const cvtx_P3D* const* src, int n, float4* out) {
 #pragma omp parallel for schedule(static) if (n >= kParallelGather)

@@ -129,7 +129,7 @@ cudaError_t p3d_induce(int reg, unsigned ops, const P3DInduceProblem& p, const L
 
 // Self-interaction form (p3d_sym.cu): the particles are their own targets
 // (tgt == src, stride 2, n_tgt == n_src, at least CVTX_GB300_SYM_MIN
-// particles, default 32,768), so each unordered pair is evaluated once.
+// particles, default 16,384), so each unordered pair is evaluated once.
 // p3d_induce takes it when it applies, the launch is not bound by a CTA
 // lifetime cap (env.cta_src_cap), no launch configuration is forced, and the
 // workspace suffices; results stay deterministic. p3d_self_ws_bytes is

@@ -362,11 +362,15 @@ cudaError_t sym_launch(const typename Op::Problem& p, const typename Op::Consts&
 }
 
 // Smallest particle count that takes the self-interaction form
-// (CVTX_GB300_SYM_MIN; 0 switches the form off).
+// (CVTX_GB300_SYM_MIN; 0 switches the form off). Below about 22,000 P3D
+// particles the rule of two items per resident CTA keeps the ordered-pair
+// kernels anyway; from there the form was timed faster on a GB300 (24,000 -
+// 32,000 particles: stretching 1.54-1.64x, velocity 1.07-1.11x, fused up to
+// 1.11x; P2D at 32,000: 1.49-1.65x).
 int sym_min_particles() {
 	static const int min_n = [] {
 		const char* e = std::getenv("CVTX_GB300_SYM_MIN");
-		return (e && *e) ? std::atoi(e) : 32768;
+		return (e && *e) ? std::atoi(e) : 16384;
 	}();
 	return min_n;
 }

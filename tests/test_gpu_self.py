@@ -41,7 +41,7 @@ def _dev(gpu, torch, rec, n, reg, ops):
 
 
 @pytest.mark.parametrize("reg", REGS)
-@pytest.mark.parametrize("n", [33_001, 70_000])
+@pytest.mark.parametrize("n", [25_000, 33_001, 70_000])
 def test_self_form_vs_oracle_and_ordered_pairs(gpu, reg, n):
     import torch
     p = workloads.vortex_ring(n, seed=71) if n == 70_000 else workloads.uniform_cube(n, seed=72)
