@@ -7,7 +7,7 @@
  * reference's ABI functions are unchanged and declared in libcvtx.h. These
  * entry points add what a GPU-resident caller needs:
  *   - an error query (the reference functions return void and fall back to
- *     the CPU silently on OpenCL errors, src/P3D.cpp:352-364; this build
+ *     the CPU silently on OpenCL errors, src/P3D.cpp:352-364; this library
  *     never falls back, it reports instead and writes NaN results);
  *   - a fused vel + dvort call over one particle set;
  *   - a device-pointer API that works on packed records already in GPU

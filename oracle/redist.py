@@ -12,7 +12,7 @@ tests/golden/redist.npz: same counts, coordinates and order bit for bit;
 strengths to 2^-21 of the largest, because grid-point sums are taken here in
 FP64 in particle order and the reference sums in FP32 per OpenMP thread.
 
-Used only by tests/ as the checker.
+Test infrastructure: only tests/ use it, to check the library's results.
 """
 from __future__ import annotations
 
