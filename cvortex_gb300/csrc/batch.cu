@@ -304,9 +304,7 @@ constexpr size_t kBatchSymSlotCap = size_t(8) << 30;
 // first and upload the tables. Independent of the ordered part's plan. If
 // the tables cannot be allocated, every problem stays with the ordered part.
 int plan_sym(cvtx_gb300_batch* b) {
-	// sums per particle of the self-interaction form: velocity and the
-	// stretching as one vector
-	const int nc = (b->ops & kOpVel ? 3 : 0) + (b->ops & kOpDvort ? 3 : 0);
+	const int nc = (b->ops & kOpVel ? 3 : 0) + (b->ops & kOpDvort ? 6 : 0);
 	const int min_n = batch_sym_min();
 	b->in_sym.assign(b->in.size(), 0);
 	std::vector<SymBatchProblem> probs;
@@ -335,7 +333,7 @@ int plan_sym(cvtx_gb300_batch* b) {
 		r.p.out_vel = (b->ops & kOpVel) ? q.vel_out : nullptr;
 		r.p.out_dvort = (b->ops & kOpDvort) ? q.dvort_out : nullptr;
 		r.p.sigma = q.sigma;
-		r.kc = make_sym_induce_consts(b->reg, q.sigma);
+		r.kc = make_induce_consts(b->reg, q.sigma);
 		r.S = S;
 		r.nb = nb;
 		const int k = int(probs.size());

@@ -45,7 +45,6 @@ struct VelSym2D {
 	static constexpr int kUnroll = R == Reg::Gaussian ? 8 : 16;
 	static constexpr int kRec = 1, kTile = kP2DSymTile, kMinBlocks = R == Reg::Gaussian ? 6 : 4;
 	static constexpr bool kOwnDiagonal = false;
-	static constexpr size_t kMinSmem = 0;
 	struct Tgt { float2 tx[kSymH], ty[kSymH], tg[kSymH]; };
 
 	__device__ __forceinline__ static void load(const Problem& p, int tb, int tid, int lim,
@@ -110,7 +109,6 @@ struct ViscSym2D {
 	static constexpr int kUnroll = 16;
 	static constexpr int kRec = 1, kTile = kP2DSymTile, kMinBlocks = 4;
 	static constexpr bool kOwnDiagonal = false;
-	static constexpr size_t kMinSmem = 0;
 	struct Tgt { float2 ntx[kSymH], nty[kSymH], ntg[kSymH], ta[kSymH]; };
 
 	__device__ __forceinline__ static void load(const Problem& p, int tb, int tid, int lim,

@@ -41,21 +41,16 @@ constexpr int kP3DSymMinBlocks = 3;
 
 // ---- pair operations (the interface is described in sym.cuh) --------------
 
-// Induced velocity and/or stretching (reference src/P3D.cpp:51-114). The
-// stretching is summed as one vector per particle, C = sum G co -
-// k_scale K (d.co) d, the reference's per-pair form; the per-call kernels
-// sum its two parts apart (A, B) and combine them at the end.
+// Induced velocity and/or stretching (reference src/P3D.cpp:51-114).
 template <Reg R, bool VEL, bool DV>
 struct InduceSym {
 	using Problem = P3DInduceProblem;
-	using Consts = SymInduceConsts;
-	static constexpr int NC = (VEL ? 3 : 0) + (DV ? 3 : 0);
+	using Consts = InduceConsts;
+	static constexpr int NC = InduceNC<VEL, DV>::value;
 	// fused, 1M cube: 4 -> 967, 8 -> 947, 2 -> 937 G/s; one output alone: 8
 	static constexpr int kUnroll = (VEL && DV) ? 4 : 8;
 	static constexpr int kRec = 2, kTile = kP3DTile, kMinBlocks = kP3DSymMinBlocks;
 	static constexpr bool kOwnDiagonal = true;
-	// the diagonal body keeps the per-call kernel's separate sums (A, B)
-	static constexpr size_t kMinSmem = induce_smem_bytes<kSymTPT, kSymNT, InduceNC<VEL, DV>::value>();
 	struct Tgt {
 		float2 tx[kSymH], ty[kSymH], tz[kSymH], ax[kSymH], ay[kSymH], az[kSymH];
 		float2 nax[kSymH], nay[kSymH], naz[kSymH];
@@ -142,18 +137,20 @@ struct InduceSym {
 				float2 ox, oy, oz;
 				cross_ref2(g.ax[h], g.ay[h], g.az[h], wx, wy, wz, nwx, nwy, nwz, ox, oy, oz);
 				const float2 pd = __ffma2_rn(dz, oz, __ffma2_rn(dy, oy, __fmul2_rn(dx, ox)));
-				// -k_scale K (d.co): t gets G co + nk d, s the negation
-				const float2 nk = __fmul2_rn(__fmul2_rn(K, bc2(kc.nk_scale)), pd);
-				acc[o + 0][h] = __ffma2_rn(G, ox, __ffma2_rn(nk, dx, acc[o + 0][h]));
-				acc[o + 1][h] = __ffma2_rn(G, oy, __ffma2_rn(nk, dy, acc[o + 1][h]));
-				acc[o + 2][h] = __ffma2_rn(G, oz, __ffma2_rn(nk, dz, acc[o + 2][h]));
+				const float2 kk = __fmul2_rn(K, pd);
+				acc[o + 0][h] = __ffma2_rn(G, ox, acc[o + 0][h]);
+				acc[o + 1][h] = __ffma2_rn(G, oy, acc[o + 1][h]);
+				acc[o + 2][h] = __ffma2_rn(G, oz, acc[o + 2][h]);
+				acc[o + 3][h] = __ffma2_rn(kk, dx, acc[o + 3][h]);
+				acc[o + 4][h] = __ffma2_rn(kk, dy, acc[o + 4][h]);
+				acc[o + 5][h] = __ffma2_rn(kk, dz, acc[o + 5][h]);
 				if (SYM) {
-					js[o + 0] = fmaf(-G.x, ox.x, fmaf(-G.y, ox.y,
-						fmaf(-nk.x, dx.x, fmaf(-nk.y, dx.y, js[o + 0]))));
-					js[o + 1] = fmaf(-G.x, oy.x, fmaf(-G.y, oy.y,
-						fmaf(-nk.x, dy.x, fmaf(-nk.y, dy.y, js[o + 1]))));
-					js[o + 2] = fmaf(-G.x, oz.x, fmaf(-G.y, oz.y,
-						fmaf(-nk.x, dz.x, fmaf(-nk.y, dz.y, js[o + 2]))));
+					js[o + 0] = fmaf(-G.x, ox.x, fmaf(-G.y, ox.y, js[o + 0]));
+					js[o + 1] = fmaf(-G.x, oy.x, fmaf(-G.y, oy.y, js[o + 1]));
+					js[o + 2] = fmaf(-G.x, oz.x, fmaf(-G.y, oz.y, js[o + 2]));
+					js[o + 3] = fmaf(-kk.x, dx.x, fmaf(-kk.y, dx.y, js[o + 3]));
+					js[o + 4] = fmaf(-kk.x, dy.x, fmaf(-kk.y, dy.y, js[o + 4]));
+					js[o + 5] = fmaf(-kk.x, dz.x, fmaf(-kk.y, dz.y, js[o + 5]));
 				}
 			}
 		}
@@ -162,24 +159,10 @@ struct InduceSym {
 	__device__ __forceinline__ static void write(const Problem& p, const Consts& kc, int t,
 		const double* s)
 	{
-		int o = 0;
-		if (VEL) {
-			float* v = p.out_vel + 3 * size_t(t);
-			v[0] = float(kc.s_vel * s[0]);
-			v[1] = float(kc.s_vel * s[1]);
-			v[2] = float(kc.s_vel * s[2]);
-			o = 3;
-		}
-		if (DV) {
-			float* w = p.out_dvort + 3 * size_t(t);
-			w[0] = float(kc.s_dv * s[o + 0]);
-			w[1] = float(kc.s_dv * s[o + 1]);
-			w[2] = float(kc.s_dv * s[o + 2]);
-		}
+		write_induce<VEL, DV>(p, kc, t, s);
 	}
 
-	// A diagonal item: the per-call CTA body over the block's ordered pairs;
-	// its stretching parts A and B are combined into C (in FP64) for the slots.
+	// A diagonal item: the per-call CTA body over the block's ordered pairs.
 	__device__ __forceinline__ static bool diagonal(const Problem& p, const Consts& kc,
 		const SymArgs& a, int b, unsigned char* smem, unsigned* err, unsigned& tcount)
 	{
@@ -191,15 +174,8 @@ struct InduceSym {
 		for (int tb = b0; tb < b1; tb += kSymPass) {
 			const bool ok = induce2_block<R, VEL, DV, kSymTPT, kSymNT, 2>(q, kc, tb, b0, b1 - b0,
 				smem, err, tcount, [&](int t, const double* s) {
-					constexpr int o = VEL ? 3 : 0;
 #pragma unroll
-					for (int c = 0; c < o; ++c) a.slots[(size_t(b) * NC + c) * n + t] = float(s[c]);
-					if (DV) {
-#pragma unroll
-						for (int c = 0; c < 3; ++c)
-							a.slots[(size_t(b) * NC + o + c) * n + t] =
-								float(s[o + c] - kc.k_scale * s[o + 3 + c]);
-					}
+					for (int c = 0; c < NC; ++c) a.slots[(size_t(b) * NC + c) * n + t] = float(s[c]);
 				});
 			if (!ok) return false;
 		}
@@ -225,7 +201,6 @@ struct ViscSym {
 	static constexpr int kRec = 2, kTile = kP3DTile;
 	static constexpr int kMinBlocks = R == Reg::Gaussian ? 4 : kP3DSymMinBlocks;
 	static constexpr bool kOwnDiagonal = false;
-	static constexpr size_t kMinSmem = 0;
 	struct Tgt {
 		float2 ntx[kSymH], nty[kSymH], ntz[kSymH], tv[kSymH], nax[kSymH], nay[kSymH], naz[kSymH];
 	};
@@ -310,7 +285,6 @@ struct VortSym {
 	static constexpr double kFactor = ZetaShape2<R>::kFactor;   // in the output scale
 	static constexpr int kRec = 2, kTile = kP3DTile, kMinBlocks = 4;
 	static constexpr bool kOwnDiagonal = false;
-	static constexpr size_t kMinSmem = 0;
 	struct Tgt {
 		float2 ntx[kSymH], nty[kSymH], ntz[kSymH], ax[kSymH], ay[kSymH], az[kSymH];
 	};
@@ -506,7 +480,7 @@ size_t p3d_self_ws_bytes(int reg, unsigned ops, int n, int num_sms, size_t ws_ca
 cudaError_t p3d_self(int reg, unsigned ops, const P3DInduceProblem& p, const LaunchEnv& env) {
 	return with_reg_ops_sym(reg, ops, [&](auto* op) {
 		using Op = std::remove_pointer_t<decltype(op)>;
-		return sym_launch<Op>(p, make_sym_induce_consts(reg, p.sigma), env);
+		return sym_launch<Op>(p, make_induce_consts(reg, p.sigma), env);
 	});
 }
 

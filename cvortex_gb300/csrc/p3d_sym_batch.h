@@ -10,24 +10,11 @@
 
 namespace cvtx {
 
-// Constants of the self-interaction form's induce operation: the per-call
-// ones and -k_scale in FP32 (its stretching sum carries that factor).
-struct SymInduceConsts : InduceConsts {
-	float nk_scale;
-};
-
-inline SymInduceConsts make_sym_induce_consts(int reg, float sigma) {
-	SymInduceConsts c;
-	static_cast<InduceConsts&>(c) = make_induce_consts(reg, sigma);
-	c.nk_scale = float(-c.k_scale);
-	return c;
-}
-
 // One problem as the kernels read it: blocks of S particles (a multiple of
 // 512), nb blocks, slots [nb][NC][n] FP32 (zeroed before every run).
 struct alignas(16) SymBatchProblem {
 	P3DInduceProblem p;
-	SymInduceConsts kc;
+	InduceConsts kc;
 	float* slots;
 	int S, nb;
 };

@@ -58,8 +58,7 @@ constexpr int kSymWarps = kSymNT / 32;
 // record's running sums `js` (FULL = false zeroes the pair for a lane whose
 // record lies past the end of the block, `valid` false); write, the output
 // of a particle from its FP64 sums; kOwnDiagonal and, if set, diagonal(),
-// the CTA body for a diagonal item, with kMinSmem the dynamic shared memory
-// that body needs (the kernels allocate at least that much).
+// the CTA body for a diagonal item.
 
 // ---- the rotation ------------------------------------------------------------
 template <class Op> using SymStream = TileStream<Op::kRec, Op::kTile, 2>;
@@ -67,11 +66,9 @@ template <class Op> using SymStream = TileStream<Op::kRec, Op::kTile, 2>;
 template <class Op>
 constexpr size_t sym_smem_bytes() {
 	// tile stages, (hi, lo) per pass particle and sum, and two buffers of
-	// per-warp record sums [2][warps][NC][32]; at least what the operation's
-	// own diagonal body needs
-	constexpr size_t rot = SymStream<Op>::kSmemBytes + size_t(2) * Op::NC * kSymPass * sizeof(float) +
+	// per-warp record sums [2][warps][NC][32]
+	return SymStream<Op>::kSmemBytes + size_t(2) * Op::NC * kSymPass * sizeof(float) +
 		size_t(2) * kSymWarps * Op::NC * 32 * sizeof(float);
-	return rot > Op::kMinSmem ? rot : Op::kMinSmem;
 }
 
 // Fire-and-forget add to global memory (no value returned, so the thread

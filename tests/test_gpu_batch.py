@@ -161,10 +161,7 @@ def test_batch_self_part_fallbacks(gpu, tmp_path):
     FP32 bound."""
     with_part = _batch_child(tmp_path, "sym", {})
     ordered = _batch_child(tmp_path, "ordered", {"CVTX_GB300_SYM_MIN": "0"})
-    # the ordered part's FP64 partials take 10.4 MB (12,000 and 30,000
-    # particles in 2 and 4 chunks of 9 sums), the self part's slots 15.5 MB
-    # (10, 12 and 15 blocks of 6 sums): a 13 MiB limit admits only the first
-    limited = _batch_child(tmp_path, "limited", {"CVTX_GB300_WS_LIMIT": str(13 << 20)})
+    limited = _batch_child(tmp_path, "limited", {"CVTX_GB300_WS_LIMIT": str(16 << 20)})
     for a, c in zip(ordered, limited):
         np.testing.assert_array_equal(a, c)
     assert any(not np.array_equal(a, c) for a, c in zip(with_part, ordered))
