@@ -45,6 +45,7 @@ struct VelSym2D {
 	static constexpr int kUnroll = R == Reg::Gaussian ? 8 : 16;
 	static constexpr int kRec = 1, kTile = kP2DSymTile, kMinBlocks = R == Reg::Gaussian ? 6 : 4;
 	static constexpr bool kOwnDiagonal = false;
+	static constexpr double kPlanFactor = 16.0;   // 200k patch: 0.5 % faster than 26
 	struct Tgt { float2 tx[kSymH], ty[kSymH], tg[kSymH]; };
 
 	__device__ __forceinline__ static void load(const Problem& p, int tb, int tid, int lim,
@@ -109,6 +110,7 @@ struct ViscSym2D {
 	static constexpr int kUnroll = 16;
 	static constexpr int kRec = 1, kTile = kP2DSymTile, kMinBlocks = 4;
 	static constexpr bool kOwnDiagonal = false;
+	static constexpr double kPlanFactor = 16.0;   // 200k patch: 0.5 % faster than 26
 	struct Tgt { float2 ntx[kSymH], nty[kSymH], ntg[kSymH], ta[kSymH]; };
 
 	__device__ __forceinline__ static void load(const Problem& p, int tb, int tid, int lim,

@@ -50,6 +50,7 @@ struct InduceSym {
 	// fused, 1M cube: 4 -> 967, 8 -> 947, 2 -> 937 G/s; one output alone: 8
 	static constexpr int kUnroll = (VEL && DV) ? 4 : 8;
 	static constexpr int kRec = 2, kTile = kP3DTile, kMinBlocks = kP3DSymMinBlocks;
+	static constexpr double kPlanFactor = 26.0;
 	static constexpr bool kOwnDiagonal = true;
 	struct Tgt {
 		float2 tx[kSymH], ty[kSymH], tz[kSymH], ax[kSymH], ay[kSymH], az[kSymH];
@@ -200,6 +201,7 @@ struct ViscSym {
 	static constexpr int kUnroll = R == Reg::Gaussian ? 8 : 16;
 	static constexpr int kRec = 2, kTile = kP3DTile;
 	static constexpr int kMinBlocks = R == Reg::Gaussian ? 4 : kP3DSymMinBlocks;
+	static constexpr double kPlanFactor = 26.0;   // 100k ring: 2,027 against 1,999 with 16
 	static constexpr bool kOwnDiagonal = false;
 	struct Tgt {
 		float2 ntx[kSymH], nty[kSymH], ntz[kSymH], tv[kSymH], nax[kSymH], nay[kSymH], naz[kSymH];
@@ -284,6 +286,7 @@ struct VortSym {
 	static constexpr int kUnroll = 8;
 	static constexpr double kFactor = ZetaShape2<R>::kFactor;   // in the output scale
 	static constexpr int kRec = 2, kTile = kP3DTile, kMinBlocks = 4;
+	static constexpr double kPlanFactor = 16.0;   // 100k ring: 2,680 against 2,625 with 26
 	static constexpr bool kOwnDiagonal = false;
 	struct Tgt {
 		float2 ntx[kSymH], nty[kSymH], ntz[kSymH], ax[kSymH], ay[kSymH], az[kSymH];
