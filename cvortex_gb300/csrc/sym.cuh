@@ -319,7 +319,7 @@ SymPlan sym_plan(int n, int nc, int capacity, size_t ws_cap, double factor) {
 }
 
 // Largest workspace the self-interaction form asks of its caller (the slots
-// grow as blocks x particles: 1M particles, fused: 3.1 GB; 4M: 14 GB).
+// grow as blocks x particles: 1M particles, fused: 3.9 GB; 4M: 15.7 GB).
 // CVTX_GB300_SYM_WS_CAP (bytes) lowers it, e.g. to test the fallback.
 size_t sym_ws_cap() {
 	static const size_t cap = [] {
