@@ -67,13 +67,17 @@ OPS = {"veldvort": "fused vel+dvort", "vel": "vel", "dvort": "dvort",
        "vort": "vorticity field (5 sigma box cut-off)",
        "inf": "F3D influence matrix, 25,000 points x 20,000 filaments (2 GB)",
        "m2s": "few targets: fused vel+dvort of the first 64 particles from all sources",
+       "f3d_vel": "F3D velocity, wake sheet of N filaments at N points",
        "f3d_dvort": "F3D vortex stretching, wake sheet of N filaments on N particles",
+       "batch": "batch of N fused vel+dvort problems, sizes log-uniform in [1,000, 50,000], "
+                "winckelmans, sigma=0.05 (graph-captured persistent launches)",
        "visc": "P3D viscous exchange (nu 1e-3)",
        "p2d_vel": "P2D velocity, Gaussian vortex patch of N particles",
        "p2d_visc": "P2D viscous exchange (nu 1e-3), Gaussian vortex patch of N particles"}
 P2D_FLOPS = {("vel", 0): 10, ("vel", 1): 15, ("vel", 2): 10, ("vel", 3): 13,
              ("visc", 1): 16, ("visc", 3): 10}
 M2S_TARGETS = 64
+F3D_VEL_FLOPS = 51
 F3D_DVORT_FLOPS = 62
 # influence matrix: F3D vel (51) + the dot with the direction (5) per entry
 INF_FLOPS = 56
@@ -92,7 +96,8 @@ def parse():
     ap.add_argument("--workload", default="cube", choices=["cube", "ring"],
                     help="cube: uniform cube (the plain workload's distribution); "
                          "ring: the scale-up vortex ring")
-    ap.add_argument("--n", type=int, default=1_000_000, help="particles")
+    ap.add_argument("--n", type=int, default=1_000_000,
+                    help="particles (filaments for the F3D ops, problems for --op batch)")
     ap.add_argument("--reg", default="winckelmans", choices=list(REG))
     ap.add_argument("--quick", action="store_true", help="skip the extra measurements")
     ap.add_argument("--op", default="veldvort", choices=list(OPS),
@@ -101,7 +106,10 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--serve-requests", type=int, default=64,
                     help="requests per arrival rate in the served-stream measurement")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.op == "batch" and not 1 <= args.n <= 4096:
+        ap.error("--op batch: --n is the number of problems, 1 to 4,096")
+    return args
 
 
 def dist_env():
@@ -305,11 +313,14 @@ def run_ours(args):
         raise SystemExit("--op vort: the singular vorticity field is zero (no kernel)")
     if op in ("visc", "p2d_visc") and reg not in VISC_FLOPS:
         raise SystemExit(f"--op {op}: only winckelmans and gaussian have a viscous kernel")
+    if op == "batch" and reg != REG["winckelmans"]:
+        raise SystemExit("--op batch: the batch workload is winckelmans")
     flops_per = (VORT_FLOPS[reg] if op == "vort" else INF_FLOPS if op == "inf"
-                 else F3D_DVORT_FLOPS if op == "f3d_dvort" else VISC_FLOPS[reg] if op == "visc"
+                 else F3D_DVORT_FLOPS if op == "f3d_dvort" else F3D_VEL_FLOPS if op == "f3d_vel"
+                 else VISC_FLOPS[reg] if op == "visc"
                  else P2D_FLOPS[("vel", reg)] if op == "p2d_vel"
                  else P2D_FLOPS[("visc", reg)] if op == "p2d_visc"
-                 else FLOPS[("veldvort", reg)] if op == "m2s" else FLOPS[(op, reg)])
+                 else FLOPS[("veldvort", reg)] if op in ("m2s", "batch") else FLOPS[(op, reg)])
     v_out = vel.data_ptr() if op in ("veldvort", "vel") else None
     d_out = dv.data_ptr() if op in ("veldvort", "dvort") else None
     pairs = float(n) * n
@@ -331,12 +342,34 @@ def run_ours(args):
         q = workloads.gaussian_patch_2d(n)
         rq = torch.from_numpy(np.ascontiguousarray(
             np.stack([q["coord"][:, 0], q["coord"][:, 1], q["vorticity"], q["area"]], 1))).cuda()
-    if op == "f3d_dvort":
+    if op in ("f3d_vel", "f3d_dvort"):
         fil = workloads.wake_sheet(n)
         rf = np.zeros((n, 8), np.float32)
         rf[:, 0:3], rf[:, 3], rf[:, 4:7] = fil["start"], fil["strength"], fil["end"]
         rfd = torch.from_numpy(rf).cuda()
+    if op == "f3d_vel":
+        tf = np.zeros((n, 4), np.float32)
+        tf[:, 0:3] = workloads.sheet_targets(n)
+        tfd = torch.from_numpy(tf).cuda()
+    if op == "f3d_dvort":
         rcube = torch.from_numpy(p3d_records(workloads.uniform_cube(n, seed=12)).reshape(n, 8)).cuda()
+    if op == "batch":
+        bsizes = workloads.batch_sizes(n)
+        pairs = float(sum(int(m) * int(m) for m in bsizes))
+        bkeep, bprobs = [], []
+        for i, m in enumerate(bsizes):
+            m = int(m)
+            brec = torch.from_numpy(
+                p3d_records(workloads.uniform_cube(m, seed=10_000 + i)).reshape(m, 8)).cuda()
+            bv = torch.empty((m, 3), dtype=torch.float32, device="cuda")
+            bd = torch.empty((m, 3), dtype=torch.float32, device="cuda")
+            bkeep.append((brec, bv, bd))
+            bprobs.append(abi.cvtx_gb300_p3d_problem(brec.data_ptr(), m, brec.data_ptr(), 2, m,
+                                                     bv.data_ptr(), bd.data_ptr(), SIGMA))
+        barr = (abi.cvtx_gb300_p3d_problem * n)(*bprobs)
+        bh = lib.cvtx_gb300_batch_create(barr, n, 1, 3)
+        if not bh or lib.cvtx_gb300_batch_tune(bh, 1) != 0 or lib.cvtx_gb300_batch_capture(bh) != 0:
+            raise RuntimeError(cv.last_error())
 
     def step():
         if op == "inf":
@@ -345,6 +378,11 @@ def run_ours(args):
         elif op == "m2s":
             rc = lib.cvtx_gb300_dev_P3D_M2M(rec.data_ptr(), n, rec.data_ptr(), 2, M2S_TARGETS,
                                             vel.data_ptr(), dv.data_ptr(), reg, SIGMA, sh)
+        elif op == "f3d_vel":
+            rc = lib.cvtx_gb300_dev_F3D_M2M_vel(rfd.data_ptr(), n, tfd.data_ptr(), 1, n,
+                                                vel.data_ptr(), sh)
+        elif op == "batch":
+            rc = lib.cvtx_gb300_batch_run(bh, sh)
         elif op == "f3d_dvort":
             rc = lib.cvtx_gb300_dev_F3D_M2M_dvort(rfd.data_ptr(), n, rcube.data_ptr(), 2, n,
                                                   vel.data_ptr(), sh)
@@ -396,6 +434,11 @@ def run_ours(args):
     if world > 1:
         torch.distributed.barrier()
     clk = clocks.stop()
+    if op == "batch":
+        bst = lib.cvtx_gb300_batch_status(bh)
+        lib.cvtx_gb300_batch_destroy(bh)
+        if bst != 0:
+            raise RuntimeError(f"batch status {bst}: {cv.last_error()}")
     total_ms = t_start.elapsed_time(t_end)
     kernel_ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
     from cvortex_gb300.multi import max_over_ranks
@@ -405,9 +448,10 @@ def run_ours(args):
     achieved = flops / (kernel_ms * 1e-3) / 1e12
     if op == "inf":
         wl = OPS[op]
-    elif op in ("f3d_dvort", "p2d_vel", "p2d_visc"):
-        wl = OPS[op].replace("N ", f"{n} ") + (f", {args.reg}, sigma={SIGMA}" if op != "f3d_dvort"
-                                                else "")
+    elif op in ("f3d_vel", "f3d_dvort", "batch"):
+        wl = OPS[op].replace("N ", f"{n} ")
+    elif op in ("p2d_vel", "p2d_visc"):
+        wl = OPS[op].replace("N ", f"{n} ") + f", {args.reg}, sigma={SIGMA}"
     else:
         wl = workload_name(args, op) + ("" if op in ("m2s", "veldvort") else ", targets = sources")
     out = {

@@ -81,3 +81,21 @@ def test_reference_arm_line():
                            "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     cb = line["cpu_baseline"]
     assert cb["value"] == line["value"] and cb["cores"] == 2 and cb["kind"] in ("reference", "port")
+
+
+def test_batch_op_takes_a_problem_count():
+    """`--op batch` reads --n as a problem count; the default particle count
+    would ask for a million problems and is refused before any CUDA call."""
+    b = _bench()
+    sys_argv = sys.argv
+    try:
+        sys.argv = ["bench.py", "--op", "batch", "--n", "128", "--quick"]
+        args = b.parse()
+        assert args.op == "batch" and args.n == 128
+        assert b.OPS["batch"].replace("N ", "128 ").startswith("batch of 128 fused")
+        sys.argv = ["bench.py", "--op", "batch"]
+        with pytest.raises(SystemExit):
+            b.parse()
+    finally:
+        sys.argv = sys_argv
+    assert b.F3D_VEL_FLOPS == 51 and "f3d_vel" in b.OPS
