@@ -35,8 +35,9 @@ RegConsts make_reg_consts_host(float sigma);
 
 namespace {
 
-// Resident CTAs per SM the registers are sized for (167 registers for the
-// fused pair). Sizing for two (217 registers) measured 5-7 % slower.
+// Resident CTAs per SM the registers are sized for (about 165 registers for
+// the fused pair). Sizing for two (217 registers) measured 5-7 % slower, and
+// four for one output alone (128 registers, small spills) 1-3 % slower.
 constexpr int kP3DSymMinBlocks = 3;
 
 // ---- pair operations (the interface is described in sym.cuh) --------------
@@ -47,8 +48,9 @@ struct InduceSym {
 	using Problem = P3DInduceProblem;
 	using Consts = InduceConsts;
 	static constexpr int NC = InduceNC<VEL, DV>::value;
-	// fused, 1M cube: 4 -> 967, 8 -> 947, 2 -> 937 G/s; one output alone: 8
-	static constexpr int kUnroll = (VEL && DV) ? 4 : 8;
+	// 1M cube, G/s: fused 8 -> 1,079, 4 -> 1,068, 2 -> 1,055; velocity /
+	// stretching alone 8 -> 2,162 / 1,590, 4 -> 2,113 / 1,555, 16 -> 2,134 / 1,585
+	static constexpr int kUnroll = 8;
 	static constexpr int kRec = 2, kTile = kP3DTile, kMinBlocks = kP3DSymMinBlocks;
 	static constexpr double kPlanFactor = 26.0;
 	static constexpr bool kOwnDiagonal = true;
@@ -116,20 +118,21 @@ struct InduceSym {
 				K = make_float2(0.f, 0.f);
 			}
 			if (VEL) {
-				// t: G d x alpha_s; s: -G d x alpha_t
-				const float2 cx = __ffma2_rn(dy, wz, __fmul2_rn(dz, nwy));
-				const float2 cy = __ffma2_rn(dz, wx, __fmul2_rn(dx, nwz));
-				const float2 cz = __ffma2_rn(dx, wy, __fmul2_rn(dy, nwx));
-				acc[0][h] = __ffma2_rn(G, cx, acc[0][h]);
-				acc[1][h] = __ffma2_rn(G, cy, acc[1][h]);
-				acc[2][h] = __ffma2_rn(G, cz, acc[2][h]);
+				// e = G d, then t: e x alpha_s and s: alpha_t x e, the cross
+				// products' terms added one by one (no separate cross product
+				// per side: 1,859 -> 2,163 G/s for the velocity alone, 968 ->
+				// 1,068 fused, 1M cube; FP64 error 2.9e-7 -> 4.0e-7)
+				const float2 ex = __fmul2_rn(G, dx), ey = __fmul2_rn(G, dy), ez = __fmul2_rn(G, dz);
+				acc[0][h] = __ffma2_rn(ey, wz, __ffma2_rn(ez, nwy, acc[0][h]));
+				acc[1][h] = __ffma2_rn(ez, wx, __ffma2_rn(ex, nwz, acc[1][h]));
+				acc[2][h] = __ffma2_rn(ex, wy, __ffma2_rn(ey, nwx, acc[2][h]));
 				if (SYM) {
-					const float2 qx = __ffma2_rn(dy, g.az[h], __fmul2_rn(dz, g.nay[h]));
-					const float2 qy = __ffma2_rn(dz, g.ax[h], __fmul2_rn(dx, g.naz[h]));
-					const float2 qz = __ffma2_rn(dx, g.ay[h], __fmul2_rn(dy, g.nax[h]));
-					js[0] = fmaf(-G.x, qx.x, fmaf(-G.y, qx.y, js[0]));
-					js[1] = fmaf(-G.x, qy.x, fmaf(-G.y, qy.y, js[1]));
-					js[2] = fmaf(-G.x, qz.x, fmaf(-G.y, qz.y, js[2]));
+					js[0] = fmaf(g.ay[h].x, ez.x, fmaf(g.ay[h].y, ez.y,
+						fmaf(g.naz[h].x, ey.x, fmaf(g.naz[h].y, ey.y, js[0]))));
+					js[1] = fmaf(g.az[h].x, ex.x, fmaf(g.az[h].y, ex.y,
+						fmaf(g.nax[h].x, ez.x, fmaf(g.nax[h].y, ez.y, js[1]))));
+					js[2] = fmaf(g.ax[h].x, ey.x, fmaf(g.ax[h].y, ey.y,
+						fmaf(g.nay[h].x, ex.x, fmaf(g.nay[h].y, ex.y, js[2]))));
 				}
 			}
 			if (DV) {
