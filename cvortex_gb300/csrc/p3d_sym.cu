@@ -468,8 +468,8 @@ bool self_shape(const float4* src, int n_src, const float4* tgt, int tstride, in
 }  // namespace
 
 // Measured on a GB300 against the ordered-pair kernel (G interactions/s):
-// fused 967 against 866 (1M cube), stretching alone 1,464 against 1,010 and
-// velocity alone 1,770 against 1,698 (100,000-particle ring).
+// fused 1,079 against 866 (1M cube), stretching alone 1,523 against 1,010 and
+// velocity alone 2,110 against 1,722 (100,000-particle ring).
 bool p3d_self_form_applies(int reg, unsigned ops, const P3DInduceProblem& p) {
 	(void)reg;
 	(void)ops;
